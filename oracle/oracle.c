@@ -1,0 +1,527 @@
+/*
+ * oracle.c -- TEST INFRASTRUCTURE ONLY: the checker, never the product.
+ *
+ * Plain-C restatement of the reference CPU path of researchgroup-zx93920/flock
+ * (float arithmetic reproduced operation by operation) and an exact int64
+ * optimality-certificate checker.  See oracle.h for the contract; each
+ * function cites the reference lines it follows.  Built with
+ * -ffp-contract=off so that x86 and Arm give the same float results.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_EPSILON 0.000001f /* parallel_structs.h:34 (epsilon)            */
+#define ORC_EPSILON2 10e-3    /* parallel_structs.h:35 (epsilon2, a double) */
+
+/* float -> int as the x86 `cvttss2si` the reference was built and run with:
+ * truncation toward zero, and INT_MIN for NaN or anything outside
+ * [-2^31, 2^31).  The C cast is undefined there (and saturates on Arm), so
+ * it is spelled out.  This matters for a line with one uncovered crossing
+ * cell, whose penalty is float(2^31) - c (IBFS_vogel.cu:591-606). */
+static int32_t f2i_x86(float f) {
+    double x = (double)f;
+    if (x != x || x >= 2147483648.0 || x < -2147483648.0) return INT32_MIN;
+    return (int32_t)x;
+}
+
+/* Flows from `from` on are undefined in the reference (it indexes past its
+ * arrays); they are written as (-1, -1, 0). */
+static void fill_undefined(int32_t* src, int32_t* dst, float* qty, int from, int to) {
+    for (int k = from; k < to; k++) { src[k] = -1; dst[k] = -1; qty[k] = 0.0f; }
+}
+
+/* IBFS_vogel.cu:546-769, find_vogel_bfs_sequencial. */
+int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
+              int32_t* src, int32_t* dst, float* qty) {
+    const int V = m + n;
+    int32_t* rs = (int32_t*)malloc(sizeof(int32_t) * (size_t)m);
+    int32_t* rd = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* rowCov = (int32_t*)calloc((size_t)m, sizeof(int32_t));
+    int32_t* colCov = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+    int32_t* diff = (int32_t*)calloc((size_t)V, sizeof(int32_t));
+    memcpy(rs, s, sizeof(int32_t) * (size_t)m);
+    memcpy(rd, d, sizeof(int32_t) * (size_t)n);
+    int coveredRows = 0, coveredCols = 0;
+    int prev_row = 1, prev_col = 1;
+    /* The reference declares its min-cost index inside the loop without an
+     * initialiser; when the chosen line has no uncovered crossing cell the
+     * index keeps the previous step's value.  That is reproduced here (the
+     * variable lives outside the loop) and counted. */
+    int i_minCost = 0;
+    int events = 0;
+    const float FMAX = (float)2147483647; /* INT_MAX converted: 2^31 */
+
+    while (coveredRows + coveredCols < V - 1) {
+        if (prev_row) { /* :588-613 */
+            for (int i = 0; i < m; i++) {
+                if (rowCov[i] == 0) {
+                    float t1 = FMAX, t2 = FMAX;
+                    for (int j = 0; j < n; j++) {
+                        if (colCov[j] == 0) {
+                            float e = c[(size_t)i * n + j];
+                            if (e <= t1) { t2 = t1; t1 = e; }
+                            else if (e <= t2) { t2 = e; }
+                        }
+                    }
+                    diff[i] = f2i_x86(t2 - t1);
+                } else {
+                    diff[i] = -1;
+                }
+            }
+            prev_row = 0;
+        }
+        if (prev_col) { /* :616-642 */
+            for (int j = 0; j < n; j++) {
+                if (colCov[j] == 0) {
+                    float t1 = FMAX, t2 = FMAX;
+                    for (int i = 0; i < m; i++) {
+                        if (rowCov[i] == 0) {
+                            float e = c[(size_t)i * n + j];
+                            if (e <= t1) { t2 = t1; t1 = e; }
+                            else if (e <= t2) { t2 = e; }
+                        }
+                    }
+                    diff[m + j] = f2i_x86(t2 - t1);
+                } else {
+                    diff[m + j] = -1;
+                }
+            }
+            prev_col = 0;
+        }
+        /* :651-659 -- compared as float, ties to the LAST index */
+        float tempDiff = (float)INT32_MIN;
+        int sel = -1;
+        for (int k = 0; k < V; k++) {
+            if ((float)diff[k] >= tempDiff) { tempDiff = (float)diff[k]; sel = k; }
+        }
+        int counter = coveredRows + coveredCols;
+        int row, col;
+        float q;
+        if (sel >= m) { /* column branch :666-714 */
+            col = sel - m;
+            float ct = FMAX;
+            int found = 0;
+            for (int i = 0; i < m; i++) {
+                float e = c[(size_t)i * n + col];
+                if (e < ct && rowCov[i] == 0) { ct = e; i_minCost = i; found = 1; }
+            }
+            if (!found) events++;
+            row = i_minCost;
+            if (row < 0 || row >= m) { events = -1; fill_undefined(src, dst, qty, counter, V - 1); break; }
+            if (rd[col] > rs[row]) {
+                q = 1.0f * rs[row];
+                rd[col] -= rs[row]; rs[row] = 0; rowCov[row] = 1; prev_row = 1; coveredRows += 1;
+            } else {
+                q = 1.0f * rd[col];
+                rs[row] -= rd[col]; rd[col] = 0; colCov[col] = 1; prev_col = 1; coveredCols += 1;
+            }
+        } else { /* row branch :716-762 */
+            row = sel;
+            float ct = FMAX;
+            int found = 0;
+            for (int j = 0; j < n; j++) {
+                float e = c[(size_t)row * n + j];
+                if (e < ct && colCov[j] == 0) { ct = e; i_minCost = j; found = 1; }
+            }
+            if (!found) events++;
+            col = i_minCost;
+            if (col < 0 || col >= n) { events = -1; fill_undefined(src, dst, qty, counter, V - 1); break; }
+            if (rd[col] > rs[row]) {
+                q = fmaxf(1.0f * rs[row], ORC_EPSILON);
+                rd[col] -= rs[row]; rs[row] = 0; rowCov[row] = 1; prev_row = 1; coveredRows += 1;
+            } else {
+                q = fmaxf(1.0f * rd[col], ORC_EPSILON);
+                rs[row] -= rd[col]; rd[col] = 0; colCov[col] = 1; prev_col = 1; coveredCols += 1;
+            }
+        }
+        src[counter] = row;
+        dst[counter] = col;
+        qty[counter] = q;
+    }
+    free(rs); free(rd); free(rowCov); free(colCov); free(diff);
+    return events;
+}
+
+/* IBFS_nwc.cu:3-33 (reads one element past the end only after the last
+ * allocation; the restatement stops first). */
+int orc_nwc(int m, int n, const int32_t* s, const int32_t* d,
+            int32_t* src, int32_t* dst, float* qty) {
+    int r = 0, k = 0, cnt = 0;
+    int32_t cd = d[0], cs = s[0];
+    while (r < m && k < n) {
+        if (cd >= cs) {
+            src[cnt] = r; dst[cnt] = k; qty[cnt] = fmaxf(1.0f * cs, ORC_EPSILON);
+            cd -= cs; r++; cs = (r < m) ? s[r] : 0;
+        } else {
+            src[cnt] = r; dst[cnt] = k; qty[cnt] = fmaxf(1.0f * cd, ORC_EPSILON);
+            cs -= cd; k++; cd = (k < n) ? d[k] : 0;
+        }
+        cnt++;
+    }
+    return cnt;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Reference CPU path: uv_model_parallel.cu:227-395 with
+ *   BFS_METHOD "vam_host", REDUCED_COST_MODE "sequencial",
+ *   CALCULATE_DUAL "host_bfs", SEQ_CYCLE_SEARCH "dfs".
+ * The basis is kept as m+n-1 flow slots with a cell->slot map, exactly the
+ * reference's TREE_LOOKUP adjacency matrix + flowMtx (parallel_kernels.cu:
+ * 46-67): a later slot on the same cell replaces the earlier one.  Adjacency
+ * lists are kept like the reference's h_Graph: initially in ascending
+ * neighbour order, then erase + push_back per pivot (PIVOT_uv.cu:248-258).
+ * The order only matters when the basis is not a tree (Vogel can return a
+ * cycle plus a separate component on degenerate input); the reference's own
+ * initial order there is the GPU atomic order, and ascending order is the
+ * one its host driver in oracle/_ref uses.                                  */
+
+typedef struct {
+    int32_t* a;
+    int32_t len, cap;
+} orc_list;
+
+static void list_push(orc_list* l, int32_t x) {
+    if (l->len == l->cap) {
+        l->cap = l->cap ? 2 * l->cap : 4;
+        l->a = (int32_t*)realloc(l->a, sizeof(int32_t) * (size_t)l->cap);
+    }
+    l->a[l->len++] = x;
+}
+
+static void list_erase_all(orc_list* l, int32_t x) {
+    int w = 0;
+    for (int r = 0; r < l->len; r++) if (l->a[r] != x) l->a[w++] = l->a[r];
+    l->len = w;
+}
+
+typedef struct { int32_t index, depth; } orc_stack_node;
+
+/* TREE_LOOKUP(a, b) -> flow slot (parallel_structs.h:93); -1 if not basic. */
+static int slot_of_cell(const int32_t* cell_slot, int m, int n, int a, int b) {
+    int r = a < b ? a : b;
+    int k = (a < b ? b : a) - m;
+    if (r < 0 || r >= m || k < 0 || k >= n) return -1;
+    return cell_slot[(size_t)r * n + k];
+}
+
+static int cmp_i64(const void* a, const void* b) {
+    int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
+    return (x > y) - (x < y);
+}
+
+int orc_solve_ref(int m, int n, const int32_t* s, const int32_t* d, const float* c,
+                  int bfs_method, int max_iter,
+                  int32_t* fsrc, int32_t* fdst, float* fqty,
+                  int32_t* tree_src, int32_t* tree_dst, orc_result* out) {
+    const int V = m + n;
+    int32_t* slot_row = (int32_t*)malloc(sizeof(int32_t) * (size_t)V);
+    int32_t* slot_col = (int32_t*)malloc(sizeof(int32_t) * (size_t)V);
+    float* flow = (float*)malloc(sizeof(float) * (size_t)V);
+    int32_t* cell_slot = (int32_t*)malloc(sizeof(int32_t) * (size_t)m * n);
+    orc_list* adj = (orc_list*)calloc((size_t)V, sizeof(orc_list));
+    float* h = (float*)malloc(sizeof(float) * (size_t)V);
+    char* vis = (char*)malloc((size_t)V);
+    int32_t* queue = (int32_t*)malloc(sizeof(int32_t) * (size_t)V);
+    int32_t* bt = (int32_t*)malloc(sizeof(int32_t) * (size_t)(V + 2));
+    size_t stack_cap = (size_t)(2 * V + 4);
+    orc_stack_node* stack = (orc_stack_node*)malloc(sizeof(orc_stack_node) * stack_cap);
+    for (size_t x = 0; x < (size_t)m * n; x++) cell_slot[x] = -1;
+
+    float* q0 = (float*)malloc(sizeof(float) * (size_t)V);
+    int ev = 0;
+    if (bfs_method == 0) orc_nwc(m, n, s, d, slot_row, slot_col, q0);
+    else ev = orc_vogel(m, n, s, d, c, slot_row, slot_col, q0);
+    if (ev < 0) {
+        /* The reference's run is undefined from here on (out-of-range index). */
+        if (out) { out->iterations = 0; out->status = 3; out->active_flows = 0;
+                   out->vogel_events = ev; out->objective = 0.0; }
+        free(q0); free(slot_row); free(slot_col); free(flow); free(cell_slot); free(adj);
+        free(h); free(vis); free(queue); free(bt); free(stack);
+        return 0;
+    }
+    /* parallel_kernels.cu:53-66: zero flow -> epsilon */
+    for (int g = 0; g < V - 1; g++) {
+        float qq = 1.0f * q0[g];
+        if (qq == 0) qq = ORC_EPSILON;
+        flow[g] = qq;
+        cell_slot[(size_t)slot_row[g] * n + slot_col[g]] = g;
+    }
+    free(q0);
+    {   /* initial adjacency in ascending neighbour order */
+        int64_t* cells = (int64_t*)malloc(sizeof(int64_t) * (size_t)V);
+        int k = 0;
+        for (int g = 0; g < V - 1; g++) {
+            int64_t cell = (int64_t)slot_row[g] * n + slot_col[g];
+            if (cell_slot[cell] == g) cells[k++] = cell;
+        }
+        qsort(cells, (size_t)k, sizeof(int64_t), cmp_i64);
+        for (int e = 0; e < k; e++) {
+            int r = (int)(cells[e] / n), col = (int)(cells[e] % n);
+            list_push(&adj[r], m + col);
+        }
+        /* columns: rows ascending -> iterate cells column-major */
+        for (int col = 0; col < n; col++)
+            for (int r = 0; r < m; r++)
+                if (cell_slot[(size_t)r * n + col] >= 0) list_push(&adj[m + col], r);
+        free(cells);
+    }
+
+    int it = 0, status = 2, done = 0;
+    while (!done && it < max_iter) {
+        /* DUAL_solver.cu:34-63 */
+        for (int v = 0; v < V; v++) { h[v] = 0.0f; vis[v] = 0; }
+        {
+            int qh = 0, qt = 0;
+            vis[0] = 1;
+            queue[qt++] = 0;
+            while (qh < qt) {
+                int p = queue[qh++];
+                for (int e = 0; e < adj[p].len; e++) {
+                    int ch = adj[p].a[e];
+                    if (!vis[ch]) {
+                        vis[ch] = 1;
+                        int row = p < ch ? p : ch;
+                        int col = (p < ch ? ch : p) - m;
+                        h[ch] = c[(size_t)row * n + col] - h[p];
+                        queue[qt++] = ch;
+                    }
+                }
+            }
+        }
+        /* uv_model_parallel.cu:178-200 */
+        float min_r = (float)2147483647;
+        int pr = -1, pc = -1;
+        for (int i = 0; i < m; i++) {
+            const float* ci = c + (size_t)i * n;
+            float ui = h[i];
+            for (int j = 0; j < n; j++) {
+                float r = ci[j] - ui - h[m + j];
+                if (r < min_r) { min_r = r; pr = i; pc = j; }
+            }
+        }
+        /* PIVOT_uv.cu:318-401 */
+        if (min_r < 0 && (double)fabsf(min_r) > ORC_EPSILON2) {
+            /* PIVOT_uv.cu:156-209 (DFS from column vertex m+pc to row pr) */
+            int depth = 1;
+            {
+                for (int v = 0; v < V; v++) vis[v] = 0;
+                int top = -1;
+                stack[++top] = (orc_stack_node){m + pc, 1};
+                while (top != -1) {
+                    orc_stack_node cv = stack[top--];
+                    if (!vis[cv.index]) {
+                        vis[cv.index] = 1;
+                        int cur_depth = cv.depth + 1;
+                        bt[cv.depth] = cv.index;
+                        int adjacent = 0;
+                        if (cv.index >= m && cell_slot[(size_t)pr * n + (cv.index - m)] >= 0) adjacent = 1;
+                        if (adjacent && cur_depth > 1) { depth = cur_depth; break; }
+                        for (int e = 0; e < adj[cv.index].len; e++) {
+                            if ((size_t)(top + 1) >= stack_cap) {
+                                stack_cap *= 2;
+                                stack = (orc_stack_node*)realloc(stack, sizeof(orc_stack_node) * stack_cap);
+                            }
+                            stack[++top] = (orc_stack_node){adj[cv.index].a[e], cur_depth};
+                        }
+                    }
+                    if (top == -1) depth = 1;
+                }
+            }
+            if (depth <= 1) { status = 1; done = 1; it++; break; }
+            bt[0] = pr;
+            bt[depth] = pr;
+            float min_flow = (float)2147483647;
+            int min_slot = -1, min_from = -1, min_to = -1;
+            for (int i = 1; i < depth; i += 2) { /* PIVOT_uv.cu:280-296 */
+                int a = bt[i], b = bt[i + 1];
+                int g = slot_of_cell(cell_slot, m, n, a, b);
+                float f = flow[g];
+                if (f < min_flow) { min_flow = f; min_slot = g; min_from = a; min_to = b; }
+            }
+            for (int i = 1; i < depth; i++) { /* PIVOT_uv.cu:236-244 */
+                int g = slot_of_cell(cell_slot, m, n, bt[i], bt[i + 1]);
+                float fl = (float)((i % 2) ? -1 : 1) * min_flow;
+                flow[g] += fl;
+            }
+            /* PIVOT_uv.cu:248-261 */
+            {
+                int r = min_from < min_to ? min_from : min_to;
+                int k = (min_from < min_to ? min_to : min_from) - m;
+                cell_slot[(size_t)r * n + k] = -1;
+                list_erase_all(&adj[min_to], min_from);
+                list_erase_all(&adj[min_from], min_to);
+            }
+            cell_slot[(size_t)pr * n + pc] = min_slot;
+            list_push(&adj[pr], m + pc);
+            list_push(&adj[m + pc], pr);
+            slot_row[min_slot] = pr;
+            slot_col[min_slot] = pc;
+            flow[min_slot] = min_flow;
+        } else {
+            status = 0;
+            done = 1;
+        }
+        it++;
+    }
+
+    /* parallel_kernels.cu:72-96,154-181 and uv_model_parallel.cu:375-385 */
+    int cnt = 0;
+    double obj = 0.0;
+    int tk = 0;
+    for (int g = 0; g < V - 1; g++) {
+        int r = slot_row[g], k = slot_col[g];
+        if (cell_slot[(size_t)r * n + k] != g) continue;
+        if (tree_src) { tree_src[tk] = r; tree_dst[tk] = k; }
+        tk++;
+        float q = roundf(flow[g]);
+        if (q == 0) continue;
+        if (fsrc) { fsrc[cnt] = r; fdst[cnt] = k; fqty[cnt] = q; }
+        float prod = q * c[(size_t)r * n + k];
+        obj += prod;
+        cnt++;
+    }
+    if (tree_src) for (; tk < V - 1; tk++) { tree_src[tk] = -1; tree_dst[tk] = -1; }
+    if (out) {
+        out->iterations = it;
+        out->status = status;
+        out->active_flows = cnt;
+        out->vogel_events = ev;
+        out->objective = obj;
+    }
+    for (int v = 0; v < V; v++) free(adj[v].a);
+    free(adj); free(slot_row); free(slot_col); free(flow); free(cell_slot);
+    free(h); free(vis); free(queue); free(bt); free(stack);
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+typedef struct {
+    int count;
+    const int32_t *ms, *ns;
+    const int64_t *s_off, *d_off, *c_off;
+    const int32_t *s, *d;
+    const float* c;
+    int bfs_method, max_iter;
+    double* objective;
+    int32_t *iterations, *status;
+    int next;
+    pthread_mutex_t mu;
+} batch_job;
+
+static void* batch_worker(void* arg) {
+    batch_job* job = (batch_job*)arg;
+    for (;;) {
+        pthread_mutex_lock(&job->mu);
+        int k = job->next++;
+        pthread_mutex_unlock(&job->mu);
+        if (k >= job->count) break;
+        orc_result r;
+        orc_solve_ref(job->ms[k], job->ns[k], job->s + job->s_off[k], job->d + job->d_off[k],
+                      job->c + job->c_off[k], job->bfs_method, job->max_iter,
+                      NULL, NULL, NULL, NULL, NULL, &r);
+        job->objective[k] = r.objective;
+        job->iterations[k] = r.iterations;
+        job->status[k] = r.status;
+    }
+    return NULL;
+}
+
+int orc_solve_ref_batch(int count, const int32_t* ms, const int32_t* ns,
+                        const int64_t* s_off, const int64_t* d_off, const int64_t* c_off,
+                        const int32_t* s, const int32_t* d, const float* c,
+                        int bfs_method, int max_iter, int nthreads,
+                        double* objective, int32_t* iterations, int32_t* status) {
+    batch_job job;
+    job.count = count; job.ms = ms; job.ns = ns;
+    job.s_off = s_off; job.d_off = d_off; job.c_off = c_off;
+    job.s = s; job.d = d; job.c = c;
+    job.bfs_method = bfs_method; job.max_iter = max_iter;
+    job.objective = objective; job.iterations = iterations; job.status = status;
+    job.next = 0;
+    pthread_mutex_init(&job.mu, NULL);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, batch_worker, &job);
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(th);
+    pthread_mutex_destroy(&job.mu);
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+int orc_tree_duals(int m, int n, const int32_t* c, int32_t k,
+                   const int32_t* tsrc, const int32_t* tdst, int64_t* u, int64_t* v) {
+    const int V = m + n;
+    int32_t* deg = (int32_t*)calloc((size_t)V + 1, sizeof(int32_t));
+    int32_t* start = (int32_t*)malloc(sizeof(int32_t) * ((size_t)V + 1));
+    int32_t* nbr = (int32_t*)malloc(sizeof(int32_t) * (size_t)(2 * (k + 1)));
+    int32_t* seen = (int32_t*)calloc((size_t)V, sizeof(int32_t));
+    int64_t* pot = (int64_t*)calloc((size_t)V, sizeof(int64_t));
+    int32_t* queue = (int32_t*)malloc(sizeof(int32_t) * (size_t)V);
+    int ok = 0;
+    for (int e = 0; e < k; e++) {
+        if (tsrc[e] < 0 || tsrc[e] >= m || tdst[e] < 0 || tdst[e] >= n) { ok = -1; break; }
+        deg[tsrc[e]]++; deg[m + tdst[e]]++;
+    }
+    if (ok == 0) {
+        start[0] = 0;
+        for (int x = 0; x < V; x++) start[x + 1] = start[x] + deg[x];
+        memset(deg, 0, sizeof(int32_t) * (size_t)V);
+        for (int e = 0; e < k; e++) {
+            int a = tsrc[e], b = m + tdst[e];
+            nbr[start[a] + deg[a]++] = b;
+            nbr[start[b] + deg[b]++] = a;
+        }
+        int qh = 0, qt = 0;
+        queue[qt++] = 0; seen[0] = 1; pot[0] = 0;
+        while (qh < qt) {
+            int p = queue[qh++];
+            for (int e = start[p]; e < start[p + 1]; e++) {
+                int ch = nbr[e];
+                if (!seen[ch]) {
+                    seen[ch] = 1;
+                    int row = p < ch ? p : ch, col = (p < ch ? ch : p) - m;
+                    pot[ch] = (int64_t)c[(size_t)row * n + col] - pot[p];
+                    queue[qt++] = ch;
+                }
+            }
+        }
+        if (qt != V || k != V - 1) ok = -1;
+        for (int i = 0; i < m; i++) u[i] = pot[i];
+        for (int j = 0; j < n; j++) v[j] = pot[m + j];
+    }
+    free(deg); free(start); free(nbr); free(seen); free(pot); free(queue);
+    return ok;
+}
+
+int orc_certify(int m, int n, const int32_t* s, const int32_t* d, const int32_t* c,
+                int32_t k, const int32_t* fsrc, const int32_t* fdst, const int64_t* fqty,
+                const int64_t* u, const int64_t* v, int64_t* objective) {
+    int bad = 0;
+    int64_t* rs = (int64_t*)calloc((size_t)m, sizeof(int64_t));
+    int64_t* cs = (int64_t*)calloc((size_t)n, sizeof(int64_t));
+    int64_t obj = 0;
+    for (int e = 0; e < k; e++) {
+        int i = fsrc[e], j = fdst[e];
+        if (i < 0 || i >= m || j < 0 || j >= n || fqty[e] < 0) { bad |= 1; continue; }
+        rs[i] += fqty[e];
+        cs[j] += fqty[e];
+        obj += fqty[e] * (int64_t)c[(size_t)i * n + j];
+        if (fqty[e] > 0 && (int64_t)c[(size_t)i * n + j] - u[i] - v[j] != 0) bad |= 16;
+    }
+    for (int i = 0; i < m; i++) if (rs[i] != s[i]) bad |= 2;
+    for (int j = 0; j < n; j++) if (cs[j] != d[j]) bad |= 4;
+    for (int i = 0; i < m && !(bad & 8); i++) {
+        const int32_t* ci = c + (size_t)i * n;
+        for (int j = 0; j < n; j++) {
+            if ((int64_t)ci[j] - u[i] - v[j] < 0) { bad |= 8; break; }
+        }
+    }
+    if (objective) *objective = obj;
+    free(rs); free(cs);
+    return bad;
+}
