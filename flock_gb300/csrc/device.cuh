@@ -1,0 +1,208 @@
+// device.cuh -- CTA-level building blocks of the transportation simplex.
+//
+// Every function here is executed by ALL threads of one CTA (block-uniform
+// control flow; they synchronise internally).  The same functions serve the
+// plain single-instance path (one CTA for the tree phases, a grid-wide sweep)
+// and the batched persistent kernel (one CTA per instance, work stealing).
+// Arrays are reached through generic pointers so one code path serves both
+// placements: shared memory for small instances, global memory otherwise.
+//
+// Vertex numbering: rows (supplies) 0..m-1, columns (demands) m..m+n-1.
+// Tree edges are identified by their child vertex; the edge of a row child
+// r with parent column p is cell (r, p-m); of a column child c with parent
+// row p, cell (p, c-m).  Arc direction is always row -> column.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace flock {
+
+// ---------------------------------------------------------------- status ---
+enum : int32_t {
+    ST_ITER_CAP = 1,          // pricing-round cap reached before optimality
+    ST_TREE_CORRUPT = 2,      // a tree walk or the dual recompute did not terminate
+    ST_SF_FAIL = 4,           // perturbed initial flow not positive (internal)
+    ST_VOGEL_UNDEF = 8,       // Vogel hit the reference's out-of-range index case
+    ST_START_REPAIRED = 16,   // Vogel flows not a feasible forest: simplex starts from NW corner
+    ST_CERT_FAIL = 32,        // certificate check failed
+    ST_RANGE = 64,            // perturbed flows would overflow int64
+};
+
+constexpr int64_t kDeadPot = -(int64_t(1) << 61);   // dual of a zero-demand column during pivoting
+constexpr uint64_t kNoKey = ~0ull;
+
+struct Scalars {
+    int32_t status;
+    int32_t done;          // 1: optimal or stopped; later kernels return at once
+    int32_t rounds;        // pricing rounds (full sweeps)
+    int32_t pivots;        // pivots applied
+    int32_t root;          // root column vertex
+    int32_t v_alive;       // vertices in the pivoting tree
+    int32_t events;        // Vogel events (see vogel_cta), -1: undefined case
+    int32_t active;        // nonzero flows in the result
+    int32_t cert;          // certificate failure bits (0: optimal)
+    int32_t max_rounds;
+    int32_t mode;          // 0 sequential (one pivot / round), 1 parallel multi-pivot
+    int32_t ncand;         // candidates in the last round
+    int64_t objective;
+    int64_t M;             // perturbation scale
+    int64_t neg_cells;     // certificate: cells with negative reduced cost
+    int32_t last_winners;
+    int32_t pad;
+};
+
+// One instance as the kernels see it.
+struct InstDev {
+    int32_t m, n, ldc;        // rows, columns, padded row pitch (multiple of 4)
+    const int32_t* cost;      // m x ldc, row-major
+    const int32_t* supply;    // m
+    const int32_t* demand;    // n
+};
+
+// Per-instance working set.  Pointers may refer to shared or global memory.
+struct Ctx {
+    InstDev I;
+    Scalars* sc;
+    // allocation list of the initial solution (Vogel or NW corner), V-1
+    int32_t* bfs_src; int32_t* bfs_dst; int32_t* bfs_qty;
+    // final basis, V-1 cells with original quantities
+    int32_t* out_src; int32_t* out_dst; int32_t* out_qty;
+    // tree
+    int32_t* parent;   // V  (-1 root, -2 not in tree)
+    int64_t* flow;     // V  perturbed flow on the edge to the parent
+    int32_t* depth;    // V
+    int64_t* pot;      // V  duals: u_i (rows), v_j (columns)
+    // pointer-jumping scratch (double buffered)
+    int32_t* anc0; int32_t* anc1; int32_t* len0; int32_t* len1; int64_t* acc0; int64_t* acc1;
+    // pricing
+    uint64_t* row_best;   // m   packed (reduced cost, column) of the best cell per row
+    uint64_t* claim;      // V   edge claims
+    int32_t* cand;        // m   candidate rows
+    int64_t* cand_theta;  // m
+    int32_t* cand_q;      // m   leaving edge (child vertex)
+    int32_t* cand_info;   // m   bit0: leaving edge on the column side; bit1: winner
+    // Vogel scratch
+    uint8_t* covered;     // V
+    int32_t* diff;        // V
+    int32_t* res;         // V  residual supply (rows) / demand (columns)
+    int4* top2;           // V  (c1, c2, j1, j2) two cheapest uncovered crossing cells
+    int32_t* rescan;      // V  list of lines whose top2 must be rebuilt
+    // start-tree scratch
+    int64_t* bsum;        // V
+    int32_t* csr_start;   // V+1
+    int32_t* csr_adj;     // 2V
+    int32_t* order;       // V  (BFS order of the start tree)
+    int32_t* uf;          // V  union-find
+};
+
+// --------------------------------------------------------------- helpers ---
+__device__ __forceinline__ int32_t f2i_x86(float f) {
+    // float -> int as x86 cvttss2si: truncation, INT_MIN for NaN/out of range.
+    if (!(f < 2147483648.0f) || !(f >= -2147483648.0f)) return INT32_MIN;
+    return __float2int_rz(f);
+}
+
+// Packed (value, index) keys: unsigned order == (value, index) order.
+__device__ __forceinline__ uint64_t pack_i32(int32_t v, uint32_t idx) {
+    return ((uint64_t)((uint32_t)v ^ 0x80000000u) << 32) | idx;
+}
+__device__ __forceinline__ int32_t key_val(uint64_t k) { return (int32_t)((uint32_t)(k >> 32) ^ 0x80000000u); }
+__device__ __forceinline__ uint32_t key_idx(uint64_t k) { return (uint32_t)k; }
+__device__ __forceinline__ int32_t clamp32(int64_t r) {
+    return r < INT32_MIN ? INT32_MIN : (r > INT32_MAX ? INT32_MAX : (int32_t)r);
+}
+
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { uint64_t w = __shfl_xor_sync(0xffffffffu, v, o); v = w < v ? w : v; }
+    return v;
+}
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { uint64_t w = __shfl_xor_sync(0xffffffffu, v, o); v = w > v ? w : v; }
+    return v;
+}
+__device__ __forceinline__ int64_t warp_sum_i64(int64_t v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Shared scratch for block reductions (one slot per warp, at most 32 warps).
+struct BlockScratch {
+    uint64_t red[32];
+    uint64_t red2[32];
+    int32_t i[8];
+};
+
+__device__ __forceinline__ uint64_t block_min_u64(uint64_t v, BlockScratch& bs) {
+    v = warp_min_u64(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) bs.red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t x = l < nw ? bs.red[l] : kNoKey;
+        x = warp_min_u64(x);
+        if (l == 0) bs.red[0] = x;
+    }
+    __syncthreads();
+    return bs.red[0];
+}
+__device__ __forceinline__ uint64_t block_max_u64(uint64_t v, BlockScratch& bs) {
+    v = warp_max_u64(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) bs.red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t x = l < nw ? bs.red[l] : 0ull;
+        x = warp_max_u64(x);
+        if (l == 0) bs.red[0] = x;
+    }
+    __syncthreads();
+    return bs.red[0];
+}
+__device__ __forceinline__ int64_t block_sum_i64(int64_t v, BlockScratch& bs) {
+    v = warp_sum_i64(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) bs.red[w] = (uint64_t)v;
+    __syncthreads();
+    if (w == 0) {
+        int64_t x = l < nw ? (int64_t)bs.red[l] : 0;
+        x = warp_sum_i64(x);
+        if (l == 0) bs.red[0] = (uint64_t)x;
+    }
+    __syncthreads();
+    return (int64_t)bs.red[0];
+}
+
+// Two smallest keys: insert / merge.
+__device__ __forceinline__ void top2_insert(uint64_t& a1, uint64_t& a2, uint64_t k) {
+    if (k < a1) { a2 = a1; a1 = k; } else if (k < a2) { a2 = k; }
+}
+__device__ __forceinline__ void top2_merge(uint64_t& a1, uint64_t& a2, uint64_t b1, uint64_t b2) {
+    uint64_t f, s;
+    if (a1 < b1) { f = a1; s = a2 < b1 ? a2 : b1; }
+    else         { f = b1; s = a1 < b2 ? a1 : b2; }
+    a1 = f; a2 = s;
+}
+__device__ __forceinline__ void warp_top2(uint64_t& a1, uint64_t& a2) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        uint64_t b1 = __shfl_xor_sync(0xffffffffu, a1, o);
+        uint64_t b2 = __shfl_xor_sync(0xffffffffu, a2, o);
+        top2_merge(a1, a2, b1, b2);
+    }
+}
+
+__device__ __forceinline__ int32_t cost_of(const InstDev& I, int row, int col) {
+    return I.cost[(size_t)row * I.ldc + col];
+}
+// cost of the tree edge whose child is v with parent p
+__device__ __forceinline__ int32_t edge_cost(const InstDev& I, int v, int p) {
+    return v < I.m ? cost_of(I, v, p - I.m) : cost_of(I, p, v - I.m);
+}
+
+}  // namespace flock

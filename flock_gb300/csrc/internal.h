@@ -1,0 +1,95 @@
+// internal.h -- layout of the per-instance working set and the batched-kernel
+// arguments, shared by host and device code.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "device.cuh"
+
+namespace flock {
+
+struct BatchDesc {
+    int32_t m, n, ldc, index;   // index: position in the caller's instance list
+    int64_t cost_off;           // into the cost arena (elements)
+    int64_t sd_off;             // supply at sd_off, demand at sd_off + m
+    int64_t out_off;            // first basis cell in the output arena
+    int64_t pot_off;            // first dual in the dual arena
+};
+
+struct BatchArgs {
+    const BatchDesc* desc;
+    int32_t count;
+    int32_t* next;              // work-stealing counter
+    const int32_t* cost;
+    const int32_t* sd;
+    int32_t* out_src; int32_t* out_dst; int32_t* out_qty;
+    int32_t* bfs_out;           // 3 ints per cell: Vogel / NW-corner allocation list
+    int64_t* pot_out;
+    Scalars* sc;
+    uint8_t* scratch;           // per-CTA global scratch
+    size_t scratch_per_cta;
+    int32_t maxV, maxM;
+    int32_t smem_mode;
+    int32_t bfs_method, mode, max_rounds;
+};
+
+struct Carver {
+    uint8_t* g; size_t go;
+    unsigned char* s; size_t so;
+    __host__ __device__ void* G(size_t bytes) {
+        go = (go + 255) & ~size_t(255);
+        void* p = g ? (void*)(g + go) : nullptr;
+        go += bytes;
+        return p;
+    }
+    __host__ __device__ void* S(size_t bytes) {
+        if (!s) return G(bytes);
+        so = (so + 15) & ~size_t(15);
+        void* p = (void*)(s + so);
+        so += bytes;
+        return p;
+    }
+};
+
+// Assign every working array of `c` for instances with at most V vertices and
+// M rows.  With `smem` the arrays touched by every pivot step live in shared
+// memory, the rest in the global region `g`.  Returns the bytes used in both.
+__host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsigned char* smem,
+                                          int64_t* pot_global, size_t* smem_bytes = nullptr,
+                                          size_t* global_bytes = nullptr) {
+    Carver k{g, 0, smem, 0};
+    const size_t v = (size_t)V, mm = (size_t)M;
+    c.parent = (int32_t*)k.S(4 * v);
+    c.depth = (int32_t*)k.S(4 * v);
+    c.flow = (int64_t*)k.S(8 * v);
+    c.claim = (uint64_t*)k.S(8 * v);
+    c.anc0 = (int32_t*)k.S(4 * v);
+    c.anc1 = (int32_t*)k.S(4 * v);
+    c.len0 = (int32_t*)k.S(4 * v);
+    c.len1 = (int32_t*)k.S(4 * v);
+    c.acc0 = (int64_t*)k.S(8 * v);
+    c.acc1 = (int64_t*)k.S(8 * v);
+    c.row_best = (uint64_t*)k.S(8 * mm);
+    c.pot = smem ? (int64_t*)k.S(8 * v) : (pot_global ? pot_global : (int64_t*)k.G(8 * v));
+    c.bfs_src = (int32_t*)k.G(4 * v);
+    c.bfs_dst = (int32_t*)k.G(4 * v);
+    c.bfs_qty = (int32_t*)k.G(4 * v);
+    c.cand = (int32_t*)k.G(4 * mm);
+    c.cand_theta = (int64_t*)k.G(8 * mm);
+    c.cand_q = (int32_t*)k.G(4 * mm);
+    c.cand_info = (int32_t*)k.G(4 * mm);
+    c.covered = (uint8_t*)k.G(v);
+    c.diff = (int32_t*)k.G(4 * v);
+    c.res = (int32_t*)k.G(4 * v);
+    c.top2 = (int4*)k.G(16 * v);
+    c.rescan = (int32_t*)k.G(4 * v);
+    c.bsum = (int64_t*)k.G(8 * v);
+    c.csr_start = (int32_t*)k.G(4 * (v + 1));
+    c.csr_adj = (int32_t*)k.G(8 * v);
+    c.order = (int32_t*)k.G(4 * v);
+    c.uf = (int32_t*)k.G(4 * v);
+    if (smem_bytes) *smem_bytes = k.so;
+    if (global_bytes) *global_bytes = (k.go + 255) & ~size_t(255);
+}
+
+}  // namespace flock

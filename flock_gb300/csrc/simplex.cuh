@@ -1,0 +1,556 @@
+// simplex.cuh -- exact int64 transportation simplex on a rooted basis tree.
+//
+// Reference path being replaced: the u-v method of uvModel_parallel::execute
+// (src/parallel_simplex_method/parallel_uv_method/uv_model_parallel.cu:227-395)
+// and the parallel stepping-stone round of SS_METHOD::perform_a_parallel_pivot
+// (src/parallel_simplex_method/parallel_ss_method/PIVOT_ss.cu:294-454).
+//
+// Design (all integer, no floating point):
+//  * The tree is rooted at a column rho and stored as parent[], depth[] and
+//    flow[] (flow on the edge to the parent).  Duals pot[] satisfy
+//    u_i + v_j = c_ij on tree edges with v_rho = 0.
+//  * Anti-cycling: pivoting runs on the perturbed right-hand side
+//    s'_i = M s_i + 1, d'_j = M d_j - 1 (j != rho), d'_rho = M d_rho + V'-1,
+//    M = 2V'+1.  Every basis of this problem is nondegenerate, so each pivot
+//    strictly lowers the perturbed objective and no basis repeats (this is
+//    Cunningham's strongly feasible tree rule in exact arithmetic).  The
+//    original flows are recovered as round(flow / M) at the end.
+//  * The start tree keeps every positive flow of the initial solution (Vogel
+//    or NW corner) and re-chooses the zero-flow basic cells so that the tree
+//    is strongly feasible (each non-root column has a positive edge to its
+//    parent).  Zero-demand columns can carry no flow and are kept out of the
+//    pivoting tree; they are attached at the end with v_j = min_i c_ij - u_i.
+//  * A round: duals by pointer jumping (O(log depth) steps), a sweep that keeps
+//    the best reduced cost per row, then every negative row-best candidate
+//    walks its cycle with parent/depth LCA steps, claims its edges with
+//    atomicMin on a (reduced cost, row) priority, and the candidates that own
+//    all their edges (an edge-disjoint set, always containing the best one)
+//    are applied together.  Edge-disjoint pivots commute, so the round equals
+//    applying them one after another.  Sequential mode applies only the best
+//    candidate (Dantzig's rule with the reference's row-major first-minimum
+//    tie-break, uv_model_parallel.cu:178-200).
+#pragma once
+#include "vogel.cuh"
+
+namespace flock {
+
+__device__ __forceinline__ int32_t block_exclusive_scan_i32(int32_t* a, int n, BlockScratch& bs) {
+    // in-place exclusive scan of a[0..n), returns the total
+    const int T = blockDim.x;
+    const int chunk = (n + T - 1) / T;
+    const int lo = threadIdx.x * chunk, hi = min(n, lo + chunk);
+    int32_t s = 0;
+    for (int k = lo; k < hi; k++) s += a[k];
+    // warp inclusive scan of per-thread sums
+    int32_t x = s;
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5, nw = T >> 5;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) { int32_t y = __shfl_up_sync(0xffffffffu, x, o); if (l >= o) x += y; }
+    __syncthreads();
+    if (l == 31) bs.red[w] = (uint64_t)(int64_t)x;
+    __syncthreads();
+    if (w == 0) {
+        int32_t t = l < nw ? (int32_t)(int64_t)bs.red[l] : 0;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) { int32_t y = __shfl_up_sync(0xffffffffu, t, o); if (l >= o) t += y; }
+        bs.red2[l] = (uint64_t)(int64_t)t;
+    }
+    __syncthreads();
+    int32_t base = (w > 0 ? (int32_t)(int64_t)bs.red2[w - 1] : 0) + x - s;
+    for (int k = lo; k < hi; k++) { int32_t v = a[k]; a[k] = base; base += v; }
+    const int32_t total = (int32_t)(int64_t)bs.red2[nw - 1];
+    __syncthreads();
+    return total;
+}
+
+__device__ __forceinline__ int uf_find(int32_t* uf, int x) {
+    while (uf[x] != x) { uf[x] = uf[uf[x]]; x = uf[x]; }
+    return x;
+}
+
+// ------------------------------------------------------------ start tree ---
+// Builds the strongly feasible start tree from the allocation list c.bfs_*.
+// If the list is not a feasible solution whose positive cells form a forest
+// (the reference's undefined Vogel case), the NW-corner solution is used.
+__device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n, V = m + n;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.bsum[v] = 0; c.uf[v] = v; }
+    if (threadIdx.x == 0) bs.i[0] = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+        const int a = c.bfs_src[k], b = c.bfs_dst[k], q = c.bfs_qty[k];
+        if (a < 0 || a >= m || b < 0 || b >= n || q < 0) { bs.i[0] = 1; continue; }
+        atomicAdd((unsigned long long*)&c.bsum[a], (unsigned long long)(int64_t)q);
+        atomicAdd((unsigned long long*)&c.bsum[m + b], (unsigned long long)(int64_t)q);
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int64_t want = v < m ? I.supply[v] : I.demand[v - m];
+        if (c.bsum[v] != want) bs.i[0] = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !bs.i[0]) {
+        for (int k = 0; k < V - 1; k++) {
+            if (c.bfs_qty[k] <= 0) continue;
+            int ra = uf_find(c.uf, c.bfs_src[k]), rb = uf_find(c.uf, m + c.bfs_dst[k]);
+            if (ra == rb) { bs.i[0] = 1; break; }
+            c.uf[ra] = rb;
+        }
+    }
+    __syncthreads();
+    if (bs.i[0]) {
+        if (threadIdx.x == 0) { nwc_thread0(c); c.sc->status |= ST_START_REPAIRED; }
+        __syncthreads();
+    }
+
+    // root: the column with the largest demand (lowest index on ties)
+    uint64_t rk = 0;
+    int32_t alive_cols = 0;
+    int64_t S = 0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const uint32_t dj = (uint32_t)I.demand[j];
+        uint64_t k = ((uint64_t)dj << 32) | (uint64_t)(0xffffffffu - (uint32_t)j);
+        rk = k > rk ? k : rk;
+        alive_cols += I.demand[j] > 0;
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) S += I.supply[i];
+    rk = block_max_u64(rk, bs);
+    const int root = m + (int)(0xffffffffu - (uint32_t)rk);
+    const int64_t nalive = block_sum_i64(alive_cols, bs) + (I.demand[root - m] == 0 ? 1 : 0);
+    S = block_sum_i64(S, bs);
+    const int v_alive = m + (int)nalive;
+    const int64_t M = 2 * (int64_t)v_alive + 1;
+    if (threadIdx.x == 0) {
+        c.sc->root = root;
+        c.sc->v_alive = v_alive;
+        c.sc->M = M;
+        if (M > ((int64_t)1 << 62) / (S + 2)) c.sc->status |= ST_RANGE;
+    }
+
+    // CSR of positive cells (order[] holds degrees, then cursors)
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.order[v] = 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+        if (c.bfs_qty[k] <= 0 || c.bfs_src[k] < 0) continue;
+        atomicAdd(&c.order[c.bfs_src[k]], 1);
+        atomicAdd(&c.order[m + c.bfs_dst[k]], 1);
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.csr_start[v] = c.order[v];
+    __syncthreads();
+    const int32_t tot = block_exclusive_scan_i32(c.csr_start, V, bs);
+    if (threadIdx.x == 0) c.csr_start[V] = tot;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.order[v] = c.csr_start[v];
+    __syncthreads();
+    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+        if (c.bfs_qty[k] <= 0 || c.bfs_src[k] < 0) continue;
+        const int a = c.bfs_src[k], b = m + c.bfs_dst[k];
+        c.csr_adj[atomicAdd(&c.order[a], 1)] = b;
+        c.csr_adj[atomicAdd(&c.order[b], 1)] = a;
+    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = -2; c.depth[v] = 0; }
+    __syncthreads();
+
+    // components of the positive cells, attached to the tree built so far
+    if (threadIdx.x == 0) {
+        c.parent[root] = -1;
+        c.depth[root] = 0;
+        c.order[0] = root;
+        int qh = 0, qt = 1;
+        while (qh < qt) {
+            const int p = c.order[qh++];
+            for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
+                const int ch = c.csr_adj[e];
+                if (c.parent[ch] == -2 && ch != root) { c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch; }
+            }
+        }
+        bs.i[1] = 0;   // scan pointer
+        bs.i[2] = qt;  // queue tail
+    }
+    __syncthreads();
+    for (int guard = 0; guard <= V; guard++) {
+        if (threadIdx.x == 0) {
+            int w = bs.i[1];
+            while (w < V && (c.parent[w] != -2 || w == root || (w >= m && I.demand[w - m] == 0))) w++;
+            bs.i[1] = w;
+            int rc = -1;
+            if (w < V) {
+                if (w < m) rc = w;
+                else {
+                    for (int e = c.csr_start[w]; e < c.csr_start[w + 1]; e++) {
+                        const int x = c.csr_adj[e];
+                        if (x < m && (rc < 0 || x < rc)) rc = x;
+                    }
+                }
+            }
+            bs.i[3] = rc;
+        }
+        __syncthreads();
+        const int rc = bs.i[3];
+        if (rc < 0) break;
+        uint64_t best = kNoKey;
+        for (int j = threadIdx.x; j < n; j += blockDim.x)
+            if (c.parent[m + j] != -2) {
+                const uint64_t k = pack_i32(cost_of(I, rc, j), (uint32_t)j);
+                best = k < best ? k : best;
+            }
+        best = block_min_u64(best, bs);
+        if (threadIdx.x == 0) {
+            const int js = m + (int)key_idx(best);
+            int qt = bs.i[2];
+            int qh = qt;
+            c.parent[rc] = js;
+            c.depth[rc] = c.depth[js] + 1;
+            c.order[qt++] = rc;
+            while (qh < qt) {
+                const int p = c.order[qh++];
+                for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
+                    const int ch = c.csr_adj[e];
+                    if (c.parent[ch] == -2 && ch != root) { c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch; }
+                }
+            }
+            bs.i[2] = qt;
+        }
+        __syncthreads();
+    }
+
+    // perturbed flows, children before parents (reverse BFS order)
+    if (threadIdx.x == 0) {
+        const int qt = bs.i[2];
+        if (qt != v_alive) c.sc->status |= ST_SF_FAIL;
+        for (int q = 0; q < qt; q++) {
+            const int v = c.order[q];
+            int64_t b;
+            if (v < m) b = M * I.supply[v] + 1;
+            else if (v != root) b = -(M * I.demand[v - m] - 1);
+            else b = -(M * I.demand[v - m] + (v_alive - 1));
+            c.bsum[v] = b;
+        }
+        for (int q = qt - 1; q >= 1; q--) {
+            const int v = c.order[q];
+            const int p = c.parent[v];
+            const int64_t f = v < m ? c.bsum[v] : -c.bsum[v];
+            c.flow[v] = f;
+            if (f <= 0) c.sc->status |= ST_SF_FAIL;
+            c.bsum[p] += c.bsum[v];
+        }
+        c.flow[root] = 0;
+        if (c.sc->status & (ST_SF_FAIL | ST_RANGE)) c.sc->done = 1;
+    }
+    __syncthreads();
+}
+
+// --------------------------------------------------------------- duals ------
+// depth[] and pot[] from parent[] by pointer jumping: pot[v] = acc + (-1)^len pot[anc].
+__device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int V = I.m + I.n;
+    const int root = c.sc->root;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int p = c.parent[v];
+        if (p == -2) { c.anc0[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
+        else if (v == root) { c.anc0[v] = v; c.len0[v] = 0; c.acc0[v] = 0; }
+        else { c.anc0[v] = p; c.len0[v] = 1; c.acc0[v] = edge_cost(I, v, p); }
+    }
+    int32_t* aA = c.anc0; int32_t* aB = c.anc1;
+    int32_t* lA = c.len0; int32_t* lB = c.len1;
+    int64_t* xA = c.acc0; int64_t* xB = c.acc1;
+    int pending = 1;
+    __syncthreads();
+    for (int it = 0; it < 40 && pending; it++) {
+        int mine = 0;
+        for (int v = threadIdx.x; v < V; v += blockDim.x) {
+            const int a = aA[v];
+            if (a < 0 || a == root) { aB[v] = a; lB[v] = lA[v]; xB[v] = xA[v]; continue; }
+            const int aa = aA[a];
+            const int la = lA[v];
+            aB[v] = aa;
+            lB[v] = la + lA[a];
+            xB[v] = xA[v] + ((la & 1) ? -xA[a] : xA[a]);
+            mine |= (aa != root);
+        }
+        pending = __syncthreads_or(mine);
+        int32_t* t1 = aA; aA = aB; aB = t1;
+        int32_t* t2 = lA; lA = lB; lB = t2;
+        int64_t* t3 = xA; xA = xB; xB = t3;
+    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        c.depth[v] = lA[v];
+        c.pot[v] = xA[v];
+    }
+    if (pending && threadIdx.x == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- sweep -----
+// CTA-local sweep: best (reduced cost, column) of every row into row_best[].
+// Rows are int4-vectorised: the row pitch is a multiple of 4 and 16-byte aligned.
+__device__ void sweep_cta(const Ctx& c) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n;
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int64_t* vpot = c.pot + m;
+    for (int i = threadIdx.x >> 5; i < m; i += nw) {
+        const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
+        const int64_t u = c.pot[i];
+        uint64_t best = kNoKey;
+        for (int q = lane; q * 4 < n; q += 32) {
+            const int4 cv = row[q];
+            const int j = q * 4;
+            const int32_t cc[4] = {cv.x, cv.y, cv.z, cv.w};
+            #pragma unroll
+            for (int e = 0; e < 4; e++) {
+                if (j + e < n) {
+                    const int64_t r = (int64_t)cc[e] - u - vpot[j + e];
+                    const uint64_t k = pack_i32(clamp32(r), (uint32_t)(j + e));
+                    best = k < best ? k : best;
+                }
+            }
+        }
+        best = warp_min_u64(best);
+        if (lane == 0) c.row_best[i] = best;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- pivots ----
+struct CycleResult {
+    int64_t theta;
+    int32_t q;        // leaving edge (child vertex)
+    int32_t lside;    // 1: leaving edge on the column (l) side
+    int32_t ok;
+};
+
+// Walk the cycle of entering cell (row k, column vertex l).  Edges on the
+// k side decrease when their child is a row, on the l side when the child is
+// a column.  Ties (impossible with the perturbation) resolve as Cunningham's
+// rule: the l side first, highest edge there; else the lowest k-side edge.
+// If P != kNoKey every edge is claimed with atomicMin(claim, P).
+__device__ __forceinline__ CycleResult cycle_walk(const Ctx& c, int k, int l, uint64_t P, int V) {
+    const int m = c.I.m;
+    int x = k, y = l;
+    int64_t bk = INT64_MAX, bl = INT64_MAX;
+    int qk = -1, ql = -1;
+    int steps = 0;
+    CycleResult res;
+    res.ok = 1;
+    while (x != y) {
+        if (++steps > 2 * V) { res.ok = 0; break; }
+        const int dx = c.depth[x], dy = c.depth[y];
+        if (dx >= dy) {
+            if (x < m) { const int64_t f = c.flow[x]; if (f < bk) { bk = f; qk = x; } }
+            if (P != kNoKey) atomicMin((unsigned long long*)&c.claim[x], (unsigned long long)P);
+            x = c.parent[x];
+        }
+        if (dy >= dx) {
+            if (y >= m) { const int64_t f = c.flow[y]; if (f <= bl) { bl = f; ql = y; } }
+            if (P != kNoKey) atomicMin((unsigned long long*)&c.claim[y], (unsigned long long)P);
+            y = c.parent[y];
+        }
+        if (x < 0 || y < 0) { res.ok = 0; break; }
+    }
+    if (bl <= bk) { res.theta = bl; res.q = ql; res.lside = 1; }
+    else          { res.theta = bk; res.q = qk; res.lside = 0; }
+    if (res.q < 0) res.ok = 0;
+    return res;
+}
+
+__device__ __forceinline__ bool cycle_owned(const Ctx& c, int k, int l, uint64_t P, int V) {
+    int x = k, y = l, steps = 0;
+    while (x != y) {
+        if (++steps > 2 * V) return false;
+        const int dx = c.depth[x], dy = c.depth[y];
+        if (dx >= dy) { if (c.claim[x] != P) return false; x = c.parent[x]; }
+        if (dy >= dx) { if (c.claim[y] != P) return false; y = c.parent[y]; }
+        if (x < 0 || y < 0) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const CycleResult& cr, int V) {
+    const int m = c.I.m;
+    const int64_t th = cr.theta;
+    int x = k, y = l, steps = 0;
+    while (x != y && ++steps <= 2 * V) {
+        const int dx = c.depth[x], dy = c.depth[y];
+        if (dx >= dy) { c.flow[x] += (x < m) ? -th : th; x = c.parent[x]; }
+        if (dy >= dx) { c.flow[y] += (y >= m) ? -th : th; y = c.parent[y]; }
+    }
+    // re-hang the subtree below the leaving edge at the entering cell
+    int v = cr.lside ? l : k;
+    int prev = cr.lside ? k : l;
+    int64_t pf = th;
+    for (int s = 0; s <= V; s++) {
+        const int nxt = c.parent[v];
+        const int64_t f = c.flow[v];
+        c.parent[v] = prev;
+        c.flow[v] = pf;
+        if (v == cr.q) break;
+        prev = v; pf = f; v = nxt;
+    }
+}
+
+// One pricing round after sweep: choose candidates, claim, apply.
+__device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, V = m + I.n;
+    const int mode = c.sc->mode;
+    if (threadIdx.x == 0) bs.i[0] = 0;
+    __syncthreads();
+    if (mode == 0) {
+        uint64_t best = kNoKey;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const uint64_t k = c.row_best[i];
+            if (k != kNoKey && key_val(k) < 0) {
+                const uint64_t P = pack_i32(key_val(k), (uint32_t)i);
+                best = P < best ? P : best;
+            }
+        }
+        best = block_min_u64(best, bs);
+        if (threadIdx.x == 0 && best != kNoKey) { c.cand[0] = (int32_t)key_idx(best); bs.i[0] = 1; }
+    } else {
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const uint64_t k = c.row_best[i];
+            if (k != kNoKey && key_val(k) < 0) c.cand[atomicAdd(&bs.i[0], 1)] = i;
+        }
+    }
+    __syncthreads();
+    const int ncand = bs.i[0];
+    if (ncand == 0) {
+        if (threadIdx.x == 0) { c.sc->done = 1; c.sc->ncand = 0; }
+        __syncthreads();
+        return;
+    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.claim[v] = kNoKey;
+    __syncthreads();
+    int bad = 0;
+    for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+        const int i = c.cand[t];
+        const uint64_t key = c.row_best[i];
+        const int l = m + (int)key_idx(key);
+        const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
+        const CycleResult cr = cycle_walk(c, i, l, P, V);
+        c.cand_theta[t] = cr.theta;
+        c.cand_q[t] = cr.q;
+        c.cand_info[t] = cr.lside | (cr.ok ? 0 : 4);
+        bad |= !cr.ok;
+    }
+    __syncthreads();
+    int wins = 0;
+    for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+        if (c.cand_info[t] & 4) continue;
+        const int i = c.cand[t];
+        const uint64_t key = c.row_best[i];
+        const int l = m + (int)key_idx(key);
+        const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
+        if (cycle_owned(c, i, l, P, V)) { c.cand_info[t] |= 2; wins++; }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+        if (!(c.cand_info[t] & 2)) continue;
+        const int i = c.cand[t];
+        const int l = m + (int)key_idx(c.row_best[i]);
+        CycleResult cr;
+        cr.theta = c.cand_theta[t]; cr.q = c.cand_q[t]; cr.lside = c.cand_info[t] & 1; cr.ok = 1;
+        cycle_apply(c, i, l, cr, V);
+    }
+    const int64_t w = block_sum_i64(wins, bs);
+    const int any_bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        c.sc->pivots += (int32_t)w;
+        c.sc->ncand = ncand;
+        c.sc->last_winners = (int32_t)w;
+        if (any_bad || w == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+    }
+    __syncthreads();
+}
+
+// -------------------------------------------------------------- finalize ----
+// Attach zero-demand columns, recover original flows, write the basis and the
+// objective.  Dual of a zero-demand column: min_i (c_ij - u_i).
+__device__ void finalize_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n, V = m + n;
+    const int root = c.sc->root;
+    const int64_t M = c.sc->M;
+    const int64_t half = (M - 1) / 2;
+    for (int j = 0; j < n; j++) {
+        if (c.parent[m + j] != -2) continue;      // uniform: all threads read the same
+        uint64_t best = kNoKey;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int64_t val = (int64_t)cost_of(I, i, j) - c.pot[i];
+            const uint64_t k = (uint64_t)val ^ 0x8000000000000000ull;
+            best = k < best ? k : best;
+        }
+        best = block_min_u64(best, bs);
+        const int64_t vmin = (int64_t)(best ^ 0x8000000000000000ull);
+        uint64_t who = kNoKey;
+        for (int i = threadIdx.x; i < m; i += blockDim.x)
+            if ((int64_t)cost_of(I, i, j) - c.pot[i] == vmin) who = (uint64_t)i < who ? (uint64_t)i : who;
+        who = block_min_u64(who, bs);
+        if (threadIdx.x == 0) { c.parent[m + j] = (int)who; c.pot[m + j] = vmin; c.flow[m + j] = 0; }
+        __syncthreads();
+    }
+    int64_t obj = 0;
+    int32_t act = 0;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        if (v == root) continue;
+        const int k = v < root ? v : v - 1;
+        const int p = c.parent[v];
+        const int row = v < m ? v : p, col = v < m ? p - m : v - m;
+        const int64_t x = (c.flow[v] + half) / M;   // flow = M x + t, |t| <= V'-1 < M/2
+        c.out_src[k] = row; c.out_dst[k] = col; c.out_qty[k] = (int32_t)x;
+        obj += x * (int64_t)cost_of(I, row, col);
+        act += x > 0;
+    }
+    obj = block_sum_i64(obj, bs);
+    const int64_t a = block_sum_i64(act, bs);
+    if (threadIdx.x == 0) { c.sc->objective = obj; c.sc->active = (int32_t)a; }
+    __syncthreads();
+}
+
+// ----------------------------------------------------------- certificate ----
+// Independent exact check of the result: quantities >= 0, row/column sums,
+// every reduced cost >= 0 (full pass over the matrix), complementary slackness.
+__device__ void certify_flows_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n, V = m + n;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.bsum[v] = 0;
+    if (threadIdx.x == 0) bs.i[0] = 0;
+    __syncthreads();
+    int bits = 0;
+    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+        const int a = c.out_src[k], b = c.out_dst[k], q = c.out_qty[k];
+        if (a < 0 || a >= m || b < 0 || b >= n || q < 0) { bits |= 1; continue; }
+        atomicAdd((unsigned long long*)&c.bsum[a], (unsigned long long)(int64_t)q);
+        atomicAdd((unsigned long long*)&c.bsum[m + b], (unsigned long long)(int64_t)q);
+        const int64_t r = (int64_t)cost_of(I, a, b) - c.pot[a] - c.pot[m + b];
+        if (q > 0 && r != 0) bits |= 16;
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int64_t want = v < m ? I.supply[v] : I.demand[v - m];
+        if (c.bsum[v] != want) bits |= v < m ? 2 : 4;
+    }
+    atomicOr(&bs.i[0], bits);
+    __syncthreads();
+    if (threadIdx.x == 0) c.sc->cert |= bs.i[0];
+    __syncthreads();
+}
+
+__device__ void certify_cells_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n;
+    int64_t neg = 0;
+    for (int i = threadIdx.x >> 5; i < m; i += blockDim.x >> 5) {
+        const int64_t u = c.pot[i];
+        for (int j = threadIdx.x & 31; j < n; j += 32)
+            neg += ((int64_t)cost_of(I, i, j) - u - c.pot[m + j]) < 0;
+    }
+    neg = block_sum_i64(neg, bs);
+    if (threadIdx.x == 0) { c.sc->neg_cells = neg; if (neg) c.sc->cert |= 8; }
+    __syncthreads();
+}
+
+}  // namespace flock

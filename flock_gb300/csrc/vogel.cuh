@@ -1,0 +1,229 @@
+// vogel.cuh -- Vogel's approximation on the device with the exact semantics of
+// the reference's sequential host routine (find_vogel_bfs_sequencial,
+// src/parallel_simplex_method/IBFS_vogel.cu:546-769):
+//
+//  * penalties are refreshed for ALL rows only after a step that covered a row,
+//    for ALL columns only after a step that covered a column (both at the
+//    start); otherwise the stored values stay stale (:570,:588-642);
+//  * penalty = second-cheapest - cheapest uncovered crossing cost, computed in
+//    float and converted to int as x86 does (one uncovered cell: float(2^31)-c,
+//    which is INT_MIN when it rounds to 2^31; none: 0); covered lines -1;
+//  * the chosen line is the LAST index with the maximal penalty over
+//    [rows, columns] (:651-659);
+//  * in that line the FIRST cheapest uncovered crossing cell is used
+//    (:671-676, :721-727); if there is none the reference reuses the previous
+//    step's index, which is reproduced (and counted) while it is in range;
+//  * min(residual supply, residual demand) is allocated; a tie covers the
+//    column (:691, :739).
+//
+// Instead of rescanning every uncovered line per refresh (O(V*m*n) in the
+// reference), each line caches its two cheapest uncovered crossing cells.  A
+// cache stays exact until one of those two crossing lines is covered; only
+// then is the line rescanned, with a warp-shuffle (or block-wide) top-2
+// reduction.  The penalties written at each refresh are therefore identical
+// to a full recomputation.
+#pragma once
+#include "device.cuh"
+
+namespace flock {
+
+__device__ __forceinline__ int32_t vogel_penalty(int4 t) {
+    long long c1 = t.z >= 0 ? (long long)t.x : 2147483648LL;
+    long long c2 = t.w >= 0 ? (long long)t.y : 2147483648LL;
+    // float(c2) - float(c1) is exact-then-rounded for |c| <= 2^24.
+    return f2i_x86(__ll2float_rn(c2 - c1));
+}
+
+__device__ __forceinline__ int4 top2_from_keys(uint64_t a1, uint64_t a2) {
+    int4 t;
+    t.x = a1 == kNoKey ? 0 : key_val(a1);
+    t.y = a2 == kNoKey ? 0 : key_val(a2);
+    t.z = a1 == kNoKey ? -1 : (int32_t)key_idx(a1);
+    t.w = a2 == kNoKey ? -1 : (int32_t)key_idx(a2);
+    return t;
+}
+
+// crossing line of line L at crossing index x
+__device__ __forceinline__ int crossing_vertex(int L, int x, int m) { return L < m ? m + x : x; }
+
+__device__ __forceinline__ bool top2_valid(const Ctx& c, int L, int4 t) {
+    const int m = c.I.m;
+    if (t.z == -2) return false;                  // never built
+    if (t.z < 0) return true;                     // nothing uncovered: stays so
+    if (c.covered[crossing_vertex(L, t.z, m)]) return false;
+    if (t.w >= 0 && c.covered[crossing_vertex(L, t.w, m)]) return false;
+    return true;
+}
+
+// one warp rebuilds the cache of line L
+__device__ void vogel_rescan_warp(const Ctx& c, int L) {
+    const InstDev& I = c.I;
+    const int lane = threadIdx.x & 31;
+    uint64_t a1 = kNoKey, a2 = kNoKey;
+    if (L < I.m) {
+        const int32_t* row = I.cost + (size_t)L * I.ldc;
+        for (int j = lane; j < I.n; j += 32)
+            if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+    } else {
+        const int j = L - I.m;
+        for (int i = lane; i < I.m; i += 32)
+            if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+    }
+    warp_top2(a1, a2);
+    if (lane == 0) c.top2[L] = top2_from_keys(a1, a2);
+}
+
+// the whole block rebuilds the cache of line L (block-uniform call)
+__device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    uint64_t a1 = kNoKey, a2 = kNoKey;
+    if (L < I.m) {
+        const int32_t* row = I.cost + (size_t)L * I.ldc;
+        for (int j = threadIdx.x; j < I.n; j += blockDim.x)
+            if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+    } else {
+        const int j = L - I.m;
+        for (int i = threadIdx.x; i < I.m; i += blockDim.x)
+            if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+    }
+    warp_top2(a1, a2);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) { bs.red[w] = a1; bs.red2[w] = a2; }
+    __syncthreads();
+    if (w == 0) {
+        uint64_t b1 = l < nw ? bs.red[l] : kNoKey, b2 = l < nw ? bs.red2[l] : kNoKey;
+        warp_top2(b1, b2);
+        if (l == 0) c.top2[L] = top2_from_keys(b1, b2);
+    }
+    __syncthreads();
+}
+
+// Refresh the stored penalties of lines [lo, hi) (all rows or all columns).
+__device__ void vogel_refresh(const Ctx& c, int lo, int hi, BlockScratch& bs) {
+    if (threadIdx.x == 0) bs.i[6] = 0;
+    __syncthreads();
+    for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
+        if (!c.covered[v] && !top2_valid(c, v, c.top2[v])) {
+            int k = atomicAdd(&bs.i[6], 1);
+            c.rescan[k] = v;
+        }
+    }
+    __syncthreads();
+    const int k = bs.i[6];
+    const int nw = blockDim.x >> 5;
+    if (k >= nw) {
+        for (int q = threadIdx.x >> 5; q < k; q += nw) vogel_rescan_warp(c, c.rescan[q]);
+    } else {
+        for (int q = 0; q < k; q++) vogel_rescan_block(c, c.rescan[q], bs);
+    }
+    __syncthreads();
+    for (int v = lo + threadIdx.x; v < hi; v += blockDim.x)
+        c.diff[v] = c.covered[v] ? -1 : vogel_penalty(c.top2[v]);
+    __syncthreads();
+}
+
+// Vogel's approximation.  Writes the V-1 allocations to c.bfs_* in allocation
+// order and the event count to c.sc->events (-1: the reference's behaviour is
+// undefined from the step written as (-1,-1,0) on).
+__device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n, V = m + n;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        c.covered[v] = 0;
+        c.res[v] = v < m ? I.supply[v] : I.demand[v - m];
+        c.diff[v] = 0;
+    }
+    // initial caches: rows one warp per row (coalesced), columns one thread
+    // per column walking down the rows (coalesced across the warp)
+    const int nw = blockDim.x >> 5;
+    for (int i = threadIdx.x >> 5; i < m; i += nw) {
+        const int32_t* row = I.cost + (size_t)i * I.ldc;
+        uint64_t a1 = kNoKey, a2 = kNoKey;
+        for (int j = threadIdx.x & 31; j < n; j += 32) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+        warp_top2(a1, a2);
+        if ((threadIdx.x & 31) == 0) c.top2[i] = top2_from_keys(a1, a2);
+    }
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        uint64_t a1 = kNoKey, a2 = kNoKey;
+        for (int i = 0; i < m; i++) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+        c.top2[m + j] = top2_from_keys(a1, a2);
+    }
+    if (threadIdx.x == 0) {
+        bs.i[0] = 1; bs.i[1] = 1;   // prev_row, prev_col
+        bs.i[2] = 0; bs.i[3] = 0;   // covered rows / columns (counters)
+        bs.i[4] = 0;                // stale min-cost index
+        bs.i[5] = 0;                // events
+        bs.i[7] = 0;                // stop
+    }
+    __syncthreads();
+    for (int step = 0; step < V - 1; step++) {
+        const int cr = bs.i[2], cc = bs.i[3];
+        if (cr + cc >= V - 1 || bs.i[7]) break;
+        const int pr = bs.i[0], pc = bs.i[1];
+        __syncthreads();
+        if (pr) vogel_refresh(c, 0, m, bs);
+        if (pc) vogel_refresh(c, m, V, bs);
+        uint64_t best = 0;
+        for (int v = threadIdx.x; v < V; v += blockDim.x) {
+            uint64_t k = pack_i32(c.diff[v], (uint32_t)v);
+            best = k > best ? k : best;
+        }
+        best = block_max_u64(best, bs);
+        const int L = (int)key_idx(best);
+        if (!top2_valid(c, L, c.top2[L])) vogel_rescan_block(c, L, bs);
+        if (threadIdx.x == 0) {
+            if (pr) bs.i[0] = 0;
+            if (pc) bs.i[1] = 0;
+            const int4 t = c.top2[L];
+            const bool found = t.z >= 0;
+            const int cross = found ? t.z : bs.i[4];
+            if (!found) bs.i[5]++;
+            int row, col;
+            bool undefined;
+            if (L >= m) { col = L - m; row = cross; undefined = row < 0 || row >= m; }
+            else        { row = L; col = cross; undefined = col < 0 || col >= n; }
+            const int counter = cr + cc;
+            if (undefined) {
+                bs.i[5] = -1;
+                bs.i[7] = 1;
+                for (int k = counter; k < V - 1; k++) { c.bfs_src[k] = -1; c.bfs_dst[k] = -1; c.bfs_qty[k] = 0; }
+            } else {
+                const int32_t rs = c.res[row], rd = c.res[m + col];
+                int32_t q;
+                if (rd > rs) {
+                    q = rs; c.res[m + col] = rd - rs; c.res[row] = 0; c.covered[row] = 1;
+                    bs.i[0] = 1; bs.i[2] = cr + 1;
+                } else {
+                    q = rd; c.res[row] = rs - rd; c.res[m + col] = 0; c.covered[m + col] = 1;
+                    bs.i[1] = 1; bs.i[3] = cc + 1;
+                }
+                c.bfs_src[counter] = row; c.bfs_dst[counter] = col; c.bfs_qty[counter] = q;
+                if (found) bs.i[4] = cross;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c.sc->events = bs.i[5];
+    __syncthreads();
+}
+
+// North-west corner rule (IBFS_nwc.cu:3-33), thread 0 only; caller syncs.
+__device__ void nwc_thread0(const Ctx& c) {
+    const InstDev& I = c.I;
+    int r = 0, k = 0, cnt = 0;
+    int32_t cd = I.demand[0], cs = I.supply[0];
+    while (r < I.m && k < I.n && cnt < I.m + I.n - 1) {
+        if (cd >= cs) {
+            c.bfs_src[cnt] = r; c.bfs_dst[cnt] = k; c.bfs_qty[cnt] = cs;
+            cd -= cs; r++; cs = r < I.m ? I.supply[r] : 0;
+        } else {
+            c.bfs_src[cnt] = r; c.bfs_dst[cnt] = k; c.bfs_qty[cnt] = cd;
+            cs -= cd; k++; cd = k < I.n ? I.demand[k] : 0;
+        }
+        cnt++;
+    }
+    for (; cnt < I.m + I.n - 1; cnt++) { c.bfs_src[cnt] = -1; c.bfs_dst[cnt] = -1; c.bfs_qty[cnt] = 0; }
+}
+
+}  // namespace flock

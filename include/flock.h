@@ -1,0 +1,184 @@
+/*
+ * flock.h -- C ABI of flock-gb300, a GB300-native (sm_103a) solver for the
+ * balanced transportation problem
+ *      min sum c_ij x_ij  s.t.  sum_j x_ij = s_i,  sum_i x_ij = d_j,  x >= 0
+ * with the method of researchgroup-zx93920/flock: Vogel's approximation for
+ * the initial basic feasible solution, u-v duals on the basis tree, a
+ * reduced-cost sweep and stepping-stone pivots (single or deconflicted
+ * parallel).  All arithmetic is integer: int32 costs and quantities, int64
+ * duals and objective.
+ *
+ * Conventions: every function returns a flock_status (0 = FLOCK_OK).  The
+ * caller owns every host buffer; the library owns device state.  Costs are
+ * row-major, cell (i, j) at cost[i * n + j].  Calls are thread-safe (a
+ * process-wide lock serialises the plain-path device workspace).
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   flock_read_dat / flock_dat_shape  <- readSize / readCosts, src/instance.cpp:80-141
+ *                                        (ProblemInstance, src/structs.h:19-40)
+ *   flock_vogel                       <- find_vogel_bfs_sequencial,
+ *                                        src/parallel_simplex_method/IBFS_vogel.cu:546-769
+ *   flock_solve                       <- uvModel_parallel / ssModel_parallel ctor + execute()
+ *                                        + create_flows(), src/algos.h:1-4,
+ *                                        parallel_uv_method/uv_model_parallel.cu:20-400,
+ *                                        parallel_ss_method/ss_model_parallel.cu:128-250
+ *   flock_flow                        <- flowInformation, src/structs.h:45-52
+ *   flock_options                     <- BFS_METHOD / MAX_ITERATIONS / pivoting switches,
+ *                                        src/parallel_simplex_method/parallel_structs.h:34-89
+ *   flock_stats                       <- model statistics (objVal, totalIterations,
+ *                                        totalSolveTime, ...), uv_model_parallel.h:33-38
+ *   flock_batch_solve, flock_server_* <- no counterpart (the reference solves one instance
+ *                                        per process); batched and served forms of flock_solve
+ */
+#ifndef FLOCK_GB300_H
+#define FLOCK_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FLOCK_OK = 0,
+    FLOCK_ERR_ARG = 1,          /* null pointer, m or n < 1, negative quantity */
+    FLOCK_ERR_UNBALANCED = 2,   /* sum of supplies != sum of demands */
+    FLOCK_ERR_FILE = 3,         /* file not found / unreadable (reference: FileNotFoundException) */
+    FLOCK_ERR_PARSE = 4,        /* malformed .dat content */
+    FLOCK_ERR_INEXACT = 5,      /* a cost is not an integer after decimal scaling */
+    FLOCK_ERR_RANGE = 6,        /* |cost| > 2^30, or the instance is too large */
+    FLOCK_ERR_CUDA = 7,         /* CUDA error (message via flock_last_error) */
+    FLOCK_ERR_NOT_OPTIMAL = 8,  /* solve stopped before optimality (see flock_stats.status) */
+    FLOCK_ERR_BUDGET = 9,       /* serving: request larger than the memory budget */
+    FLOCK_ERR_CAPACITY = 10     /* output buffer too small */
+} flock_status;
+
+/* One balanced instance (host memory). */
+typedef struct {
+    int32_t m, n;               /* supplies (rows), demands (columns) */
+    const int32_t* supply;      /* m */
+    const int32_t* demand;      /* n */
+    const int32_t* cost;        /* m*n, row-major */
+} flock_instance;
+
+/* One flow: qty units from supply `source` to demand `destination`. */
+typedef struct {
+    int32_t source, destination, qty;
+} flock_flow;
+
+enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1 };            /* BFS_METHOD nwc_host / vam_host */
+enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1 }; /* -a parallel_uv / parallel_ss  */
+
+typedef struct {
+    int32_t bfs_method;      /* FLOCK_BFS_VOGEL (default) or FLOCK_BFS_NWC */
+    int32_t pivot_method;    /* FLOCK_PIVOT_PARALLEL (default) or FLOCK_PIVOT_SEQUENTIAL */
+    int32_t max_iterations;  /* cap on pricing rounds; <= 0: 1 << 30 */
+    int32_t verify;          /* nonzero: run the exact certificate check (default on) */
+} flock_options;
+
+/* Failures reported in flock_stats.status (bit set; 0 = optimal). */
+enum {
+    FLOCK_ST_ITER_CAP = 1,        /* round cap reached before optimality */
+    FLOCK_ST_TREE_CORRUPT = 2,    /* internal consistency failure */
+    FLOCK_ST_SF_FAIL = 4,         /* internal: start tree not strongly feasible */
+    FLOCK_ST_CERT_FAIL = 32,      /* certificate failed */
+    FLOCK_ST_RANGE = 64           /* perturbed flows would overflow */
+};
+/* Notes reported in flock_stats.notes (informational, the result is still optimal). */
+enum {
+    FLOCK_NOTE_VOGEL_UNDEF = 8,     /* Vogel reached the reference's undefined case */
+    FLOCK_NOTE_START_REPAIRED = 16  /* simplex started from the NW corner instead */
+};
+
+typedef struct {
+    int64_t objective;       /* sum c_ij x_ij (exact) */
+    int32_t iterations;      /* pricing rounds (full reduced-cost sweeps) */
+    int32_t pivots;          /* pivots applied */
+    int32_t active_flows;    /* nonzero flows written to `flows` */
+    int32_t status;          /* FLOCK_ST_* failure bits, 0 = optimal */
+    int32_t notes;           /* FLOCK_NOTE_* bits */
+    int32_t certified;       /* 1: certificate checked and passed */
+    int32_t vogel_events;    /* Vogel steps whose line had no uncovered cell; -1 undefined */
+    double ms_total;         /* wall time of the call (ms) */
+    double ms_bfs;           /* device time of the initial solution + start tree */
+    double ms_simplex;       /* device time of the pivot loop */
+} flock_stats;
+
+void flock_default_options(flock_options* opt);
+const char* flock_last_error(void);
+const char* flock_version(void);
+
+/* .dat reader.  Format: "m n", m supplies, n demands, m*n costs (row-major),
+ * whitespace separated (src/instance.cpp:96-141).  Costs are decimal text and
+ * are multiplied by 10^decimal_scale exactly (FLOCK_ERR_INEXACT otherwise).
+ * flock_dat_scale reports the smallest scale making every cost integral. */
+int flock_dat_shape(const char* path, int32_t* m, int32_t* n);
+int flock_dat_scale(const char* path, int32_t* scale);
+int flock_read_dat(const char* path, int32_t decimal_scale, int32_t m, int32_t n,
+                   int32_t* supply, int32_t* demand, int32_t* cost);
+
+/* Vogel's approximation on the GPU with the reference's exact semantics.
+ * Writes m+n-1 allocations in allocation order.  *events as flock_stats. */
+int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events);
+
+/* Solve one instance on the GPU.  `flows` has room for m+n-1 entries; the
+ * nonzero flows are written first (stats->active_flows of them), then the
+ * zero-flow basic cells, so flows[0..m+n-2] is always the full basis.
+ * duals_u (m) and duals_v (n) are optional (NULL): the optimal duals with
+ * c_ij - u_i - v_j >= 0 everywhere and = 0 on the basis.
+ * Returns FLOCK_ERR_NOT_OPTIMAL when stats->status != 0. */
+int flock_solve(const flock_instance* inst, const flock_options* opt, flock_flow* flows,
+                int64_t* duals_u, int64_t* duals_v, flock_stats* stats);
+
+/* Batched form: `count` independent instances solved by one persistent kernel
+ * family (one CTA per instance, work stealing, size buckets).  Flows of
+ * instance k start at flows[flow_offset[k]] with room for m_k+n_k-1 entries
+ * (same layout as flock_solve); flow_offset may be NULL (packed in order).
+ * stats has `count` entries. */
+int flock_batch_solve(int32_t count, const flock_instance* insts, const flock_options* opt,
+                      flock_flow* flows, const int64_t* flow_offset, flock_stats* stats);
+
+/* Served form: continuous batching with admission by a device-memory budget. */
+typedef struct flock_server flock_server;
+typedef struct {
+    int64_t memory_budget_bytes;   /* resident device state allowed (default 40 GiB) */
+    int32_t max_inflight_batches;  /* concurrent launches (streams), default 4 */
+    int32_t max_batch;             /* instances per launch, default 512 */
+    flock_options options;
+} flock_server_config;
+typedef struct {
+    uint64_t ticket;
+    int32_t status;                /* flock_status of this request */
+    flock_stats stats;
+    double latency_ms;             /* submit -> result ready */
+} flock_result;
+
+void flock_default_server_config(flock_server_config* cfg);
+int flock_server_create(const flock_server_config* cfg, flock_server** out);
+/* Copies the instance; the result's flows are returned by flock_server_poll. */
+int flock_server_submit(flock_server* s, const flock_instance* inst, uint64_t* ticket);
+/* Returns up to `max` finished results; flows of result k go to flows_out[k]
+ * (each with room for m+n-1 entries; may be NULL).  *count is set. */
+int flock_server_poll(flock_server* s, flock_result* results, flock_flow** flows_out,
+                      int32_t max, int32_t* count);
+/* Blocks until every submitted request has finished. */
+int flock_server_drain(flock_server* s);
+int flock_server_destroy(flock_server* s);
+
+/* Deterministic instance generators (splitmix64 + Lemire bounded integers).
+ * kind 0: uniform costs [c_lo, c_hi], supplies [q_lo, q_hi], raw demands
+ *         [q_lo, q_hi] rescaled to sum to the supply total (remainder to the
+ *         last demand).
+ * kind 1: Euclidean: m sources and n sinks uniform in [0,1000]^2, cost =
+ *         round(distance) half away from zero; quantities as kind 0.
+ * Buffers are caller-owned (m, n, m*n). */
+int flock_generate(int32_t kind, uint64_t seed, int32_t m, int32_t n,
+                   int32_t c_lo, int32_t c_hi, int32_t q_lo, int32_t q_hi,
+                   int32_t* supply, int32_t* demand, int32_t* cost);
+/* log-uniform integer sizes in [lo, hi]: round(exp(U(ln lo, ln hi))) */
+int flock_generate_sizes(uint64_t seed, int32_t count, int32_t lo, int32_t hi,
+                         int32_t* ms, int32_t* ns);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,28 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+REFERENCE = "/root/reference"   # present only where the golden files were made
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built native library")
+
+
+@pytest.fixture(scope="session")
+def flock_lib():
+    import flock_gb300
+    return flock_gb300.lib()
+
+
+@pytest.fixture(scope="session")
+def orc():
+    import oracle
+    oracle.orc()
+    return oracle

@@ -1,0 +1,142 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle (the
+reference CPU path restated in C) on the same seeded inputs.
+
+Bar: Vogel allocations bit-identical; objective identical wherever the
+reference path ends by optimality; every GPU solution passes the exact
+int64 certificate (feasibility, all reduced costs >= 0, complementary
+slackness)."""
+import numpy as np
+import pytest
+
+import flock_gb300 as fg
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def tiny_instances(seed, count, max_dim=8):
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < count:
+        m = int(rng.integers(1, max_dim + 1)); n = int(rng.integers(1, max_dim + 1))
+        if m + n < 3:
+            continue
+        hi = int(rng.choice([3, 5, 20, 100]))
+        c = rng.integers(0, hi, size=(m, n)).astype(np.int32)
+        qh = int(rng.choice([2, 4, 10, 50]))
+        s = rng.integers(0, qh, size=m).astype(np.int32)
+        d = rng.integers(0, qh, size=n).astype(np.int32)
+        diff = int(s.sum() - d.sum())
+        if diff > 0:
+            d[-1] += diff
+        else:
+            s[-1] -= diff
+        out.append(fg.Instance(s, d, c))
+    return out
+
+
+def assert_vogel_parity(inst):
+    gpu, ev = fg.vogel(inst)
+    src, dst, q, oev = oracle.vogel(inst.supply, inst.demand, inst.cost)
+    assert ev == oev
+    if oev < 0:      # the reference is undefined from the first (-1) entry on
+        k = int(np.argmax(src < 0))
+        src, dst, q, gpu = src[:k], dst[:k], q[:k], gpu[:k]
+    qi = np.where(q < 0.5, 0, q).astype(np.int64)     # the reference writes 1e-6 for zero
+    np.testing.assert_array_equal(gpu[:, 0], src)
+    np.testing.assert_array_equal(gpu[:, 1], dst)
+    np.testing.assert_array_equal(gpu[:, 2].astype(np.int64), qi)
+
+
+def assert_optimal(inst, res, ref=None):
+    assert res.status == 0, f"status {res.status}"
+    assert res.certified
+    bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, res.flows, res.u, res.v)
+    assert bits == 0, f"certificate bits {bits}"
+    assert obj == res.objective
+    if ref is None:
+        ref = oracle.solve_ref(inst.supply, inst.demand, inst.cost)
+    if ref["status"] == 0:
+        assert res.objective == int(round(ref["objective"]))
+    return ref
+
+
+def test_vogel_tiny_degenerate():
+    for inst in tiny_instances(11, 400):
+        assert_vogel_parity(inst)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_vogel_uniform100(seed):
+    assert_vogel_parity(fg.config_instance("uniform100", seed))
+
+
+def test_vogel_degenerate_shape():
+    assert_vogel_parity(fg.config_instance("degenerate1000", 3, m=300, n=250))
+
+
+def test_vogel_euclid_shape():
+    assert_vogel_parity(fg.config_instance("euclid8000", 5, m=200, n=300))
+
+
+@pytest.mark.parametrize("pivot", ["parallel", "sequential"])
+def test_solve_tiny(pivot):
+    for inst in tiny_instances(23, 150):
+        res = fg.solve(inst, pivot=pivot)
+        assert_optimal(inst, res)
+
+
+@pytest.mark.parametrize("pivot", ["parallel", "sequential"])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_solve_uniform100(pivot, seed):
+    inst = fg.config_instance("uniform100", seed)
+    assert_optimal(inst, fg.solve(inst, pivot=pivot))
+
+
+def test_solve_nwc_start():
+    inst = fg.config_instance("uniform100", 7)
+    res = fg.solve(inst, bfs="nwc")
+    assert_optimal(inst, res)
+
+
+def test_solve_degenerate_mid():
+    inst = fg.config_instance("degenerate1000", 1, m=400, n=300)
+    assert_optimal(inst, fg.solve(inst))
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (6, 1), (2, 2), (3, 50), (50, 3)])
+def test_edge_shapes(shape):
+    m, n = shape
+    rng = np.random.default_rng(m * 100 + n)
+    s = rng.integers(0, 20, m).astype(np.int32)
+    d = np.zeros(n, np.int32)
+    d[:] = s.sum() // n
+    d[-1] += s.sum() - d.sum()
+    c = rng.integers(1, 30, (m, n)).astype(np.int32)
+    inst = fg.Instance(s, d, c)
+    assert_vogel_parity(inst)
+    assert_optimal(inst, fg.solve(inst))
+
+
+def test_zero_quantities():
+    m, n = 6, 7
+    rng = np.random.default_rng(5)
+    c = rng.integers(1, 9, (m, n)).astype(np.int32)
+    s = np.array([0, 4, 0, 3, 0, 5], np.int32)
+    d = np.array([0, 0, 6, 0, 6, 0, 0], np.int32)
+    inst = fg.Instance(s, d, c)
+    assert_optimal(inst, fg.solve(inst))
+    inst0 = fg.Instance(np.zeros(m, np.int32), np.zeros(n, np.int32), c)
+    res = fg.solve(inst0)
+    assert res.status == 0 and res.objective == 0
+
+
+def test_batch_matches_plain():
+    insts = fg.mixed_batch(3, 64, 10, 120)
+    out = fg.batch_solve(insts)
+    for inst, r in zip(insts, out):
+        p = fg.solve(inst)
+        assert r.status == 0 and r.certified
+        assert r.objective == p.objective
+        bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, r.flows, p.u, p.v)
+        assert obj == r.objective

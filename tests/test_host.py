@@ -1,0 +1,150 @@
+"""CPU: host logic of the product with no GPU -- the C ABI library loads and
+exports every symbol include/flock.h declares, the generator is
+deterministic, the .dat reader and the argument checks return the
+documented status codes, the C++ facade compiles, the CLI reports usage
+errors, and the server refuses requests over its memory budget."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import flock_gb300 as fg
+from conftest import ROOT
+from golden_util import checksum
+
+HEADER = os.path.join(ROOT, "include", "flock.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(flock_[a-z_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(flock_lib):
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(flock_lib, s), s
+
+
+def test_version(flock_lib):
+    assert "sm_103a" in fg.version()
+
+
+def test_generator_deterministic():
+    a = fg.config_instance("uniform100", 0)
+    b = fg.config_instance("uniform100", 0)
+    assert checksum(a.supply, a.demand, a.cost) == checksum(b.supply, b.demand, b.cost)
+    assert checksum(a.supply, a.demand, a.cost) == "c2b1152114b4affd"
+    assert a.supply.sum() == a.demand.sum()
+    assert a.cost.min() >= 1 and a.cost.max() <= 100
+    e = fg.config_instance("euclid8000", 0, m=150, n=200)
+    assert checksum(e.supply, e.demand, e.cost) == "65e5f43ff1f0024c"
+    assert e.supply.sum() == e.demand.sum() and e.cost.min() >= 0 and e.cost.max() <= 1415
+
+
+def test_generator_sizes():
+    ms, ns = fg.generate_sizes(1, 2000, 10, 500)
+    assert ms.min() >= 10 and ms.max() <= 500 and ns.min() >= 10 and ns.max() <= 500
+    # log-uniform: median near sqrt(10*500) ~ 71
+    assert 50 < np.median(ms) < 100
+
+
+def test_degenerate_config_balanced():
+    x = fg.config_instance("degenerate1000", 2, m=300, n=300)
+    assert x.supply.sum() == x.demand.sum()
+    assert x.cost.max() <= 20 and x.supply.max() <= 50
+
+
+def write(tmp_path, name, text):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+def test_reader_formats(tmp_path):
+    p = write(tmp_path, "a.dat", "2 3\n5\t7\n4 4 4\n1.25 2 3\n4 5.5 6.75\n")
+    inst, scale = fg.read_dat(p)
+    assert scale == 2
+    assert inst.supply.tolist() == [5, 7] and inst.demand.tolist() == [4, 4, 4]
+    assert inst.cost.tolist() == [[125, 200, 300], [400, 550, 675]]
+    inst0, s0 = fg.read_dat(write(tmp_path, "b.dat", "1 1 3 3 17"))
+    assert s0 == 0 and inst0.cost.tolist() == [[17]]
+
+
+def test_reader_errors(tmp_path):
+    with pytest.raises(fg.FileNotFoundException):
+        fg.read_dat(str(tmp_path / "missing.dat"))
+    with pytest.raises(fg.FlockError) as ex:
+        fg.read_dat(write(tmp_path, "bad.dat", "2 2\n1 1\n1 x\n1 2 3 4\n"))
+    assert ex.value.status == fg.FLOCK_ERR_PARSE
+    with pytest.raises(fg.FlockError) as ex:
+        fg.read_dat(write(tmp_path, "short.dat", "2 2\n1 1\n1 1\n1 2 3\n"))
+    assert ex.value.status == fg.FLOCK_ERR_PARSE
+    with pytest.raises(fg.FlockError) as ex:
+        fg.read_dat(write(tmp_path, "inexact.dat", "1 2\n2\n1 1\n1.5 2.25\n"), scale=1)
+    assert ex.value.status == fg.FLOCK_ERR_INEXACT
+
+
+def test_reader_reference_fixture_copy(tmp_path):
+    """A fixture of the reference's tests/ folder, written back as text."""
+    import json
+    fx = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_fixtures.json")))
+    e = [x for x in fx if x["file"] == "test_TransportModel_25_25_1.dat"][0]
+    txt = f"{e['m']} {e['n']}\n" + " ".join(map(str, e["supply"])) + "\n" + " ".join(map(str, e["demand"])) + "\n"
+    txt += " ".join("%d.%02d" % (c // 100, c % 100) for c in e["cost"]) + "\n"
+    inst, scale = fg.read_dat(write(tmp_path, "fx.dat", txt))
+    assert scale <= 2
+    assert (inst.cost.reshape(-1) * 10 ** (2 - scale)).tolist() == e["cost"]
+
+
+def test_solve_argument_errors():
+    bad = fg.Instance(np.array([3, 4], np.int32), np.array([5, 1], np.int32), np.ones((2, 2), np.int32))
+    with pytest.raises(fg.FlockError) as ex:
+        fg.solve(bad)
+    assert ex.value.status == fg.FLOCK_ERR_UNBALANCED
+    neg = fg.Instance(np.array([-1, 2], np.int32), np.array([1, 0], np.int32), np.ones((2, 2), np.int32))
+    with pytest.raises(fg.FlockError) as ex:
+        fg.solve(neg)
+    assert ex.value.status == fg.FLOCK_ERR_ARG
+    big = fg.Instance(np.array([1], np.int32), np.array([1], np.int32), np.array([[1 << 31 - 1]], np.int32))
+    big.cost[0, 0] = (1 << 30) + 5
+    with pytest.raises(fg.FlockError) as ex:
+        fg.solve(big)
+    assert ex.value.status == fg.FLOCK_ERR_RANGE
+
+
+def test_cpp_facade_compiles(tmp_path):
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "flock/algos.h"\nint main(){ProblemInstance p; std::vector<flowInformation> f(1);'
+                   ' uvModel_parallel a(&p, f.data()); ssModel_parallel b(&p, f.data());'
+                   ' switchModel_parallel c(&p, f.data()); (void)a; (void)b; (void)c; return 0;}\n')
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_cli_usage_errors(tmp_path):
+    cli = os.path.join(ROOT, "flock_gb300", "flock")
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    r = subprocess.run([cli], capture_output=True, text=True)
+    assert r.returncode == 255 and "-i" in r.stderr
+    r = subprocess.run([cli, "-i", str(tmp_path / "none.dat"), "-a", "parallel_uv"], capture_output=True, text=True)
+    assert r.returncode == 255 and "doesn't exist" in r.stderr
+    p = write(tmp_path, "ok.dat", "1 1\n1\n1\n1\n")
+    r = subprocess.run([cli, "-i", p, "-a", "nonsense"], capture_output=True, text=True)
+    assert r.returncode == 254 and "Invalid Algorithm" in r.stderr
+
+
+def test_server_budget_rejection():
+    s = fg.Server(memory_budget_bytes=1000)
+    inst = fg.config_instance("uniform100", 0)
+    with pytest.raises(fg.FlockError) as ex:
+        s.submit(inst)
+    assert ex.value.status == fg.FLOCK_ERR_BUDGET
+    s.close()

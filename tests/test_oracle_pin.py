@@ -1,0 +1,137 @@
+"""CPU: the oracle (C restatement of the reference CPU path) pinned to the
+reference itself -- golden outputs of the reference's own functions
+(tests/golden, made by make_golden.py from the reference build), the
+reference's published run logs, and, where the reference sources are
+present, the reference build run live.  Also checks the certificate checker
+by planting mistakes in its inputs."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, REFERENCE
+from golden_util import float_costs, tiny
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return json.load(f)
+
+
+def check_against(e, s, d, cf):
+    src, dst, q, ev = oracle.vogel(s, d, cf)
+    if ev >= 0:
+        assert src.tolist() == e["vogel_src"]
+        assert dst.tolist() == e["vogel_dst"]
+        assert np.array_equal(q, np.asarray(e["vogel_qty"], np.float32))
+    else:   # undefined in the reference from the first marked step on
+        k = int(np.argmax(src < 0))
+        assert src[:k].tolist() == e["vogel_src"][:k]
+        return
+    r = oracle.solve_ref(s, d, cf)
+    assert r["iterations"] == e["iterations"]
+    assert r["status"] == e["status"]
+    assert r["objective"] == e["objective"]
+    assert r["active"] == e["active"]
+
+
+@pytest.mark.parametrize("e", load("reference_fixtures.json"), ids=lambda e: e["file"])
+def test_reference_fixtures(orc, e):
+    s = np.array(e["supply"], np.int32)
+    d = np.array(e["demand"], np.int32)
+    cf = np.array(e["cost_f32"], np.float32) if "cost_f32" in e else float_costs(e["cost"], e["scale"])
+    check_against(e, s, d, cf)
+
+
+def test_reference_random(orc):
+    g = load("reference_random.json")
+    insts = tiny(g["seed"], g["count"], g["max_dim"])
+    for (s, d, c), e in zip(insts, g["results"]):
+        check_against(e, s, d, c.astype(np.float32))
+
+
+def test_reference_synthetic(orc):
+    fg = pytest.importorskip("flock_gb300")
+    from golden_util import checksum
+    for e in load("reference_synthetic.json"):
+        inst = fg.config_instance(e["name"], e["seed"], m=e["m"], n=e["n"])
+        assert checksum(inst.supply, inst.demand, inst.cost) == e["checksum"]
+        check_against(e, inst.supply, inst.demand, inst.cost.astype(np.float32))
+
+
+def test_known_optima(orc):
+    # integer fixtures: optimum also confirmed with an LP solver
+    known = {"test_simple1_degenerate.dat": 92, "test_simple2.dat": 743, "test_simple4.dat": 555,
+             "test_TransportModel_10_10_0.dat": 13084, "test_TransportModel_100_100_0.dat": 64823}
+    for e in load("reference_fixtures.json"):
+        if e["file"] in known:
+            r = oracle.solve_ref(np.array(e["supply"], np.int32), np.array(e["demand"], np.int32),
+                                 float_costs(e["cost"], 0))
+            assert r["status"] == 0 and r["objective"] == known[e["file"]]
+
+
+def _published_data_files():
+    d = os.path.join(REFERENCE, "data")
+    if not os.path.isdir(d):
+        return []
+    pub = load("published.json")["pure_sequencial"]
+    out = []
+    for f, v in sorted(pub.items()):
+        p = os.path.join(d, f)
+        if os.path.exists(p) and os.path.getsize(p) < 500_000:
+            out.append((p, v))
+    return out
+
+
+@pytest.mark.parametrize("path,pub", _published_data_files(), ids=lambda x: os.path.basename(str(x)))
+def test_published_cpu_path(orc, path, pub):
+    """Iterations and objective of results/pure_sequencial, reproduced."""
+    tok = open(path).read().split()
+    m, n = int(tok[0]), int(tok[1])
+    s = np.array(tok[2:2 + m], np.int32)
+    d = np.array(tok[2 + m:2 + m + n], np.int32)
+    c = np.array([float(x) for x in tok[2 + m + n:]], np.float32)
+    r = oracle.solve_ref(s, d, c)
+    assert r["iterations"] == pub["iterations"]
+    assert "%g" % r["objective"] == pub["objective"]
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference build not present")
+def test_live_reference_build(orc):
+    """The restatement against the reference's own compiled functions."""
+    rng = np.random.default_rng(77)
+    for (s, d, c) in tiny(4242, 200):
+        cf = c.astype(np.float32)
+        a = oracle.ref_vogel(s, d, cf)
+        b = oracle.vogel(s, d, cf)
+        if b[3] < 0:
+            continue
+        for x, y in zip(a, b[:3]):
+            assert np.array_equal(x, y)
+        ra, rb = oracle.ref_solve(s, d, cf), oracle.solve_ref(s, d, cf)
+        assert (ra["iterations"], ra["status"], ra["objective"]) == (rb["iterations"], rb["status"], rb["objective"])
+    del rng
+
+
+def test_certificate_checker_plants(orc):
+    """Mistakes planted in the checker's inputs are all caught."""
+    e = [x for x in load("reference_fixtures.json") if x["file"] == "test_TransportModel_10_10_0.dat"][0]
+    s = np.array(e["supply"], np.int32)
+    d = np.array(e["demand"], np.int32)
+    c = np.array(e["cost"], np.int32).reshape(e["m"], e["n"])
+    r = oracle.solve_ref(s, d, c.astype(np.float32))
+    ok, u, v = oracle.tree_duals(c, r["tree"])
+    assert ok == 0
+    flows = r["flows"]
+    bits, obj = oracle.certify(s, d, c, flows, u, v)
+    assert bits == 0 and obj == 13084
+    f = flows.copy(); f[0, 2] = -1
+    assert oracle.certify(s, d, c, f, u, v)[0] & 1
+    f = flows.copy(); f[0, 2] += 1
+    assert oracle.certify(s, d, c, f, u, v)[0] & 6
+    u2 = u.copy(); u2[0] += 1000
+    assert oracle.certify(s, d, c, flows, u2, v)[0] & 8
+    u3 = u.copy(); u3[int(flows[0, 0])] -= 1
+    assert oracle.certify(s, d, c, flows, u3, v)[0] & 16
