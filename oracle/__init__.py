@@ -198,3 +198,19 @@ def ref_solve(s, d, c, max_iter: int = 30000):
     a = act.value
     return dict(iterations=it.value, status=st.value, objective=obj.value, active=a,
                 flows=np.stack([fs[:a], fd[:a], fq[:a].astype(np.int64)], 1))
+
+
+def verdict(s, d, c_int, r):
+    """Classify a result of solve_ref with the exact certificate:
+    'optimal' (its basis is a spanning tree whose exact duals certify the
+    flows), 'feasible' (flows satisfy every constraint, not certified),
+    'infeasible', or 'stopped' (forest guard / cap with infeasible flows)."""
+    c = np.asarray(c_int, dtype=np.int32).reshape(len(s), len(d))
+    ok, u, v = tree_duals(c, r["tree"])
+    bits, _ = certify(s, d, c, r["flows"], u, v)
+    if ok == 0 and bits == 0 and r["status"] == 0:
+        return "optimal"
+    if bits & 7 == 0:
+        return "feasible"
+    return "infeasible" if r["status"] == 0 else "stopped"
+
