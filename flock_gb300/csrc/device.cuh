@@ -48,7 +48,7 @@ struct Scalars {
     int64_t M;             // perturbation scale
     int64_t neg_cells;     // certificate: cells with negative reduced cost
     int32_t last_winners;
-    int32_t pad;
+    int32_t fail_site;     // first failed internal check (0: none), see fail_check
 };
 
 // One instance as the kernels see it.
@@ -96,6 +96,16 @@ struct Ctx {
 };
 
 // --------------------------------------------------------------- helpers ---
+#define FLOCK_IN(x, V) ((unsigned)(x) < (unsigned)(V))
+
+// An internal index check failed: record the first failing site, mark the
+// solve corrupt and stop it.  The caller skips the access.
+__device__ __forceinline__ void fail_check(Scalars* sc, int site) {
+    atomicCAS(&sc->fail_site, 0, site);
+    atomicOr(&sc->status, ST_TREE_CORRUPT);
+    atomicExch(&sc->done, 1);
+}
+
 __device__ __forceinline__ int32_t f2i_x86(float f) {
     // float -> int as x86 cvttss2si: truncation, INT_MIN for NaN/out of range.
     if (!(f < 2147483648.0f) || !(f >= -2147483648.0f)) return INT32_MIN;

@@ -150,6 +150,14 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
         __syncthreads();
         if (idx >= a.count) break;
         const BatchDesc d = a.desc[idx];
+        if (d.m < 1 || d.n < 1 || d.m + d.n > a.maxV || d.m > a.maxM || d.ldc < d.n || (d.ldc & 3) ||
+            (d.cost_off & 3)) {
+            if (threadIdx.x == 0) {
+                a.sc[d.index].status = ST_TREE_CORRUPT;
+                a.sc[d.index].fail_site = 1;
+            }
+            continue;
+        }
         Ctx c;
         c.I.m = d.m; c.I.n = d.n; c.I.ldc = d.ldc;
         c.I.cost = a.cost + d.cost_off;
@@ -432,7 +440,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     int status = S.status & kFailMask;
     if (opt.verify && S.cert) status |= ST_CERT_FAIL;
     if (st) {
-        st->notes = S.status & ~kFailMask;
+        st->notes = (S.status & ~kFailMask) | (S.fail_site << 8);
         st->objective = S.objective;
         st->iterations = S.rounds;
         st->pivots = S.pivots;
@@ -786,7 +794,7 @@ struct BatchRunner {
         if (st_out) {
             int status = S.status & kFailMask;
             if (opt.verify && S.cert) status |= ST_CERT_FAIL;
-            st_out->notes = S.status & ~kFailMask;
+            st_out->notes = (S.status & ~kFailMask) | (S.fail_site << 8);
             st_out->objective = S.objective;
             st_out->iterations = S.rounds;
             st_out->pivots = S.pivots;

@@ -162,6 +162,7 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
             const int p = c.order[qh++];
             for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
                 const int ch = c.csr_adj[e];
+                if (!FLOCK_IN(ch, V) || qt >= V) { fail_check(c.sc, 31); break; }
                 if (c.parent[ch] == -2 && ch != root) { c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch; }
             }
         }
@@ -196,7 +197,8 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
                 best = k < best ? k : best;
             }
         best = block_min_u64(best, bs);
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && (best == kNoKey || !FLOCK_IN(rc, m) || bs.i[2] >= V)) fail_check(c.sc, 33);
+        if (threadIdx.x == 0 && !(best == kNoKey || !FLOCK_IN(rc, m) || bs.i[2] >= V)) {
             const int js = m + (int)key_idx(best);
             int qt = bs.i[2];
             int qh = qt;
@@ -207,6 +209,7 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
                 const int p = c.order[qh++];
                 for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
                     const int ch = c.csr_adj[e];
+                    if (!FLOCK_IN(ch, V) || qt >= V) { fail_check(c.sc, 32); break; }
                     if (c.parent[ch] == -2 && ch != root) { c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch; }
                 }
             }
@@ -251,6 +254,7 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
         const int p = c.parent[v];
         if (p == -2) { c.anc0[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
         else if (v == root) { c.anc0[v] = v; c.len0[v] = 0; c.acc0[v] = 0; }
+        else if (!FLOCK_IN(p, V) || (p < I.m) == (v < I.m)) { fail_check(c.sc, 20); c.anc0[v] = root; c.len0[v] = 0; c.acc0[v] = 0; }
         else { c.anc0[v] = p; c.len0[v] = 1; c.acc0[v] = edge_cost(I, v, p); }
     }
     int32_t* aA = c.anc0; int32_t* aB = c.anc1;
@@ -263,7 +267,9 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
         for (int v = threadIdx.x; v < V; v += blockDim.x) {
             const int a = aA[v];
             if (a < 0 || a == root) { aB[v] = a; lB[v] = lA[v]; xB[v] = xA[v]; continue; }
+            if (!FLOCK_IN(a, V)) { fail_check(c.sc, 21); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
             const int aa = aA[a];
+            if (!FLOCK_IN(aa, V)) { fail_check(c.sc, 22); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
             const int la = lA[v];
             aB[v] = aa;
             lB[v] = la + lA[a];
@@ -336,7 +342,7 @@ __device__ __forceinline__ CycleResult cycle_walk(const Ctx& c, int k, int l, ui
     CycleResult res;
     res.ok = 1;
     while (x != y) {
-        if (++steps > 2 * V) { res.ok = 0; break; }
+        if (++steps > 2 * V || !FLOCK_IN(x, V) || !FLOCK_IN(y, V)) { res.ok = 0; fail_check(c.sc, 11); break; }
         const int dx = c.depth[x], dy = c.depth[y];
         if (dx >= dy) {
             if (x < m) { const int64_t f = c.flow[x]; if (f < bk) { bk = f; qk = x; } }
@@ -348,7 +354,6 @@ __device__ __forceinline__ CycleResult cycle_walk(const Ctx& c, int k, int l, ui
             if (P != kNoKey) atomicMin((unsigned long long*)&c.claim[y], (unsigned long long)P);
             y = c.parent[y];
         }
-        if (x < 0 || y < 0) { res.ok = 0; break; }
     }
     if (bl <= bk) { res.theta = bl; res.q = ql; res.lside = 1; }
     else          { res.theta = bk; res.q = qk; res.lside = 0; }
@@ -359,11 +364,10 @@ __device__ __forceinline__ CycleResult cycle_walk(const Ctx& c, int k, int l, ui
 __device__ __forceinline__ bool cycle_owned(const Ctx& c, int k, int l, uint64_t P, int V) {
     int x = k, y = l, steps = 0;
     while (x != y) {
-        if (++steps > 2 * V) return false;
+        if (++steps > 2 * V || !FLOCK_IN(x, V) || !FLOCK_IN(y, V)) { fail_check(c.sc, 12); return false; }
         const int dx = c.depth[x], dy = c.depth[y];
         if (dx >= dy) { if (c.claim[x] != P) return false; x = c.parent[x]; }
         if (dy >= dx) { if (c.claim[y] != P) return false; y = c.parent[y]; }
-        if (x < 0 || y < 0) return false;
     }
     return true;
 }
@@ -372,7 +376,8 @@ __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const Cy
     const int m = c.I.m;
     const int64_t th = cr.theta;
     int x = k, y = l, steps = 0;
-    while (x != y && ++steps <= 2 * V) {
+    while (x != y) {
+        if (++steps > 2 * V || !FLOCK_IN(x, V) || !FLOCK_IN(y, V)) { fail_check(c.sc, 13); return; }
         const int dx = c.depth[x], dy = c.depth[y];
         if (dx >= dy) { c.flow[x] += (x < m) ? -th : th; x = c.parent[x]; }
         if (dy >= dx) { c.flow[y] += (y >= m) ? -th : th; y = c.parent[y]; }
@@ -382,12 +387,14 @@ __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const Cy
     int prev = cr.lside ? k : l;
     int64_t pf = th;
     for (int s = 0; s <= V; s++) {
+        if (!FLOCK_IN(v, V)) { fail_check(c.sc, 14); return; }
         const int nxt = c.parent[v];
         const int64_t f = c.flow[v];
         c.parent[v] = prev;
         c.flow[v] = pf;
         if (v == cr.q) break;
         prev = v; pf = f; v = nxt;
+        if (s == V) fail_check(c.sc, 15);
     }
 }
 
@@ -498,6 +505,7 @@ __device__ void finalize_cta(const Ctx& c, BlockScratch& bs) {
         if (v == root) continue;
         const int k = v < root ? v : v - 1;
         const int p = c.parent[v];
+        if (!FLOCK_IN(p, V) || (p < m) == (v < m)) { fail_check(c.sc, 41); continue; }
         const int row = v < m ? v : p, col = v < m ? p - m : v - m;
         const int64_t x = (c.flow[v] + half) / M;   // flow = M x + t, |t| <= V'-1 < M/2
         c.out_src[k] = row; c.out_dst[k] = col; c.out_qty[k] = (int32_t)x;

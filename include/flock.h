@@ -95,7 +95,7 @@ typedef struct {
     int32_t pivots;          /* pivots applied */
     int32_t active_flows;    /* nonzero flows written to `flows` */
     int32_t status;          /* FLOCK_ST_* failure bits, 0 = optimal */
-    int32_t notes;           /* FLOCK_NOTE_* bits */
+    int32_t notes;           /* FLOCK_NOTE_* bits; bits 8+: internal check site on failure */
     int32_t certified;       /* 1: certificate checked and passed */
     int32_t vogel_events;    /* Vogel steps whose line had no uncovered cell; -1 undefined */
     double ms_total;         /* wall time of the call (ms) */

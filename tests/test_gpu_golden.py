@@ -65,6 +65,8 @@ def test_reference_random():
         res = fg.solve(inst)
         certified(inst, res)
         live = oracle.solve_ref(s, d, c)      # pinned to the golden entry by test_oracle_pin
+        if live["status"] == 3:               # undefined in the reference (out-of-range index)
+            continue
         assert live["objective"] == e["objective"]
         v = oracle.verdict(s, d, c, live)
         if v == "optimal":
