@@ -100,7 +100,7 @@ def lib() -> ctypes.CDLL:
     L.flock_server_destroy.argtypes = [ctypes.c_void_p]
     L.flock_default_server_config.argtypes = [P(CServerConfig)]
     L.flock_default_options.argtypes = [P(COptions)]
-    L.flock_bench_batch_rerun.argtypes = [P(ctypes.c_float)]
+    L.flock_bench_batch_rerun.argtypes = [P(ctypes.c_float), P(i32)]
     _lib = L
     return L
 
@@ -286,14 +286,15 @@ def batch_solve(insts: Sequence[Instance], bfs: str = "vogel", pivot: str = "par
     return out
 
 
-def bench_batch_rerun_ms() -> float:
+def bench_batch_rerun() -> Tuple[float, int]:
     """Benchmark hook: device time (ms) of re-solving the last batch with its
-    inputs already resident on the GPU."""
+    inputs already resident on the GPU, and the kernels it launched."""
     ms = ctypes.c_float()
-    rc = lib().flock_bench_batch_rerun(ctypes.byref(ms))
+    n = i32()
+    rc = lib().flock_bench_batch_rerun(ctypes.byref(ms), ctypes.byref(n))
     if rc:
         raise _err(rc)
-    return float(ms.value)
+    return float(ms.value), int(n.value)
 
 
 class Server:

@@ -23,9 +23,7 @@ struct BatchRunner;
 BatchRunner* batch_runner_new();
 void batch_runner_free(BatchRunner* r);
 int batch_runner_prepare(BatchRunner* r, int cnt, const flock_instance* insts, const flock_options* o);
-int batch_runner_launch(BatchRunner* r);
-int batch_runner_wait(BatchRunner* r);
-bool batch_runner_ready(BatchRunner* r);
+int batch_runner_solve(BatchRunner* r);
 void batch_runner_collect(BatchRunner* r, int k, flock_flow* flows, flock_stats* st);
 }  // namespace flock
 
@@ -252,11 +250,12 @@ int flock_generate_sizes(uint64_t seed, int32_t count, int32_t lo, int32_t hi, i
 }  // extern "C"
 
 // ================================================================ server ===
-// Requests are copied at submit.  A worker thread retires finished launches
-// and admits waiting requests (FIFO) into free launch slots while the summed
-// resident estimate stays within the budget.  Each slot is one batched launch
-// on its own streams, so requests arriving while others run are admitted as
-// slots and memory free up and overlap with them on the device.
+// Requests are copied at submit.  A dispatcher thread admits waiting requests
+// (FIFO) into free launch slots while the summed resident estimate stays
+// within the budget.  Each slot has its own thread, batch runner and CUDA
+// streams, so a slot solving one group of requests overlaps on the device
+// with the other slots; requests arriving meanwhile are admitted into the
+// next slot that frees up.
 struct flock_server {
     struct Req {
         uint64_t ticket;
@@ -272,11 +271,13 @@ struct flock_server {
     struct Slot {
         flock::BatchRunner* runner = nullptr;
         std::vector<Req> reqs;
-        bool busy = false;
+        bool busy = false;      // assigned requests, running or about to run
+        std::thread th;
     };
     flock_server_config cfg;
     std::mutex mu;
-    std::condition_variable cv;
+    std::condition_variable cv;        // dispatcher and slot threads wait here
+    std::condition_variable cv_done;   // drain waits here
     std::deque<Req> pending;
     std::deque<Done> done;
     std::vector<Slot> slots;
@@ -284,47 +285,63 @@ struct flock_server {
     uint64_t next_ticket = 1;
     int64_t submitted = 0, finished = 0;
     bool stop = false;
-    std::thread worker;
+    std::thread dispatcher;
 
     static int64_t estimate(int m, int n) {
         const int64_t ldc = (n + 3) & ~3;
         return 4 * (int64_t)m * ldc + 256 * (int64_t)(m + n) + 4096;
     }
 
-    void run() {
+    void slot_loop(int id) {
+        Slot& sl = slots[id];
         std::unique_lock<std::mutex> lk(mu);
-        while (true) {
-            bool progressed = false;
-            // retire
-            for (auto& sl : slots) {
-                if (!sl.busy) continue;
-                lk.unlock();
-                const bool ready = flock::batch_runner_ready(sl.runner);
-                lk.lock();
-                if (!ready) continue;
-                lk.unlock();
-                flock::batch_runner_wait(sl.runner);
-                std::vector<Done> out(sl.reqs.size());
-                const auto now = std::chrono::steady_clock::now();
-                for (size_t k = 0; k < sl.reqs.size(); k++) {
-                    Done& d = out[k];
-                    d.flows.resize((size_t)sl.reqs[k].m + sl.reqs[k].n - 1);
+        for (;;) {
+            cv.wait(lk, [&] { return stop || (sl.busy && !sl.reqs.empty()); });
+            if (!(sl.busy && !sl.reqs.empty())) { if (stop) return; continue; }
+            std::vector<Req> reqs = std::move(sl.reqs);
+            sl.reqs.clear();
+            lk.unlock();
+            std::vector<flock_instance> insts(reqs.size());
+            for (size_t k = 0; k < reqs.size(); k++)
+                insts[k] = {reqs[k].m, reqs[k].n, reqs[k].s.data(), reqs[k].d.data(), reqs[k].c.data()};
+            int rc = flock::batch_runner_prepare(sl.runner, (int)insts.size(), insts.data(), &cfg.options);
+            if (!rc) rc = flock::batch_runner_solve(sl.runner);
+            const auto now = std::chrono::steady_clock::now();
+            std::vector<Done> out(reqs.size());
+            for (size_t k = 0; k < reqs.size(); k++) {
+                Done& d = out[k];
+                memset(&d.res, 0, sizeof(d.res));
+                d.res.ticket = reqs[k].ticket;
+                if (rc) {
+                    d.res.status = rc;
+                } else {
+                    d.flows.assign((size_t)reqs[k].m + reqs[k].n - 1, flock_flow{0, 0, 0});
                     flock::batch_runner_collect(sl.runner, (int)k, d.flows.data(), &d.res.stats);
-                    d.res.ticket = sl.reqs[k].ticket;
                     d.res.status = d.res.stats.status ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
-                    d.res.latency_ms = std::chrono::duration<double, std::milli>(now - sl.reqs[k].t_submit).count();
-                    d.res.stats.ms_total = d.res.latency_ms;
                 }
-                lk.lock();
-                for (auto& r : sl.reqs) resident -= r.bytes;
-                for (auto& d : out) done.push_back(std::move(d));
-                finished += (int64_t)sl.reqs.size();
-                sl.reqs.clear();
-                sl.busy = false;
-                progressed = true;
-                cv.notify_all();
+                d.res.latency_ms = std::chrono::duration<double, std::milli>(now - reqs[k].t_submit).count();
+                d.res.stats.ms_total = d.res.latency_ms;
             }
-            // admit
+            lk.lock();
+            for (auto& r : reqs) resident -= r.bytes;
+            for (auto& d : out) done.push_back(std::move(d));
+            finished += (int64_t)reqs.size();
+            sl.busy = false;
+            cv.notify_all();
+            cv_done.notify_all();
+        }
+    }
+
+    void dispatch_loop() {
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv.wait(lk, [&] {
+                if (stop) return true;
+                if (pending.empty()) return false;
+                for (auto& sl : slots) if (!sl.busy) return true;
+                return false;
+            });
+            if (stop) return;
             for (auto& sl : slots) {
                 if (sl.busy || pending.empty()) continue;
                 std::vector<Req> take;
@@ -334,44 +351,13 @@ struct flock_server {
                     take.push_back(std::move(pending.front()));
                     pending.pop_front();
                 }
-                if (take.empty()) break;
+                if (take.empty()) break;    // the budget is full: wait for a slot to retire
                 sl.reqs = std::move(take);
                 sl.busy = true;
-                std::vector<flock_instance> insts(sl.reqs.size());
-                for (size_t k = 0; k < sl.reqs.size(); k++)
-                    insts[k] = {sl.reqs[k].m, sl.reqs[k].n, sl.reqs[k].s.data(), sl.reqs[k].d.data(), sl.reqs[k].c.data()};
-                lk.unlock();
-                int rc = flock::batch_runner_prepare(sl.runner, (int)insts.size(), insts.data(), &cfg.options);
-                if (!rc) rc = flock::batch_runner_launch(sl.runner);
-                lk.lock();
-                if (rc) {   // report the failure for every request of the launch
-                    for (auto& r : sl.reqs) {
-                        Done d;
-                        memset(&d.res, 0, sizeof(d.res));
-                        d.res.ticket = r.ticket;
-                        d.res.status = rc;
-                        resident -= r.bytes;
-                        done.push_back(std::move(d));
-                        finished++;
-                    }
-                    sl.reqs.clear();
-                    sl.busy = false;
-                    cv.notify_all();
-                }
-                progressed = true;
             }
-            bool any_busy = false;
-            for (auto& sl : slots) any_busy |= sl.busy;
-            if (stop && pending.empty() && !any_busy) break;
-            if (!progressed) {
-                if (any_busy) {
-                    lk.unlock();
-                    std::this_thread::sleep_for(std::chrono::microseconds(50));
-                    lk.lock();
-                } else {
-                    cv.wait_for(lk, std::chrono::milliseconds(5));
-                }
-            }
+            cv.notify_all();
+            // nothing admitted (budget full): wait for a retirement
+            cv.wait_for(lk, std::chrono::milliseconds(1));
         }
     }
 };
@@ -393,8 +379,11 @@ int flock_server_create(const flock_server_config* cfg, flock_server** out) {
     if (s->cfg.max_inflight_batches < 1) s->cfg.max_inflight_batches = 1;
     if (s->cfg.max_batch < 1) s->cfg.max_batch = 1;
     s->slots.resize(s->cfg.max_inflight_batches);
-    for (auto& sl : s->slots) sl.runner = flock::batch_runner_new();
-    s->worker = std::thread([s] { s->run(); });
+    for (size_t k = 0; k < s->slots.size(); k++) {
+        s->slots[k].runner = flock::batch_runner_new();
+        s->slots[k].th = std::thread([s, k] { s->slot_loop((int)k); });
+    }
+    s->dispatcher = std::thread([s] { s->dispatch_loop(); });
     *out = s;
     return FLOCK_OK;
 }
@@ -437,18 +426,20 @@ int flock_server_poll(flock_server* s, flock_result* results, flock_flow** flows
 int flock_server_drain(flock_server* s) {
     if (!s) return FLOCK_ERR_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
-    s->cv.wait(lk, [s] { return s->finished >= s->submitted; });
+    s->cv_done.wait(lk, [s] { return s->finished >= s->submitted; });
     return FLOCK_OK;
 }
 
 int flock_server_destroy(flock_server* s) {
     if (!s) return FLOCK_ERR_ARG;
+    flock_server_drain(s);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
         s->cv.notify_all();
     }
-    if (s->worker.joinable()) s->worker.join();
+    if (s->dispatcher.joinable()) s->dispatcher.join();
+    for (auto& sl : s->slots) if (sl.th.joinable()) sl.th.join();
     for (auto& sl : s->slots) flock::batch_runner_free(sl.runner);
     delete s;
     return FLOCK_OK;

@@ -14,22 +14,22 @@ struct BatchDesc {
     int64_t sd_off;             // supply at sd_off, demand at sd_off + m
     int64_t out_off;            // first basis cell in the output arena
     int64_t pot_off;            // first dual in the dual arena
+    int64_t ws_off;             // the instance's working set in the state arena (bytes)
 };
 
 struct BatchArgs {
     const BatchDesc* desc;
     int32_t count;
-    int32_t* next;              // work-stealing counter
+    int32_t* next;              // work-stealing counter of this launch (zeroed before it)
+    int32_t* active;            // round kernel: instances still running after the round
     const int32_t* cost;
     const int32_t* sd;
     int32_t* out_src; int32_t* out_dst; int32_t* out_qty;
     int32_t* bfs_out;           // 3 ints per cell: Vogel / NW-corner allocation list
     int64_t* pot_out;
     Scalars* sc;
-    uint8_t* scratch;           // per-CTA global scratch
-    size_t scratch_per_cta;
-    int32_t maxV, maxM;
-    int32_t smem_mode;
+    uint8_t* ws;                // per-instance working sets
+    int32_t maxV, maxM;         // largest instance of the launch (shared-memory staging size)
     int32_t bfs_method, mode, max_rounds;
 };
 

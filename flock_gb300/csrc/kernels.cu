@@ -9,8 +9,10 @@
 //     k_pivot <<<1 CTA>>>   candidates, cycle walks, atomicMin claims, apply, duals
 //   k_finalize<<<1 CTA>>>   original flows, zero-demand columns, objective, flow certificate
 //   k_cert_cells<<<grid>>>  certificate: every reduced cost >= 0
-// Batched path: k_batch, one CTA per instance with work stealing over a
-// size-sorted queue; one launch (stream) per size bucket.
+// Batched path: per size bucket, k_bsetup, then chunks of k_bround (one
+// pricing round of every active instance, work stealing, tree staged in
+// shared memory) captured as CUDA graphs, then k_bfinal; buckets run
+// concurrently on their own streams.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -137,37 +139,52 @@ __global__ void k_fill_bench(int32_t* cost, size_t cells, int64_t* pot, int V) {
         pot[k] = (int64_t)((k * 40503u) % 700u);
 }
 
-// ------------------------------------------------------- batched kernel ----
-__global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
+
+// ------------------------------------------------------- batched kernels ---
+// The batched form runs many instances side by side, one CTA per instance at
+// a time, with work stealing over a size bucket's instance list:
+//   k_bsetup  Vogel (or NW corner) and the strongly feasible start tree, per
+//             instance, in the instance's global working set
+//   k_bround  ONE pricing round of every active instance: the tree arrays are
+//             staged into shared memory, duals recomputed, the CTA-local sweep
+//             and the deconflicted pivots run there, and parent/flow/duals are
+//             written back; the host captures chunks of rounds in a CUDA graph
+//   k_bfinal  original flows, objective and the exact certificate
+__device__ __forceinline__ bool batch_desc_ok(const BatchArgs& a, const BatchDesc& d) {
+    return d.m >= 1 && d.n >= 1 && d.m + d.n <= a.maxV && d.m <= a.maxM && d.ldc >= d.n && !(d.ldc & 3) &&
+           !(d.cost_off & 3) && !(d.ws_off & 255);
+}
+
+__device__ __forceinline__ void batch_ctx(const BatchArgs& a, const BatchDesc& d, Ctx& g) {
+    g.I.m = d.m; g.I.n = d.n; g.I.ldc = d.ldc;
+    g.I.cost = a.cost + d.cost_off;
+    g.I.supply = a.sd + d.sd_off;
+    g.I.demand = a.sd + d.sd_off + d.m;
+    g.sc = a.sc + d.index;
+    g.out_src = a.out_src + d.out_off; g.out_dst = a.out_dst + d.out_off; g.out_qty = a.out_qty + d.out_off;
+    carve_ctx(g, a.ws + d.ws_off, d.m + d.n, d.m, nullptr, a.pot_out + d.pot_off);
+}
+
+// returns the next instance of this launch for the CTA, or -1
+__device__ __forceinline__ int batch_next(const BatchArgs& a, int* s_idx) {
+    if (threadIdx.x == 0) *s_idx = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int idx = *s_idx;
+    __syncthreads();
+    return idx < a.count ? idx : -1;
+}
+
+__global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
     __shared__ BlockScratch bs;
     __shared__ int s_idx;
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint8_t* scratch = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
-    for (;;) {
-        if (threadIdx.x == 0) s_idx = atomicAdd(a.next, 1);
-        __syncthreads();
-        const int idx = s_idx;
-        __syncthreads();
-        if (idx >= a.count) break;
+    for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
-        if (d.m < 1 || d.n < 1 || d.m + d.n > a.maxV || d.m > a.maxM || d.ldc < d.n || (d.ldc & 3) ||
-            (d.cost_off & 3)) {
-            if (threadIdx.x == 0) {
-                a.sc[d.index].status = ST_TREE_CORRUPT;
-                a.sc[d.index].fail_site = 1;
-            }
+        if (!batch_desc_ok(a, d)) {
+            if (threadIdx.x == 0) { a.sc[d.index].status = ST_TREE_CORRUPT; a.sc[d.index].fail_site = 1; a.sc[d.index].done = 1; }
             continue;
         }
         Ctx c;
-        c.I.m = d.m; c.I.n = d.n; c.I.ldc = d.ldc;
-        c.I.cost = a.cost + d.cost_off;
-        c.I.supply = a.sd + d.sd_off;
-        c.I.demand = a.sd + d.sd_off + d.m;
-        c.sc = a.sc + d.index;
-        const int V = d.m + d.n;
-        c.out_src = a.out_src + d.out_off; c.out_dst = a.out_dst + d.out_off; c.out_qty = a.out_qty + d.out_off;
-        int64_t* pot_global = a.pot_out + d.pot_off;
-        carve_ctx(c, scratch, a.maxV, a.maxM, a.smem_mode ? smem : nullptr, pot_global);
+        batch_ctx(a, d, c);
         if (threadIdx.x == 0) {
             Scalars z;
             memset(&z, 0, sizeof(z));
@@ -183,7 +200,7 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
             __syncthreads();
         }
         if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
-        // the start list is needed later only for the Vogel output: keep it
+        const int V = d.m + d.n;
         for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
             a.bfs_out[3 * (d.out_off + k) + 0] = c.bfs_src[k];
             a.bfs_out[3 * (d.out_off + k) + 1] = c.bfs_dst[k];
@@ -191,27 +208,78 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
         }
         __syncthreads();
         sf_init_cta(c, bs);
-        if (!c.sc->done) tree_recompute_cta(c, bs);
-        for (int guard = 0; guard < (1 << 30); guard++) {
-            if (c.sc->done) break;
+    }
+}
+
+// shared-memory staging of the arrays every pivot step touches
+__device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
+    Carver k{nullptr, 0, smem, 0};
+    c.parent = (int32_t*)k.S(4 * (size_t)V);
+    c.depth = (int32_t*)k.S(4 * (size_t)V);
+    c.flow = (int64_t*)k.S(8 * (size_t)V);
+    c.claim = (uint64_t*)k.S(8 * (size_t)V);
+    c.anc0 = (int32_t*)k.S(4 * (size_t)V);
+    c.anc1 = (int32_t*)k.S(4 * (size_t)V);
+    c.len0 = (int32_t*)k.S(4 * (size_t)V);
+    c.len1 = (int32_t*)k.S(4 * (size_t)V);
+    c.acc0 = (int64_t*)k.S(8 * (size_t)V);
+    c.acc1 = (int64_t*)k.S(8 * (size_t)V);
+    c.row_best = (uint64_t*)k.S(8 * (size_t)M);
+    c.pot = (int64_t*)k.S(8 * (size_t)V);
+}
+
+__host__ __device__ inline size_t staged_bytes(int V, int M) {
+    Carver k{nullptr, 0, (unsigned char*)16, 0};
+    k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
+    k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V);
+    k.S(8 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
+    return (k.so + 15) & ~size_t(15);
+}
+
+__global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
+    __shared__ BlockScratch bs;
+    __shared__ int s_idx;
+    extern __shared__ __align__(16) unsigned char smem[];
+    for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
+        const BatchDesc d = a.desc[idx];
+        if (!batch_desc_ok(a, d)) continue;
+        if (a.sc[d.index].done) continue;          // every thread reads the same value
+        Ctx g;
+        batch_ctx(a, d, g);
+        Ctx c = g;
+        stage_hot(c, smem, a.maxV, a.maxM);
+        const int V = d.m + d.n;
+        for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
+        __syncthreads();
+        tree_recompute_cta(c, bs);
+        if (!c.sc->done) {
             sweep_cta(c);
             pivot_round_cta(c, bs);
-            if (threadIdx.x == 0) {
-                c.sc->rounds++;
-                if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
-            }
-            __syncthreads();
-            if (c.sc->done) break;
-            tree_recompute_cta(c, bs);
         }
-        if (!(c.sc->status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE))) {
-            finalize_cta(c, bs);
-            certify_flows_cta(c, bs);
-            certify_cells_cta(c, bs);
+        if (threadIdx.x == 0) {
+            c.sc->rounds++;
+            if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
+            if (!c.sc->done) atomicAdd(a.active, 1);
         }
-        if (a.smem_mode)
-            for (int v = threadIdx.x; v < V; v += blockDim.x) pot_global[v] = c.pot[v];
+        for (int v = threadIdx.x; v < V; v += blockDim.x) {
+            g.parent[v] = c.parent[v]; g.flow[v] = c.flow[v]; g.pot[v] = c.pot[v];
+        }
         __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bfinal(BatchArgs a) {
+    __shared__ BlockScratch bs;
+    __shared__ int s_idx;
+    for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
+        const BatchDesc d = a.desc[idx];
+        if (!batch_desc_ok(a, d)) continue;
+        if (a.sc[d.index].status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) continue;
+        Ctx c;
+        batch_ctx(a, d, c);
+        finalize_cta(c, bs);
+        certify_flows_cta(c, bs);
+        certify_cells_cta(c, bs);
     }
 }
 
@@ -522,118 +590,132 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 }
 
 // -------------------------------------------------------- batched solver ---
-static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 4096, 1 << 30};
-static const int kNumBuckets = 8;
+// Size buckets by V = m + n.  Instances above the last edge run on the plain
+// path (their staged tree would not fit in shared memory).
+static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 3072};
+static const int kNumBuckets = 7;
+static const int kMaxStagedV = 3072;
+static const int kMaxChunk = 64;
 
 static int bucket_of(int V) {
     int b = 0;
-    while (V > kBucketEdges[b]) b++;
-    return b;
+    while (b < kNumBuckets && V > kBucketEdges[b]) b++;
+    return b;   // kNumBuckets: plain path
 }
 
-struct TuneCfg { int threads; int smem; };
+// Launch configuration of a bucket.  threads: block size of the three
+// kernels; grid_mult: resident CTAs per SM multiplier for work stealing;
+// chunk: pricing rounds per graph launch.
+struct TuneCfg { int threads; int grid_mult; int chunk; };
 
 static std::mutex g_tune_mu;
 static TuneCfg g_tuned[kNumBuckets];
 static bool g_tuned_ok[kNumBuckets];
 
-static size_t batch_smem_bytes(int maxV, int maxM) {
-    Ctx probe;
-    size_t sb = 0;
-    carve_ctx(probe, nullptr, maxV, maxM, (unsigned char*)16, nullptr, &sb, nullptr);
-    return (sb + 15) & ~size_t(15);
-}
-static size_t batch_global_bytes(int maxV, int maxM, bool smem) {
-    Ctx probe;
-    size_t gb = 0;
-    carve_ctx(probe, nullptr, maxV, maxM, smem ? (unsigned char*)16 : nullptr, (int64_t*)16, nullptr, &gb);
-    return al256(gb);
-}
-
-static TuneCfg heuristic_cfg(int maxV, int maxM) {
+static TuneCfg default_cfg(int maxV) {
     TuneCfg t;
-    t.threads = maxV <= 256 ? 128 : (maxV <= 1024 ? 256 : 512);
-    t.smem = batch_smem_bytes(maxV, maxM) <= 100 * 1024 ? 1 : 0;
+    t.threads = maxV <= 256 ? 128 : 256;
+    t.grid_mult = 1;
+    t.chunk = 16;
     return t;
 }
 
+static size_t instance_ws_bytes(int V, int m) {
+    Ctx probe;
+    size_t gb = 0;
+    carve_ctx(probe, nullptr, V, m, nullptr, (int64_t*)16, nullptr, &gb);
+    return al256(gb);
+}
+
 struct BatchRunner {
-    DevBuf d_cost, d_sd, d_desc, d_out, d_bfs, d_pot, d_sc, d_next, d_scratch;
-    HostBuf h_cost, h_sd, h_desc, h_out, h_bfs, h_pot, h_sc;
+    DevBuf d_cost, d_sd, d_desc, d_out, d_bfs, d_pot, d_sc, d_ws, d_ctr;
+    HostBuf h_cost, h_sd, h_desc, h_out, h_sc, h_ctr;
     cudaStream_t st[kNumBuckets] = {};
-    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_done = nullptr, ev_join = nullptr;
     bool init = false;
     // per call
     int count = 0;
-    std::vector<int> V_of, m_of, n_of;
+    std::vector<int> V_of, m_of, n_of, plain_list;
     std::vector<int64_t> out_off, pot_off;
-    int64_t total_cells = 0, total_pot = 0, total_cost = 0, total_sd = 0;
+    int64_t total_cells = 0, total_pot = 0, total_cost = 0, total_sd = 0, total_ws = 0;
     std::vector<BatchDesc> descs;           // grouped by bucket
     int bstart[kNumBuckets + 1] = {};
     int bmaxV[kNumBuckets] = {}, bmaxM[kNumBuckets] = {};
     flock_options opt;
+    const flock_instance* insts = nullptr;
+    std::vector<flock_stats> plain_stats;
+    std::vector<std::vector<flock_flow>> plain_flows;
+    int32_t launches = 0;                   // kernels launched by the last run
 
     int setup() {
         if (init) return FLOCK_OK;
         for (auto& s : st) FLOCK_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         FLOCK_CK(cudaEventCreate(&ev_start));
         FLOCK_CK(cudaEventCreate(&ev_done));
-        FLOCK_CK(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        FLOCK_CK(d_next.ensure(kNumBuckets * sizeof(int32_t) * 32));
+        FLOCK_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+        FLOCK_CK(cudaFuncSetAttribute(k_bround, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+        FLOCK_CK(d_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
+        FLOCK_CK(h_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         init = true;
         return FLOCK_OK;
     }
 
     // Validate and stage the instances into pinned host memory.
-    int prepare(int cnt, const flock_instance* insts, const flock_options* opt_in) {
+    int prepare(int cnt, const flock_instance* in, const flock_options* opt_in) {
         int rc = setup();
         if (rc) return rc;
         flock_default_options(&opt);
         if (opt_in) opt = *opt_in;
+        insts = in;
         count = cnt;
         V_of.assign(cnt, 0); m_of.assign(cnt, 0); n_of.assign(cnt, 0);
         out_off.assign(cnt, 0); pot_off.assign(cnt, 0);
-        total_cells = total_pot = total_cost = total_sd = 0;
-        std::vector<int64_t> cost_off(cnt), sd_off(cnt);
+        plain_list.clear();
+        total_cells = total_pot = total_cost = total_sd = total_ws = 0;
+        std::vector<int64_t> cost_off(cnt), sd_off(cnt), ws_off(cnt);
         for (int k = 0; k < cnt; k++) {
-            if ((rc = validate_instance(&insts[k]))) return rc;
-            const int m = insts[k].m, n = insts[k].n;
+            if ((rc = validate_instance(&in[k]))) return rc;
+            const int m = in[k].m, n = in[k].n;
             m_of[k] = m; n_of[k] = n; V_of[k] = m + n;
+            out_off[k] = total_cells; total_cells += m + n - 1;
+            pot_off[k] = total_pot; total_pot += m + n;
+            if (m + n > kMaxStagedV) { plain_list.push_back(k); continue; }
             const int ldc = (n + 3) & ~3;
             cost_off[k] = total_cost; total_cost += (int64_t)m * ldc;
             sd_off[k] = total_sd; total_sd += m + n;
-            out_off[k] = total_cells; total_cells += m + n - 1;
-            pot_off[k] = total_pot; total_pot += m + n;
+            ws_off[k] = total_ws; total_ws += (int64_t)instance_ws_bytes(m + n, m);
         }
         FLOCK_CK(h_cost.ensure((size_t)total_cost * 4 + 16));
         FLOCK_CK(h_sd.ensure((size_t)total_sd * 4 + 16));
         for (int k = 0; k < cnt; k++) {
+            if (V_of[k] > kMaxStagedV) continue;
             const int m = m_of[k], n = n_of[k], ldc = (n + 3) & ~3;
             int32_t* dst = h_cost.as<int32_t>() + cost_off[k];
-            if (ldc == n) memcpy(dst, insts[k].cost, (size_t)m * n * 4);
+            if (ldc == n) memcpy(dst, in[k].cost, (size_t)m * n * 4);
             else for (int i = 0; i < m; i++) {
-                memcpy(dst + (size_t)i * ldc, insts[k].cost + (size_t)i * n, (size_t)n * 4);
+                memcpy(dst + (size_t)i * ldc, in[k].cost + (size_t)i * n, (size_t)n * 4);
                 memset(dst + (size_t)i * ldc + n, 0, (size_t)(ldc - n) * 4);
             }
-            memcpy(h_sd.as<int32_t>() + sd_off[k], insts[k].supply, (size_t)m * 4);
-            memcpy(h_sd.as<int32_t>() + sd_off[k] + m, insts[k].demand, (size_t)n * 4);
+            memcpy(h_sd.as<int32_t>() + sd_off[k], in[k].supply, (size_t)m * 4);
+            memcpy(h_sd.as<int32_t>() + sd_off[k] + m, in[k].demand, (size_t)n * 4);
         }
-        // bucket, largest first inside each bucket
-        std::vector<int> order(cnt);
-        for (int k = 0; k < cnt; k++) order[k] = k;
+        // bucket, largest first inside each bucket (work stealing starts with the long solves)
+        std::vector<int> order;
+        for (int k = 0; k < cnt; k++) if (V_of[k] <= kMaxStagedV) order.push_back(k);
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
             const int ba = bucket_of(V_of[a]), bb = bucket_of(V_of[b]);
             if (ba != bb) return ba < bb;
             return (int64_t)m_of[a] * n_of[a] > (int64_t)m_of[b] * n_of[b];
         });
-        descs.resize(cnt);
+        descs.resize(order.size());
         for (int b = 0; b <= kNumBuckets; b++) bstart[b] = 0;
         for (int b = 0; b < kNumBuckets; b++) { bmaxV[b] = 0; bmaxM[b] = 0; }
-        for (int q = 0; q < cnt; q++) {
+        for (size_t q = 0; q < order.size(); q++) {
             const int k = order[q];
             BatchDesc d;
             d.m = m_of[k]; d.n = n_of[k]; d.ldc = (n_of[k] + 3) & ~3; d.index = k;
             d.cost_off = cost_off[k]; d.sd_off = sd_off[k]; d.out_off = out_off[k]; d.pot_off = pot_off[k];
+            d.ws_off = ws_off[k];
             descs[q] = d;
             const int b = bucket_of(V_of[k]);
             bstart[b + 1]++;
@@ -647,45 +729,29 @@ struct BatchRunner {
     int ensure_device() {
         FLOCK_CK(d_cost.ensure((size_t)total_cost * 4 + 16));
         FLOCK_CK(d_sd.ensure((size_t)total_sd * 4 + 16));
-        FLOCK_CK(d_desc.ensure((size_t)count * sizeof(BatchDesc)));
+        FLOCK_CK(d_desc.ensure(std::max<size_t>(1, descs.size()) * sizeof(BatchDesc)));
         FLOCK_CK(d_out.ensure((size_t)total_cells * 12 + 16));
         FLOCK_CK(d_bfs.ensure((size_t)total_cells * 12 + 16));
         FLOCK_CK(d_pot.ensure((size_t)total_pot * 8 + 16));
         FLOCK_CK(d_sc.ensure((size_t)count * sizeof(Scalars)));
-        FLOCK_CK(h_desc.ensure((size_t)count * sizeof(BatchDesc)));
+        FLOCK_CK(d_ws.ensure((size_t)total_ws + 256));
+        FLOCK_CK(h_desc.ensure(std::max<size_t>(1, descs.size()) * sizeof(BatchDesc)));
         FLOCK_CK(h_out.ensure((size_t)total_cells * 12 + 16));
-        FLOCK_CK(h_bfs.ensure((size_t)total_cells * 12 + 16));
-        FLOCK_CK(h_pot.ensure((size_t)total_pot * 8 + 16));
         FLOCK_CK(h_sc.ensure((size_t)count * sizeof(Scalars)));
-        memcpy(h_desc.p, descs.data(), (size_t)count * sizeof(BatchDesc));
+        if (!descs.empty()) memcpy(h_desc.p, descs.data(), descs.size() * sizeof(BatchDesc));
         return FLOCK_OK;
     }
 
     TuneCfg cfg_for(int b) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        if (g_tuned_ok[b]) {
-            TuneCfg t = g_tuned[b];
-            if (t.smem && batch_smem_bytes(bmaxV[b], bmaxM[b]) > 200 * 1024) t.smem = 0;
-            return t;
-        }
-        return heuristic_cfg(bmaxV[b], bmaxM[b]);
+        return g_tuned_ok[b] ? g_tuned[b] : default_cfg(bmaxV[b]);
     }
 
-    // Launch the bucket [q0, q1) of descs on stream s with config t.
-    int launch_bucket(int b, int q0, int q1, TuneCfg t, cudaStream_t s, int32_t* next) {
-        if (q1 <= q0) return FLOCK_OK;
-        const int maxV = bmaxV[b], maxM = bmaxM[b];
-        const size_t smem = t.smem ? batch_smem_bytes(maxV, maxM) : 0;
-        int per_sm = 0;
-        FLOCK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, t.threads, smem));
-        if (per_sm < 1) per_sm = 1;
-        const int grid = std::max(1, std::min(q1 - q0, per_sm * num_sms()));
-        const size_t per_cta = batch_global_bytes(maxV, maxM, t.smem != 0);
-        (void)b;
+    BatchArgs args_for(int b) {
         BatchArgs a;
-        a.desc = d_desc.as<BatchDesc>() + q0;
-        a.count = q1 - q0;
-        a.next = next;
+        a.desc = d_desc.as<BatchDesc>() + bstart[b];
+        a.count = bstart[b + 1] - bstart[b];
+        a.next = nullptr; a.active = nullptr;
         a.cost = d_cost.as<int32_t>();
         a.sd = d_sd.as<int32_t>();
         a.out_src = d_out.as<int32_t>();
@@ -694,88 +760,98 @@ struct BatchRunner {
         a.bfs_out = d_bfs.as<int32_t>();
         a.pot_out = d_pot.as<int64_t>();
         a.sc = d_sc.as<Scalars>();
-        a.scratch_per_cta = per_cta;
-        a.maxV = maxV; a.maxM = maxM;
-        a.smem_mode = t.smem;
+        a.ws = d_ws.as<uint8_t>();
+        a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = opt.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : 1;
         a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
-        a.scratch = nullptr;
-        // scratch: one region per concurrent bucket launch, carved from d_scratch
-        a.scratch = scratch_base[b];
-        FLOCK_CK(cudaMemsetAsync(next, 0, sizeof(int32_t), s));
-        k_batch<<<grid, t.threads, smem, s>>>(a);
-        FLOCK_CK(cudaGetLastError());
-        return FLOCK_OK;
+        return a;
     }
 
-    uint8_t* scratch_base[kNumBuckets] = {};
+    int32_t* ctr(int b) { return d_ctr.as<int32_t>() + (size_t)b * 2 * kMaxChunk; }
 
-    int reserve_scratch(const TuneCfg* cfg) {
-        size_t total = 0;
-        size_t offs[kNumBuckets];
-        for (int b = 0; b < kNumBuckets; b++) {
-            offs[b] = total;
-            const int nb = bstart[b + 1] - bstart[b];
-            if (!nb) continue;
-            const size_t smem = cfg[b].smem ? batch_smem_bytes(bmaxV[b], bmaxM[b]) : 0;
-            int per_sm = 0;
-            FLOCK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, cfg[b].threads, smem));
-            if (per_sm < 1) per_sm = 1;
-            const int grid = std::max(1, std::min(nb, per_sm * num_sms()));
-            total += al256((size_t)grid * batch_global_bytes(bmaxV[b], bmaxM[b], cfg[b].smem != 0));
+    int grid_for(int b, const TuneCfg& t, size_t smem, const void* fn) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, smem);
+        if (per_sm < 1) per_sm = 1;
+        const int nb = bstart[b + 1] - bstart[b];
+        return std::max(1, std::min(nb, per_sm * num_sms() * t.grid_mult));
+    }
+
+    // Pricing rounds of bucket b as a CUDA graph: `chunk` x (zero the
+    // counters, one k_bround launch).
+    int capture_rounds(int b, const TuneCfg& t, cudaGraphExec_t* exec) {
+        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b]);
+        const int grid = grid_for(b, t, smem, (const void*)k_bround);
+        cudaStream_t s = st[b];
+        cudaGraph_t g;
+        FLOCK_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int r = 0; r < t.chunk; r++) {
+            BatchArgs a = args_for(b);
+            a.next = ctr(b) + r;
+            a.active = ctr(b) + kMaxChunk + r;
+            cudaMemsetAsync(a.next, 0, sizeof(int32_t), s);
+            cudaMemsetAsync(a.active, 0, sizeof(int32_t), s);
+            k_bround<<<grid, t.threads, smem, s>>>(a);
         }
-        FLOCK_CK(d_scratch.ensure(total + 256));
-        for (int b = 0; b < kNumBuckets; b++) scratch_base[b] = d_scratch.as<uint8_t>() + offs[b];
+        FLOCK_CK(cudaStreamEndCapture(s, &g));
+        FLOCK_CK(cudaGraphInstantiate(exec, g, 0));
+        cudaGraphDestroy(g);
         return FLOCK_OK;
     }
 
-    // H2D, all buckets concurrently, D2H.  Asynchronous; wait() to finish.
-    int launch() {
-        int rc = ensure_device();
-        if (rc) return rc;
-        TuneCfg cfg[kNumBuckets];
-        for (int b = 0; b < kNumBuckets; b++) cfg[b] = cfg_for(b);
-        if ((rc = reserve_scratch(cfg))) return rc;
-        cudaStream_t s0 = st[0];
-        FLOCK_CK(cudaEventRecord(ev_start, s0));
-        FLOCK_CK(cudaMemcpyAsync(d_cost.p, h_cost.p, (size_t)total_cost * 4, cudaMemcpyHostToDevice, s0));
-        FLOCK_CK(cudaMemcpyAsync(d_sd.p, h_sd.p, (size_t)total_sd * 4, cudaMemcpyHostToDevice, s0));
-        FLOCK_CK(cudaMemcpyAsync(d_desc.p, h_desc.p, (size_t)count * sizeof(BatchDesc), cudaMemcpyHostToDevice, s0));
-        FLOCK_CK(cudaEventRecord(ev_done, s0));
-        for (int b = 1; b < kNumBuckets; b++) FLOCK_CK(cudaStreamWaitEvent(st[b], ev_done, 0));
-        for (int b = 0; b < kNumBuckets; b++)
-            if ((rc = launch_bucket(b, bstart[b], bstart[b + 1], cfg[b], st[b], d_next.as<int32_t>() + 32 * b))) return rc;
-        for (int b = 1; b < kNumBuckets; b++) {
-            FLOCK_CK(cudaEventRecord(ev_done, st[b]));
-            FLOCK_CK(cudaStreamWaitEvent(s0, ev_done, 0));
-        }
-        FLOCK_CK(cudaMemcpyAsync(h_out.p, d_out.p, (size_t)total_cells * 12, cudaMemcpyDeviceToHost, s0));
-        FLOCK_CK(cudaMemcpyAsync(h_sc.p, d_sc.p, (size_t)count * sizeof(Scalars), cudaMemcpyDeviceToHost, s0));
-        FLOCK_CK(cudaEventRecord(ev_done, s0));
-        return FLOCK_OK;
-    }
-
-    int wait() {
-        FLOCK_CK(cudaEventSynchronize(ev_done));
-        return FLOCK_OK;
-    }
-    bool ready() { return cudaEventQuery(ev_done) == cudaSuccess; }
-
-    // Device-resident inputs only: rerun the kernels on what is already staged.
-    int rerun_device_only(float* ms) {
-        TuneCfg cfg[kNumBuckets];
-        for (int b = 0; b < kNumBuckets; b++) cfg[b] = cfg_for(b);
-        int rc = reserve_scratch(cfg);
-        if (rc) return rc;
+    // Solve every staged bucket (all buckets concurrently, one stream each).
+    // Inputs must already be on the device.  Returns when all are done.
+    int run_device(const TuneCfg* cfg, float* ms, int only_bucket = -1) {
+        int rc;
         cudaStream_t s0 = st[0];
         FLOCK_CK(cudaEventRecord(ev_start, s0));
         for (int b = 1; b < kNumBuckets; b++) FLOCK_CK(cudaStreamWaitEvent(st[b], ev_start, 0));
-        for (int b = 0; b < kNumBuckets; b++)
-            if ((rc = launch_bucket(b, bstart[b], bstart[b + 1], cfg[b], st[b], d_next.as<int32_t>() + 32 * b))) return rc;
+        cudaGraphExec_t exec[kNumBuckets] = {};
+        bool live[kNumBuckets] = {};
+        launches = 0;
+        for (int b = 0; b < kNumBuckets; b++) {
+            const int nb = bstart[b + 1] - bstart[b];
+            if (!nb || (only_bucket >= 0 && b != only_bucket)) continue;
+            live[b] = true;
+            BatchArgs a = args_for(b);
+            a.next = ctr(b);
+            FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
+            k_bsetup<<<grid_for(b, cfg[b], 0, (const void*)k_bsetup), cfg[b].threads, 0, st[b]>>>(a);
+            FLOCK_CK(cudaGetLastError());
+            launches++;
+            if ((rc = capture_rounds(b, cfg[b], &exec[b]))) return rc;
+        }
+        int32_t* hc = h_ctr.as<int32_t>();
+        for (int guard = 0; guard < (1 << 26); guard++) {
+            bool any = false;
+            for (int b = 0; b < kNumBuckets; b++) {
+                if (!live[b]) continue;
+                any = true;
+                FLOCK_CK(cudaGraphLaunch(exec[b], st[b]));
+                launches += cfg[b].chunk;
+                FLOCK_CK(cudaMemcpyAsync(hc + (size_t)b * 2 * kMaxChunk + kMaxChunk, ctr(b) + kMaxChunk,
+                                         (size_t)cfg[b].chunk * sizeof(int32_t), cudaMemcpyDeviceToHost, st[b]));
+            }
+            if (!any) break;
+            for (int b = 0; b < kNumBuckets; b++) {
+                if (!live[b]) continue;
+                FLOCK_CK(cudaStreamSynchronize(st[b]));
+                if (hc[(size_t)b * 2 * kMaxChunk + kMaxChunk + cfg[b].chunk - 1] == 0) {
+                    live[b] = false;
+                    BatchArgs a = args_for(b);
+                    a.next = ctr(b);
+                    FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
+                    k_bfinal<<<grid_for(b, cfg[b], 0, (const void*)k_bfinal), cfg[b].threads, 0, st[b]>>>(a);
+                    FLOCK_CK(cudaGetLastError());
+                    launches++;
+                }
+            }
+        }
+        for (int b = 0; b < kNumBuckets; b++) if (exec[b]) cudaGraphExecDestroy(exec[b]);
         for (int b = 1; b < kNumBuckets; b++) {
-            FLOCK_CK(cudaEventRecord(ev_done, st[b]));
-            FLOCK_CK(cudaStreamWaitEvent(s0, ev_done, 0));
+            FLOCK_CK(cudaEventRecord(ev_join, st[b]));
+            FLOCK_CK(cudaStreamWaitEvent(s0, ev_join, 0));
         }
         FLOCK_CK(cudaEventRecord(ev_done, s0));
         FLOCK_CK(cudaEventSynchronize(ev_done));
@@ -783,7 +859,61 @@ struct BatchRunner {
         return FLOCK_OK;
     }
 
+    int upload() {
+        cudaStream_t s0 = st[0];
+        if (total_cost) FLOCK_CK(cudaMemcpyAsync(d_cost.p, h_cost.p, (size_t)total_cost * 4, cudaMemcpyHostToDevice, s0));
+        if (total_sd) FLOCK_CK(cudaMemcpyAsync(d_sd.p, h_sd.p, (size_t)total_sd * 4, cudaMemcpyHostToDevice, s0));
+        if (!descs.empty())
+            FLOCK_CK(cudaMemcpyAsync(d_desc.p, h_desc.p, descs.size() * sizeof(BatchDesc), cudaMemcpyHostToDevice, s0));
+        return FLOCK_OK;
+    }
+
+    int download() {
+        cudaStream_t s0 = st[0];
+        FLOCK_CK(cudaMemcpyAsync(h_out.p, d_out.p, (size_t)total_cells * 12, cudaMemcpyDeviceToHost, s0));
+        FLOCK_CK(cudaMemcpyAsync(h_sc.p, d_sc.p, (size_t)count * sizeof(Scalars), cudaMemcpyDeviceToHost, s0));
+        FLOCK_CK(cudaStreamSynchronize(s0));
+        return FLOCK_OK;
+    }
+
+    // Whole solve: upload, device rounds, download, then the large instances
+    // on the plain path.  Blocking.
+    float last_ms = 0;
+    int solve_all() {
+        int rc = ensure_device();
+        if (rc) return rc;
+        TuneCfg cfg[kNumBuckets];
+        for (int b = 0; b < kNumBuckets; b++) cfg[b] = cfg_for(b);
+        if ((rc = upload())) return rc;
+        if ((rc = run_device(cfg, &last_ms))) return rc;
+        if ((rc = download())) return rc;
+        plain_stats.assign(plain_list.size(), flock_stats{});
+        plain_flows.assign(plain_list.size(), {});
+        for (size_t q = 0; q < plain_list.size(); q++) {
+            const int k = plain_list[q];
+            plain_flows[q].resize((size_t)V_of[k] - 1);
+            rc = solve_plain(&insts[k], &opt, plain_flows[q].data(), nullptr, nullptr, &plain_stats[q]);
+            if (rc && rc != FLOCK_ERR_NOT_OPTIMAL) return rc;
+        }
+        return FLOCK_OK;
+    }
+
+    // Device-resident rerun for the benchmark: inputs stay where they are.
+    int rerun_device_only(float* ms) {
+        TuneCfg cfg[kNumBuckets];
+        for (int b = 0; b < kNumBuckets; b++) cfg[b] = cfg_for(b);
+        return run_device(cfg, ms);
+    }
+
     void collect(int k, flock_flow* flows, flock_stats* st_out) const {
+        if (V_of[k] > kMaxStagedV) {
+            for (size_t q = 0; q < plain_list.size(); q++)
+                if (plain_list[q] == k) {
+                    if (flows) memcpy(flows, plain_flows[q].data(), plain_flows[q].size() * sizeof(flock_flow));
+                    if (st_out) *st_out = plain_stats[q];
+                }
+            return;
+        }
         const Scalars& S = h_sc.as<Scalars>()[k];
         const int V = V_of[k];
         const int32_t* src = h_out.as<int32_t>() + out_off[k];
@@ -806,40 +936,36 @@ struct BatchRunner {
         }
     }
 
-    // Autotune every bucket with enough instances: each candidate config
-    // solves the bucket once (inputs already on the device); fastest wins.
+    // Autotune each bucket with enough instances: the bucket alone is solved
+    // once per candidate configuration (inputs resident) and the fastest wins.
+    // Block sizes are limited to the ones validated on the GPU for the
+    // bucket's sizes (128/256 up to V = 256, 256 above).
     int autotune() {
         int rc = ensure_device();
         if (rc) return rc;
-        cudaStream_t s0 = st[0];
-        FLOCK_CK(cudaMemcpyAsync(d_cost.p, h_cost.p, (size_t)total_cost * 4, cudaMemcpyHostToDevice, s0));
-        FLOCK_CK(cudaMemcpyAsync(d_sd.p, h_sd.p, (size_t)total_sd * 4, cudaMemcpyHostToDevice, s0));
-        FLOCK_CK(cudaMemcpyAsync(d_desc.p, h_desc.p, (size_t)count * sizeof(BatchDesc), cudaMemcpyHostToDevice, s0));
-        FLOCK_CK(cudaStreamSynchronize(s0));
+        if ((rc = upload())) return rc;
+        FLOCK_CK(cudaStreamSynchronize(st[0]));
         for (int b = 0; b < kNumBuckets; b++) {
             const int nb = bstart[b + 1] - bstart[b];
             {
                 std::lock_guard<std::mutex> lk(g_tune_mu);
-                if (g_tuned_ok[b] || nb < 16) continue;
+                if (g_tuned_ok[b] || nb < 32) continue;
             }
-            const int threads_opts[3] = {128, 256, 512};
+            std::vector<TuneCfg> cands;
+            const int thr[2] = {128, 256};
+            for (int ti = 0; ti < 2; ti++) {
+                if (thr[ti] == 128 && bmaxV[b] > 256) continue;
+                for (int gm = 1; gm <= 2; gm++)
+                    for (int ch : {8, 32}) cands.push_back(TuneCfg{thr[ti], gm, ch});
+            }
             float best_ms = 1e30f;
-            TuneCfg best = heuristic_cfg(bmaxV[b], bmaxM[b]);
-            for (int ti = 0; ti < 3; ti++) {
-                for (int sm = 1; sm >= 0; sm--) {
-                    TuneCfg t{threads_opts[ti], sm};
-                    if (sm && batch_smem_bytes(bmaxV[b], bmaxM[b]) > 200 * 1024) continue;
-                    TuneCfg cfg[kNumBuckets];
-                    for (int x = 0; x < kNumBuckets; x++) cfg[x] = t;
-                    if ((rc = reserve_scratch(cfg))) return rc;
-                    FLOCK_CK(cudaEventRecord(ev_start, s0));
-                    if ((rc = launch_bucket(b, bstart[b], bstart[b + 1], t, s0, d_next.as<int32_t>() + 32 * b))) return rc;
-                    FLOCK_CK(cudaEventRecord(ev_done, s0));
-                    FLOCK_CK(cudaEventSynchronize(ev_done));
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, ev_start, ev_done);
-                    if (ms < best_ms) { best_ms = ms; best = t; }
-                }
+            TuneCfg best = default_cfg(bmaxV[b]);
+            for (const TuneCfg& t : cands) {
+                TuneCfg cfg[kNumBuckets];
+                for (int x = 0; x < kNumBuckets; x++) cfg[x] = t;
+                float ms = 0;
+                if ((rc = run_device(cfg, &ms, b))) return rc;
+                if (ms < best_ms) { best_ms = ms; best = t; }
             }
             std::lock_guard<std::mutex> lk(g_tune_mu);
             g_tuned[b] = best;
@@ -852,9 +978,7 @@ struct BatchRunner {
 BatchRunner* batch_runner_new() { return new BatchRunner(); }
 void batch_runner_free(BatchRunner* r) { delete r; }
 int batch_runner_prepare(BatchRunner* r, int cnt, const flock_instance* insts, const flock_options* o) { return r->prepare(cnt, insts, o); }
-int batch_runner_launch(BatchRunner* r) { return r->launch(); }
-int batch_runner_wait(BatchRunner* r) { return r->wait(); }
-bool batch_runner_ready(BatchRunner* r) { return r->ready(); }
+int batch_runner_solve(BatchRunner* r) { return r->solve_all(); }
 void batch_runner_collect(BatchRunner* r, int k, flock_flow* flows, flock_stats* st) { r->collect(k, flows, st); }
 int batch_runner_count(BatchRunner* r) { return r->count; }
 
@@ -873,10 +997,8 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
     if (rc) return rc;
     const char* at = getenv("FLOCK_AUTOTUNE");
     if (!at || strcmp(at, "0") != 0) { if ((rc = R.autotune())) return rc; }
-    if ((rc = R.launch())) return rc;
-    if ((rc = R.wait())) return rc;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, R.ev_start, R.ev_done);
+    if ((rc = R.solve_all())) return rc;
+    const float ms = R.last_ms;
     int worst = FLOCK_OK;
     int64_t off = 0;
     for (int k = 0; k < cnt; k++) {
@@ -894,10 +1016,12 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
 
 // Device-only timing hook for the benchmark: solve the last staged batch
 // again with its inputs already resident.  Returns the kernel time in ms.
-int batch_rerun_device(float* ms) {
+int batch_rerun_device(float* ms, int32_t* launches) {
     std::lock_guard<std::mutex> lk(g_batch_mu);
     if (!g_batch) return FLOCK_ERR_ARG;
-    return g_batch->rerun_device_only(ms);
+    const int rc = g_batch->rerun_device_only(ms);
+    if (launches) *launches = g_batch->launches;
+    return rc;
 }
 
 }  // namespace flock
@@ -933,7 +1057,7 @@ int flock_batch_solve(int32_t count, const flock_instance* insts, const flock_op
 
 /* Benchmark hook (not part of the public header): rerun the last batch with
  * its inputs resident on the device and report the device time. */
-int flock_bench_batch_rerun(float* ms) { return flock::batch_rerun_device(ms); }
+int flock_bench_batch_rerun(float* ms, int32_t* launches) { return flock::batch_rerun_device(ms, launches); }
 
 /* Benchmark hook: average device time of the fused reduced-cost sweep on an
  * m x n matrix (random costs and duals, inputs resident). */

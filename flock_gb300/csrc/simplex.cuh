@@ -162,8 +162,11 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
             const int p = c.order[qh++];
             for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
                 const int ch = c.csr_adj[e];
-                if (!FLOCK_IN(ch, V) || qt >= V) { fail_check(c.sc, 31); break; }
-                if (c.parent[ch] == -2 && ch != root) { c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch; }
+                if (!FLOCK_IN(ch, V)) { fail_check(c.sc, 31); break; }
+                if (c.parent[ch] == -2 && ch != root) {
+                    if (qt >= V) { fail_check(c.sc, 34); break; }
+                    c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch;
+                }
             }
         }
         bs.i[1] = 0;   // scan pointer
@@ -209,8 +212,11 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
                 const int p = c.order[qh++];
                 for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
                     const int ch = c.csr_adj[e];
-                    if (!FLOCK_IN(ch, V) || qt >= V) { fail_check(c.sc, 32); break; }
-                    if (c.parent[ch] == -2 && ch != root) { c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch; }
+                    if (!FLOCK_IN(ch, V)) { fail_check(c.sc, 32); break; }
+                    if (c.parent[ch] == -2 && ch != root) {
+                        if (qt >= V) { fail_check(c.sc, 35); break; }
+                        c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch;
+                    }
                 }
             }
             bs.i[2] = qt;
