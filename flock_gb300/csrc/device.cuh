@@ -12,8 +12,13 @@
 // r with parent column p is cell (r, p-m); of a column child c with parent
 // row p, cell (p, c-m).  Arc direction is always row -> column.
 #pragma once
+#include <climits>
 #include <cstdint>
+#ifdef FLOCK_EMU
+#include "emu/cuda_emu.h"   // host emulation for sanitizer runs of the device code
+#else
 #include <cuda_runtime.h>
+#endif
 
 namespace flock {
 

@@ -171,7 +171,12 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
         }
         best = block_max_u64(best, bs);
         const int L = (int)key_idx(best);
-        if (!top2_valid(c, L, c.top2[L])) vogel_rescan_block(c, L, bs);
+        // One thread decides whether the chosen line's cache is stale; the
+        // decision is broadcast and a barrier separates every read of
+        // covered[] here from thread 0's allocation below, which writes it.
+        if (threadIdx.x == 0) bs.i[6] = top2_valid(c, L, c.top2[L]) ? 0 : 1;
+        __syncthreads();
+        if (bs.i[6]) vogel_rescan_block(c, L, bs);
         if (threadIdx.x == 0) {
             if (pr) bs.i[0] = 0;
             if (pc) bs.i[1] = 0;
