@@ -1066,3 +1066,147 @@ int flock_bench_sweep(int32_t m, int32_t n, int32_t iters, float* avg_ms, int32_
 }
 
 }  // extern "C"
+
+// ======================================================= static scratch ===
+// flock_vogel_static: Vogel's approximation on the GPU without any
+// allocation.  Every device array of the call (the padded cost
+// matrix, supplies/demands, the Vogel working set, the packed flow list and
+// the status scalars) is carved from one file-scope __device__ array of fixed
+// size, so a call makes no cudaMalloc/cudaFree, no pinned-host allocation and
+// no stream or event creation.  The device code is the same vogel_cta that
+// flock_vogel runs; results are identical.
+//
+// Limits: m + n <= FLOCK_VOGEL_STATIC_MAX_V and m * ceil4(n) <=
+// FLOCK_VOGEL_STATIC_MAX_CELLS (include/flock.h); larger instances are
+// rejected with FLOCK_ERR_RANGE before any CUDA call.
+//
+// Set-up: the first call on a device resolves the scratch array's device
+// address with cudaGetSymbolAddress (once per device, cached).  That first
+// call should come before any stream capture on the calling thread.
+//
+// Concurrency: every call on one device uses the same scratch, so calls that
+// overlap in time (several host threads, or a caller reusing the stream while
+// a call is in flight) race on it.  Callers serialise.
+
+namespace flock {
+namespace {
+
+constexpr size_t kStaticBytes = size_t(6) << 20;   // 6 MiB per device
+static __device__ __align__(256) unsigned char g_vogel_scratch[kStaticBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+int cuda_err(const char* what, cudaError_t e) {
+    set_error(std::string("flock_vogel_static: ") + what + ": " + cudaGetErrorString(e));
+    return FLOCK_ERR_CUDA;
+}
+
+// Byte offsets of the regions inside the scratch array for one instance.
+struct Layout {
+    size_t cost, sd, ws, flows, sc, end;
+};
+Layout layout_for(int m, int n) {
+    const int V = m + n, ldc = (n + 3) & ~3;
+    Layout L;
+    L.cost = 0;
+    L.sd = al(L.cost + (size_t)m * ldc * 4);
+    L.ws = al(L.sd + (size_t)V * 4);
+    size_t gbytes = 0;
+    Ctx probe;
+    carve_ctx(probe, nullptr, V, m, nullptr, nullptr, nullptr, &gbytes);
+    L.flows = al(L.ws + gbytes);
+    L.sc = al(L.flows + (size_t)(V - 1) * sizeof(flock_flow));
+    L.end = L.sc + sizeof(Scalars);
+    return L;
+}
+
+// The largest admitted shapes both fit: m+n at the vertex limit with the cell
+// limit spent on few rows, and the cell limit with a square matrix.
+bool fits(int m, int n) { return layout_for(m, n).end <= kStaticBytes; }
+
+}  // namespace
+
+// Variant of k_vogel_only that also packs the allocation list into the
+// caller's flow layout, so one device-to-host copy returns it.
+__global__ void __launch_bounds__(1024) k_vogel_static(Ctx c, flock_flow* out) {
+    __shared__ BlockScratch bs;
+    vogel_cta(c, bs);
+    const int V = c.I.m + c.I.n;
+    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) out[k] = {c.bfs_src[k], c.bfs_dst[k], c.bfs_qty[k]};
+}
+
+static int vogel_static(const flock_instance* I, flock_flow* flows, int32_t* events) {
+    int rc = validate_instance(I);
+    if (rc) return rc;
+    const int m = I->m, n = I->n, V = m + n, ldc = (n + 3) & ~3;
+    if (V > FLOCK_VOGEL_STATIC_MAX_V || (int64_t)m * ldc > FLOCK_VOGEL_STATIC_MAX_CELLS || !fits(m, n)) {
+        set_error("flock_vogel_static: instance exceeds the static scratch (m + n <= " +
+                  std::to_string(FLOCK_VOGEL_STATIC_MAX_V) + " and m * ceil4(n) <= " +
+                  std::to_string(FLOCK_VOGEL_STATIC_MAX_CELLS) + " required)");
+        return FLOCK_ERR_RANGE;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_err("cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices) { set_error("flock_vogel_static: device ordinal out of range"); return FLOCK_ERR_ARG; }
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_vogel_scratch);
+        if (e != cudaSuccess) return cuda_err("cudaGetSymbolAddress", e);
+        g_scratch_ptr[dev] = p;
+    }
+    unsigned char* base = (unsigned char*)g_scratch_ptr[dev];
+    const Layout L = layout_for(m, n);
+    cudaStream_t s = cudaStreamPerThread;
+
+    Ctx c;
+    carve_ctx(c, base + L.ws, V, m, nullptr, nullptr);
+    c.I.m = m; c.I.n = n; c.I.ldc = ldc;
+    c.I.cost = (const int32_t*)(base + L.cost);
+    c.I.supply = (const int32_t*)(base + L.sd);
+    c.I.demand = (const int32_t*)(base + L.sd) + m;
+    c.sc = (Scalars*)(base + L.sc);
+    flock_flow* dflows = (flock_flow*)(base + L.flows);
+
+    // Inputs.  The padding columns of the cost rows are never read.
+    e = cudaMemcpy2DAsync(base + L.cost, (size_t)ldc * 4, I->cost, (size_t)n * 4, (size_t)n * 4, m,
+                          cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_err("cost upload", e);
+    e = cudaMemcpyAsync(base + L.sd, I->supply, (size_t)m * 4, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_err("supply upload", e);
+    e = cudaMemcpyAsync(base + L.sd + (size_t)m * 4, I->demand, (size_t)n * 4, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_err("demand upload", e);
+    // The status scalars (events, status, fail site) must start at zero; the
+    // Vogel working arrays are initialised by the kernel itself.
+    e = cudaMemsetAsync(c.sc, 0, sizeof(Scalars), s);
+    if (e != cudaSuccess) return cuda_err("scalar reset", e);
+
+    const int nt = std::max(128, std::min(1024, ((V + 31) / 32) * 32));
+    k_vogel_static<<<1, nt, 0, s>>>(c, dflows);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err("k_vogel_static launch", e);
+
+    Scalars hs;
+    e = cudaMemcpyAsync(flows, dflows, (size_t)(V - 1) * sizeof(flock_flow), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_err("flow download", e);
+    e = cudaMemcpyAsync(&hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_err("scalar download", e);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err("k_vogel_static", e);
+    if (hs.status & ST_TREE_CORRUPT) {
+        set_error("flock_vogel_static: internal check failed at site " + std::to_string(hs.fail_site));
+        return FLOCK_ERR_CUDA;
+    }
+    if (events) *events = hs.events;
+    return FLOCK_OK;
+}
+
+}  // namespace flock
+
+extern "C" int flock_vogel_static(const flock_instance* inst, flock_flow* flows, int32_t* events) {
+    if (!flows) return FLOCK_ERR_ARG;
+    return flock::vogel_static(inst, flows, events);
+}

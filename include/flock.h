@@ -120,6 +120,28 @@ int flock_read_dat(const char* path, int32_t decimal_scale, int32_t m, int32_t n
  * Writes m+n-1 allocations in allocation order.  *events as flock_stats. */
 int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events);
 
+/* No counterpart in the reference.  flock_vogel without any allocation:
+ * the same kernel and identical results, but every device array of the call
+ * lives in one static 6 MiB __device__ array per device, so the call makes no
+ * cudaMalloc/cudaFree, allocates no pinned host memory and creates no stream
+ * or event.  It is for callers that cannot allocate: a process whose device
+ * memory is already reserved by another allocator (a caching allocator or a
+ * fixed serving budget holding the device), where cudaMalloc fails or takes
+ * memory promised elsewhere; and latency-bound callers on a busy device,
+ * where cudaFree's implicit device-wide synchronisation would stall other
+ * streams.
+ * Limits: m + n <= FLOCK_VOGEL_STATIC_MAX_V and m * ceil4(n) <=
+ * FLOCK_VOGEL_STATIC_MAX_CELLS; larger instances return FLOCK_ERR_RANGE
+ * (message via flock_last_error) before any CUDA call.
+ * The first call on a device does the set-up (cudaGetSymbolAddress of the
+ * scratch array, cached per device) and should come before any stream
+ * capture.  Work runs on cudaStreamPerThread; the call returns after
+ * synchronising it.  Calls that overlap in time on one device share the
+ * scratch and race: callers serialise them. */
+#define FLOCK_VOGEL_STATIC_MAX_V 8192
+#define FLOCK_VOGEL_STATIC_MAX_CELLS 1048576
+int flock_vogel_static(const flock_instance* inst, flock_flow* flows, int32_t* events);
+
 /* Solve one instance on the GPU.  `flows` has room for m+n-1 entries; the
  * nonzero flows are written first (stats->active_flows of them), then the
  * zero-flow basic cells, so flows[0..m+n-2] is always the full basis.
