@@ -174,40 +174,48 @@ __device__ __forceinline__ int batch_next(const BatchArgs& a, int* s_idx) {
     return idx < a.count ? idx : -1;
 }
 
+// Initial solution and strongly feasible start tree of one instance, in the
+// instance's global working set.
+__device__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs) {
+    Ctx c;
+    batch_ctx(a, d, c);
+    if (threadIdx.x == 0) {
+        Scalars z;
+        memset(&z, 0, sizeof(z));
+        z.max_rounds = a.max_rounds;
+        z.mode = a.mode;
+        *c.sc = z;
+    }
+    __syncthreads();
+    if (a.bfs_method == FLOCK_BFS_VOGEL) {
+        vogel_cta(c, bs);
+    } else {
+        if (threadIdx.x == 0) nwc_thread0(c);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
+    const int V = d.m + d.n;
+    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+        a.bfs_out[3 * (d.out_off + k) + 0] = c.bfs_src[k];
+        a.bfs_out[3 * (d.out_off + k) + 1] = c.bfs_dst[k];
+        a.bfs_out[3 * (d.out_off + k) + 2] = c.bfs_qty[k];
+    }
+    __syncthreads();
+    sf_init_cta(c, bs);
+    __syncthreads();
+}
+
+__device__ __forceinline__ void bdesc_reject(const BatchArgs& a, const BatchDesc& d) {
+    if (threadIdx.x == 0) { a.sc[d.index].status = ST_TREE_CORRUPT; a.sc[d.index].fail_site = 1; a.sc[d.index].done = 1; }
+}
+
 __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
     __shared__ BlockScratch bs;
     __shared__ int s_idx;
     for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
-        if (!batch_desc_ok(a, d)) {
-            if (threadIdx.x == 0) { a.sc[d.index].status = ST_TREE_CORRUPT; a.sc[d.index].fail_site = 1; a.sc[d.index].done = 1; }
-            continue;
-        }
-        Ctx c;
-        batch_ctx(a, d, c);
-        if (threadIdx.x == 0) {
-            Scalars z;
-            memset(&z, 0, sizeof(z));
-            z.max_rounds = a.max_rounds;
-            z.mode = a.mode;
-            *c.sc = z;
-        }
-        __syncthreads();
-        if (a.bfs_method == FLOCK_BFS_VOGEL) {
-            vogel_cta(c, bs);
-        } else {
-            if (threadIdx.x == 0) nwc_thread0(c);
-            __syncthreads();
-        }
-        if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
-        const int V = d.m + d.n;
-        for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
-            a.bfs_out[3 * (d.out_off + k) + 0] = c.bfs_src[k];
-            a.bfs_out[3 * (d.out_off + k) + 1] = c.bfs_dst[k];
-            a.bfs_out[3 * (d.out_off + k) + 2] = c.bfs_qty[k];
-        }
-        __syncthreads();
-        sf_init_cta(c, bs);
+        if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); continue; }
+        bsetup_one(a, d, bs);
     }
 }
 
@@ -236,21 +244,18 @@ __host__ __device__ inline size_t staged_bytes(int V, int M) {
     return (k.so + 15) & ~size_t(15);
 }
 
-__global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
-    __shared__ BlockScratch bs;
-    __shared__ int s_idx;
-    extern __shared__ __align__(16) unsigned char smem[];
-    for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
-        const BatchDesc d = a.desc[idx];
-        if (!batch_desc_ok(a, d)) continue;
-        if (a.sc[d.index].done) continue;          // every thread reads the same value
-        Ctx g;
-        batch_ctx(a, d, g);
-        Ctx c = g;
-        stage_hot(c, smem, a.maxV, a.maxM);
-        const int V = d.m + d.n;
-        for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
-        __syncthreads();
+// Pricing rounds of one instance with its tree staged in shared memory:
+// `max_here` rounds at most (1 for the round-kernel form), or until done.
+__device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs, unsigned char* smem,
+                            int max_here) {
+    Ctx g;
+    batch_ctx(a, d, g);
+    Ctx c = g;
+    stage_hot(c, smem, a.maxV, a.maxM);
+    const int V = d.m + d.n;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
+    __syncthreads();
+    for (int r = 0; r < max_here; r++) {
         tree_recompute_cta(c, bs);
         if (!c.sc->done) {
             sweep_cta(c);
@@ -259,12 +264,36 @@ __global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
         if (threadIdx.x == 0) {
             c.sc->rounds++;
             if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
-            if (!c.sc->done) atomicAdd(a.active, 1);
-        }
-        for (int v = threadIdx.x; v < V; v += blockDim.x) {
-            g.parent[v] = c.parent[v]; g.flow[v] = c.flow[v]; g.pot[v] = c.pot[v];
+            if (!c.sc->done && a.active && r + 1 == max_here) atomicAdd(a.active, 1);
         }
         __syncthreads();
+        if (c.sc->done) break;       // written before the barrier: every thread reads the same value
+    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        g.parent[v] = c.parent[v]; g.flow[v] = c.flow[v]; g.pot[v] = c.pot[v];
+    }
+    __syncthreads();
+}
+
+__device__ void bfinal_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs) {
+    if (a.sc[d.index].status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) return;   // uniform
+    Ctx c;
+    batch_ctx(a, d, c);
+    finalize_cta(c, bs);
+    certify_flows_cta(c, bs);
+    certify_cells_cta(c, bs);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
+    __shared__ BlockScratch bs;
+    __shared__ int s_idx;
+    extern __shared__ __align__(16) unsigned char smem[];
+    for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
+        const BatchDesc d = a.desc[idx];
+        if (!batch_desc_ok(a, d)) continue;
+        if (a.sc[d.index].done) continue;          // every thread reads the same value
+        brounds_one(a, d, bs, smem, 1);
     }
 }
 
@@ -274,12 +303,23 @@ __global__ void __launch_bounds__(256) k_bfinal(BatchArgs a) {
     for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) continue;
-        if (a.sc[d.index].status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) continue;
-        Ctx c;
-        batch_ctx(a, d, c);
-        finalize_cta(c, bs);
-        certify_flows_cta(c, bs);
-        certify_cells_cta(c, bs);
+        bfinal_one(a, d, bs);
+    }
+}
+
+// Persistent form: a CTA takes the next instance of the bucket (largest
+// first) and runs it from the initial solution to the certificate, all
+// pricing rounds inside with the tree resident in shared memory.
+__global__ void __launch_bounds__(256, 4) k_bsolve(BatchArgs a) {
+    __shared__ BlockScratch bs;
+    __shared__ int s_idx;
+    extern __shared__ __align__(16) unsigned char smem[];
+    for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
+        const BatchDesc d = a.desc[idx];
+        if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); continue; }
+        bsetup_one(a, d, bs);
+        if (!a.sc[d.index].done) brounds_one(a, d, bs, smem, 1 << 30);
+        bfinal_one(a, d, bs);
     }
 }
 
@@ -603,10 +643,12 @@ static int bucket_of(int V) {
     return b;   // kNumBuckets: plain path
 }
 
-// Launch configuration of a bucket.  threads: block size of the three
-// kernels; grid_mult: resident CTAs per SM multiplier for work stealing;
-// chunk: pricing rounds per graph launch.
-struct TuneCfg { int threads; int grid_mult; int chunk; };
+// Launch configuration of a bucket.  threads: block size of the kernels;
+// persistent: 1 = one k_bsolve launch (every round inside), 0 = k_bsetup,
+// graph-captured chunks of k_bround, k_bfinal; grid_mult: resident CTAs per
+// SM multiplier for work stealing (round form); chunk: pricing rounds per
+// graph launch (round form).
+struct TuneCfg { int threads; int grid_mult; int chunk; int persistent; };
 
 static std::mutex g_tune_mu;
 static TuneCfg g_tuned[kNumBuckets];
@@ -617,6 +659,7 @@ static TuneCfg default_cfg(int maxV) {
     t.threads = maxV <= 256 ? 128 : 256;
     t.grid_mult = 1;
     t.chunk = 16;
+    t.persistent = 1;
     return t;
 }
 
@@ -653,7 +696,8 @@ struct BatchRunner {
         FLOCK_CK(cudaEventCreate(&ev_start));
         FLOCK_CK(cudaEventCreate(&ev_done));
         FLOCK_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-        FLOCK_CK(cudaFuncSetAttribute(k_bround, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+        FLOCK_CK(cudaFuncSetAttribute(k_bround, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
+        FLOCK_CK(cudaFuncSetAttribute(k_bsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
         FLOCK_CK(d_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         FLOCK_CK(h_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         init = true;
@@ -742,9 +786,17 @@ struct BatchRunner {
         return FLOCK_OK;
     }
 
+    // FLOCK_BATCH_FORM=round|persistent forces the form (tests run both).
     TuneCfg cfg_for(int b) {
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        return g_tuned_ok[b] ? g_tuned[b] : default_cfg(bmaxV[b]);
+        TuneCfg t;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            t = g_tuned_ok[b] ? g_tuned[b] : default_cfg(bmaxV[b]);
+        }
+        const char* f = getenv("FLOCK_BATCH_FORM");
+        if (f && !strcmp(f, "round")) t.persistent = 0;
+        if (f && !strcmp(f, "persistent")) t.persistent = 1;
+        return t;
     }
 
     BatchArgs args_for(int b) {
@@ -810,12 +862,21 @@ struct BatchRunner {
         cudaGraphExec_t exec[kNumBuckets] = {};
         bool live[kNumBuckets] = {};
         launches = 0;
-        for (int b = 0; b < kNumBuckets; b++) {
+        // largest bucket first: its long solves start before the small ones
+        for (int b = kNumBuckets - 1; b >= 0; b--) {
             const int nb = bstart[b + 1] - bstart[b];
             if (!nb || (only_bucket >= 0 && b != only_bucket)) continue;
-            live[b] = true;
             BatchArgs a = args_for(b);
             a.next = ctr(b);
+            if (cfg[b].persistent) {
+                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b]);
+                FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
+                k_bsolve<<<grid_for(b, cfg[b], smem, (const void*)k_bsolve), cfg[b].threads, smem, st[b]>>>(a);
+                FLOCK_CK(cudaGetLastError());
+                launches++;
+                continue;
+            }
+            live[b] = true;
             FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
             k_bsetup<<<grid_for(b, cfg[b], 0, (const void*)k_bsetup), cfg[b].threads, 0, st[b]>>>(a);
             FLOCK_CK(cudaGetLastError());
@@ -955,8 +1016,9 @@ struct BatchRunner {
             const int thr[2] = {128, 256};
             for (int ti = 0; ti < 2; ti++) {
                 if (thr[ti] == 128 && bmaxV[b] > 256) continue;
+                cands.push_back(TuneCfg{thr[ti], 1, 16, 1});
                 for (int gm = 1; gm <= 2; gm++)
-                    for (int ch : {8, 32}) cands.push_back(TuneCfg{thr[ti], gm, ch});
+                    for (int ch : {8, 32}) cands.push_back(TuneCfg{thr[ti], gm, ch, 0});
             }
             float best_ms = 1e30f;
             TuneCfg best = default_cfg(bmaxV[b]);

@@ -145,3 +145,22 @@ def test_batch_matches_plain():
         assert r.objective == p.objective
         bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, r.flows, p.u, p.v)
         assert obj == r.objective
+
+
+@pytest.mark.parametrize("form", ["persistent", "round"])
+def test_batch_forms_all_buckets(form, monkeypatch):
+    """Both batched forms on instances from every size bucket (V up to 3072)
+    plus two above it (plain path): certified optima equal to the plain
+    solver's, and the same pricing rounds in both forms."""
+    monkeypatch.setenv("FLOCK_BATCH_FORM", form)
+    shapes = [(5, 7), (30, 30), (60, 60), (100, 150), (200, 300), (400, 500), (900, 1000),
+              (1500, 1500), (1000, 2072), (1600, 1600), (12, 40), (3, 3)]
+    insts = [fg.generate(0, 500 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(shapes)]
+    insts += fg.mixed_batch(17, 96, 10, 300)
+    out = fg.batch_solve(insts)
+    for k, (inst, r) in enumerate(zip(insts, out)):
+        assert r.status == 0 and r.certified, (k, inst.m, inst.n, r.status)
+        if inst.m * inst.n <= 300 * 300 or k < len(shapes):
+            p = fg.solve(inst)
+            assert r.objective == p.objective, (k, inst.m, inst.n)
+            assert r.iterations == p.iterations, (k, inst.m, inst.n)
