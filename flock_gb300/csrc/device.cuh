@@ -34,6 +34,10 @@ enum : int32_t {
 };
 
 constexpr int64_t kDeadPot = -(int64_t(1) << 61);   // dual of a zero-demand column during pivoting
+// int32 column duals for the sweep: live duals must lie strictly inside
+// (kDead32, -kDead32) so that c - v fits int32 for |c| <= 2^30; a dead
+// (zero-demand) column is stored as kDead32 and re-checked exactly.
+constexpr int32_t kDead32 = -((1 << 30) - 1);
 constexpr uint64_t kNoKey = ~0ull;
 
 struct Scalars {
@@ -54,6 +58,8 @@ struct Scalars {
     int64_t neg_cells;     // certificate: cells with negative reduced cost
     int32_t last_winners;
     int32_t fail_site;     // first failed internal check (0: none), see fail_check
+    int32_t narrow;        // 1: every live column dual fits the int32 sweep (v32 valid)
+    int32_t pad_;
 };
 
 // One instance as the kernels see it.
@@ -77,6 +83,7 @@ struct Ctx {
     int64_t* flow;     // V  perturbed flow on the edge to the parent
     int32_t* depth;    // V
     int64_t* pot;      // V  duals: u_i (rows), v_j (columns)
+    int32_t* v32;      // n  column duals as int32 when sc->narrow (kDead32: zero-demand column)
     // pointer-jumping scratch (double buffered)
     int32_t* anc0; int32_t* anc1; int32_t* len0; int32_t* len1; int64_t* acc0; int64_t* acc1;
     // pricing
@@ -101,6 +108,14 @@ struct Ctx {
 };
 
 // --------------------------------------------------------------- helpers ---
+// A column dual as the int32 sweep sees it; sets `wide` when it does not fit.
+__device__ __forceinline__ int32_t narrow_dual(int64_t p, int& wide) {
+    if (p == kDeadPot) return kDead32;
+    if (p > kDead32 && p < -(int64_t)kDead32) return (int32_t)p;
+    wide = 1;
+    return 0;
+}
+
 #define FLOCK_IN(x, V) ((unsigned)(x) < (unsigned)(V))
 
 // An internal index check failed: record the first failing site, mark the

@@ -20,10 +20,12 @@
 #define __host__
 #define __global__
 #define __forceinline__ inline
+#define __noinline__
 #define __launch_bounds__(...)
 #define __align__(x) alignas(x)
 
 struct int4 { int x, y, z, w; };
+inline int4 make_int4(int x, int y, int z, int w) { return int4{x, y, z, w}; }
 struct EmuDim { unsigned x = 0, y = 0, z = 0; };
 
 namespace emu {

@@ -40,6 +40,7 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.out_src = arr<int32_t>(keep, V); c.out_dst = arr<int32_t>(keep, V); c.out_qty = arr<int32_t>(keep, V);
     c.parent = arr<int32_t>(keep, V); c.flow = arr<int64_t>(keep, V); c.depth = arr<int32_t>(keep, V);
     c.pot = arr<int64_t>(keep, V);
+    c.v32 = arr<int32_t>(keep, V);
     c.anc0 = arr<int32_t>(keep, V); c.anc1 = arr<int32_t>(keep, V);
     c.len0 = arr<int32_t>(keep, V); c.len1 = arr<int32_t>(keep, V);
     c.acc0 = arr<int64_t>(keep, V); c.acc1 = arr<int64_t>(keep, V);

@@ -71,6 +71,7 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.acc1 = (int64_t*)k.S(8 * v);
     c.row_best = (uint64_t*)k.S(8 * mm);
     c.pot = smem ? (int64_t*)k.S(8 * v) : (pot_global ? pot_global : (int64_t*)k.G(8 * v));
+    c.v32 = (int32_t*)k.S(4 * v);
     c.bfs_src = (int32_t*)k.G(4 * v);
     c.bfs_dst = (int32_t*)k.G(4 * v);
     c.bfs_qty = (int32_t*)k.G(4 * v);

@@ -49,45 +49,77 @@ __global__ void __launch_bounds__(1024) k_vogel_only(Ctx c) {
     vogel_cta(c, bs);
 }
 
-// Grid-wide sweep.  blockIdx.x = tile + ntile * row_group.  Each warp owns
-// one row segment of `tile` columns; lanes read 16-byte vectors.
-__global__ void __launch_bounds__(256) k_sweep(Ctx c, int tile, int ntile) {
+// Grid-wide sweep.  blockIdx.x = tile + ntile * row_group.  The block stages
+// the int32 column duals of its tile (narrow form) in shared memory; a warp
+// work unit is one row segment of kSegCols columns, read as 16-byte vectors
+// that bypass L1 (each cost element is used once per sweep), eight per lane
+// in flight.  Units combine into row_best[] with atomicMin, so row_best must
+// hold kNoKey before the sweep (k_setup and k_pivot leave it so).
+constexpr int kSweepTile = 8192;   // columns per block tile (32 KB of int32 duals)
+constexpr int kSegCols = 1024;     // columns per warp work unit
+constexpr int kSweepThreads = 512;
+
+__device__ __forceinline__ int4 ld_stream4(const int4* p) {
+    int4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+
+__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int ntile) {
     if (c.sc->done) return;
-    extern __shared__ int64_t vt[];
+    __shared__ __align__(16) int32_t vt[kSweepTile];
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
     const int t = blockIdx.x % ntile, rg = blockIdx.x / ntile, nrg = gridDim.x / ntile;
     const int j0 = t * tile;
     const int jn = min(tile, n - j0);
-    for (int jj = threadIdx.x; jj < jn; jj += blockDim.x) vt[jj] = c.pot[m + j0 + jj];
-    __syncthreads();
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
-    const int nq = (jn + 3) >> 2;
-    for (int i = rg * wpb + warp; i < m; i += nrg * wpb) {
+    const int nseg = (jn + kSegCols - 1) / kSegCols;
+    const long long units = (long long)m * nseg, stride = (long long)nrg * wpb;
+    if (!c.sc->narrow) {
+        for (long long u = (long long)rg * wpb + warp; u < units; u += stride) {
+            const int i = (int)(u / nseg), s = (int)(u % nseg);
+            const int a = j0 + s * kSegCols, b = min(j0 + jn, a + kSegCols);
+            const uint64_t k = row_best_exact(I.cost + (size_t)i * I.ldc, c.pot[i], c.pot + m, a, b);
+            if (lane == 0) atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)k);
+        }
+        return;
+    }
+    for (int jj = threadIdx.x; jj < jn; jj += blockDim.x) vt[jj] = c.v32[j0 + jj];
+    __syncthreads();
+    const int4* v4 = reinterpret_cast<const int4*>(vt);
+    for (long long u = (long long)rg * wpb + warp; u < units; u += stride) {
+        const int i = (int)(u / nseg), s = (int)(u % nseg);
+        const int a = s * kSegCols, b = min(jn, a + kSegCols);   // tile-local columns [a, b)
         const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc + j0);
-        const int64_t u = c.pot[i];
-        uint64_t best = kNoKey;
-        #pragma unroll 4
-        for (int q = lane; q < nq; q += 32) {
-            const int4 cv = __ldcs(row + q);   // streamed once per round: do not keep in L1
-            const int jl = q * 4;
-            const int32_t cc[4] = {cv.x, cv.y, cv.z, cv.w};
+        int32_t bv = INT32_MAX, bj = INT32_MAX;
+        const int qa = a >> 2, qb = b >> 2;
+        if (qb - qa == kSegCols / 4) {
+            int4 cv[8];
             #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                if (jl + e < jn) {
-                    const int64_t r = (int64_t)cc[e] - u - vt[jl + e];
-                    const uint64_t k = pack_i32(clamp32(r), (uint32_t)(j0 + jl + e));
-                    best = k < best ? k : best;
-                }
+            for (int k = 0; k < 8; k++) cv[k] = ld_stream4(row + qa + lane + 32 * k);
+            #pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int q = qa + lane + 32 * k;
+                min4(bv, bj, cv[k], v4[q], j0 + 4 * q);
+            }
+        } else {
+            for (int q = qa + lane; q < qb; q += 32) min4(bv, bj, ld_stream4(row + q), v4[q], j0 + 4 * q);
+            if (lane < b - 4 * qb) {
+                const int jl = 4 * qb + lane;
+                const int32_t tv = I.cost[(size_t)i * I.ldc + j0 + jl] - vt[jl];
+                if (tv < bv) { bv = tv; bj = j0 + jl; }
             }
         }
-        best = warp_min_u64(best);
-        if (lane == 0) {
-            if (ntile == 1) c.row_best[i] = best;
-            else atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)best);
-        }
+        const uint64_t k = narrow_row_key(c, i, j0 + a, j0 + b, bv, bj);
+        if (lane == 0) atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)k);
     }
 }
+
+// Launch shape of k_sweep for an m x n instance: column tiles of at most
+// kSweepTile, two blocks per SM in total, no more blocks than work units.
+static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile);
 
 __global__ void __launch_bounds__(1024) k_pivot(Ctx c) {
     __shared__ BlockScratch bs;
@@ -131,6 +163,19 @@ __global__ void __launch_bounds__(256) k_cert_cells(Ctx c) {
     }
 }
 
+
+// int32 column duals and the narrow flag from pot[] (benchmark hook: the
+// solver publishes them from the dual recompute).
+__global__ void __launch_bounds__(1024) k_publish_duals(Ctx c) {
+    const int m = c.I.m, n = c.I.n;
+    int wide = 0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) c.v32[j] = narrow_dual(c.pot[m + j], wide);
+    wide = __syncthreads_or(wide);
+    if (threadIdx.x == 0) c.sc->narrow = !wide;
+}
+
+// Test hook: the CTA-local sweep on one instance (one block).
+__global__ void __launch_bounds__(1024) k_sweep_cta_only(Ctx c) { sweep_cta(c); }
 
 __global__ void k_fill_bench(int32_t* cost, size_t cells, int64_t* pot, int V) {
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < cells; k += (size_t)gridDim.x * blockDim.x)
@@ -234,6 +279,7 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     c.acc1 = (int64_t*)k.S(8 * (size_t)V);
     c.row_best = (uint64_t*)k.S(8 * (size_t)M);
     c.pot = (int64_t*)k.S(8 * (size_t)V);
+    c.v32 = (int32_t*)k.S(4 * (size_t)V);
 }
 
 __host__ __device__ inline size_t staged_bytes(int V, int M) {
@@ -241,6 +287,7 @@ __host__ __device__ inline size_t staged_bytes(int V, int M) {
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V);
     k.S(8 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
+    k.S(4 * (size_t)V);
     return (k.so + 15) & ~size_t(15);
 }
 
@@ -310,7 +357,8 @@ __global__ void __launch_bounds__(256) k_bfinal(BatchArgs a) {
 // Persistent form: a CTA takes the next instance of the bucket (largest
 // first) and runs it from the initial solution to the certificate, all
 // pricing rounds inside with the tree resident in shared memory.
-__global__ void __launch_bounds__(256, 4) k_bsolve(BatchArgs a) {
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
     __shared__ BlockScratch bs;
     __shared__ int s_idx;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -321,6 +369,14 @@ __global__ void __launch_bounds__(256, 4) k_bsolve(BatchArgs a) {
         if (!a.sc[d.index].done) brounds_one(a, d, bs, smem, 1 << 30);
         bfinal_one(a, d, bs);
     }
+}
+
+// The persistent kernel compiled for the block size: up to 256 threads four
+// blocks per SM (64 registers), 512 two, 1024 one.
+static const void* bsolve_fn(int threads) {
+    if (threads <= 256) return (const void*)k_bsolve<256, 4>;
+    if (threads <= 512) return (const void*)k_bsolve<512, 2>;
+    return (const void*)k_bsolve<1024, 1>;
 }
 
 }  // namespace flock
@@ -411,7 +467,6 @@ struct PlainSolver {
         FLOCK_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         for (auto& e : ev) FLOCK_CK(cudaEventCreate(&e));
         FLOCK_CK(h_sc.ensure(sizeof(Scalars)));
-        FLOCK_CK(cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 8));
         init = true;
         return FLOCK_OK;
     }
@@ -490,12 +545,8 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     k_setup<<<1, nt, 0, P.stream>>>(c, opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL);
     FLOCK_CK(cudaGetLastError());
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
-    // sweep launch shape
-    const int tile = std::min((n + 3) & ~3, 8192);
-    const int ntile = (n + tile - 1) / tile;
-    const int nrg = std::max(1, std::min((m + 7) / 8, (4 * num_sms()) / ntile));
-    const int grid = ntile * nrg;
-    const size_t smem = (size_t)tile * 8;
+    int grid = 0, tile = 0, ntile = 0;
+    sweep_shape(m, n, &grid, &tile, &ntile);
     // pivot loop: chunks of rounds captured once as a CUDA graph
     int chunk = 8;
     cudaGraphExec_t exec = nullptr;
@@ -508,7 +559,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
             cudaGraph_t g;
             FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
             for (int r = 0; r < chunk; r++) {
-                k_sweep<<<grid, 256, smem, P.stream>>>(c, tile, ntile);
+                k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
                 k_pivot<<<1, nt, 0, P.stream>>>(c);
             }
             FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
@@ -593,6 +644,60 @@ static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* even
 // Benchmark hook: time `iters` launches of the fused sweep on an m x n matrix
 // with random costs and duals already resident (no pivots).  Writes the
 // average launch time (CUDA events on the launching stream).
+static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile) {
+    const int ldc = (n + 3) & ~3;
+    *tile = std::min(ldc, kSweepTile);
+    *ntile = (n + *tile - 1) / *tile;
+    const int nseg = (std::min(*tile, n) + kSegCols - 1) / kSegCols;
+    const long long wpb = kSweepThreads / 32;
+    const long long want = ((long long)m * nseg + wpb - 1) / wpb;
+    const long long cap = std::max(1, (2 * num_sms()) / *ntile);
+    const int nrg = (int)std::max(1LL, std::min(want, cap));
+    *grid = *ntile * nrg;
+}
+
+// Test hook: one sweep over caller-given costs (m x n, row-major) and duals
+// (pot[V], rows then columns; kDeadPot marks a zero-demand column), row keys
+// back in keys[m].  cta_form: 0 grid-wide k_sweep, 1 the CTA-local sweep of
+// the batched form with `threads` threads.
+static int test_sweep(int m, int n, const int32_t* cost, const int64_t* pot, uint64_t* keys, int cta_form,
+                      int threads) {
+    if (m < 1 || n < 1 || !cost || !pot || !keys) return FLOCK_ERR_ARG;
+    if (cta_form && (threads < 32 || threads > 1024 || threads % 32)) return FLOCK_ERR_ARG;
+    PlainSolver& P = plain();
+    std::lock_guard<std::mutex> lk(P.mu);
+    int rc = P.setup();
+    if (rc) return rc;
+    const int V = m + n, ldc = (n + 3) & ~3;
+    FLOCK_CK(P.cost.ensure((size_t)m * ldc * 4 + 16));
+    size_t gbytes = 0;
+    Ctx probe;
+    carve_ctx(probe, nullptr, V, m, nullptr, nullptr, nullptr, &gbytes);
+    FLOCK_CK(P.ws.ensure(al256(gbytes) + al256(sizeof(Scalars))));
+    Ctx c;
+    carve_ctx(c, P.ws.as<uint8_t>(), V, m, nullptr, nullptr);
+    c.sc = P.ws.as<Scalars>(al256(gbytes));
+    c.I.m = m; c.I.n = n; c.I.ldc = ldc; c.I.cost = P.cost.as<int32_t>();
+    if ((rc = P.reset_scalars(c.sc, 1, 1))) return rc;
+    FLOCK_CK(cudaMemsetAsync(P.cost.p, 0x7f, (size_t)m * ldc * 4, P.stream));   // padding: never read
+    FLOCK_CK(cudaMemcpy2DAsync(P.cost.p, (size_t)ldc * 4, cost, (size_t)n * 4, (size_t)n * 4, m,
+                               cudaMemcpyHostToDevice, P.stream));
+    FLOCK_CK(cudaMemcpyAsync(c.pot, pot, (size_t)V * 8, cudaMemcpyHostToDevice, P.stream));
+    k_publish_duals<<<1, 1024, 0, P.stream>>>(c);
+    FLOCK_CK(cudaMemsetAsync(c.row_best, 0xff, (size_t)m * 8, P.stream));
+    if (cta_form) {
+        k_sweep_cta_only<<<1, threads, 0, P.stream>>>(c);
+    } else {
+        int grid = 0, tile = 0, ntile = 0;
+        sweep_shape(m, n, &grid, &tile, &ntile);
+        k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
+    }
+    FLOCK_CK(cudaGetLastError());
+    FLOCK_CK(cudaMemcpyAsync(keys, c.row_best, (size_t)m * 8, cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaStreamSynchronize(P.stream));
+    return FLOCK_OK;
+}
+
 static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
     if (m < 1 || n < 1 || iters < 1 || !avg_ms) return FLOCK_ERR_ARG;
     PlainSolver& P = plain();
@@ -613,13 +718,13 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
     k_fill_bench<<<std::min(4096, (int)(((size_t)m * ldc + 255) / 256)), 256, 0, P.stream>>>(
         P.cost.as<int32_t>(), (size_t)m * ldc, c.pot, V);
     FLOCK_CK(cudaGetLastError());
-    const int tile = std::min(ldc, 8192);
-    const int ntile = (n + tile - 1) / tile;
-    const int nrg = std::max(1, std::min((m + 7) / 8, (4 * num_sms()) / ntile));
-    const size_t smem = (size_t)tile * 8;
-    for (int w = 0; w < 3; w++) k_sweep<<<ntile * nrg, 256, smem, P.stream>>>(c, tile, ntile);
+    k_publish_duals<<<1, 1024, 0, P.stream>>>(c);
+    FLOCK_CK(cudaMemsetAsync(c.row_best, 0xff, (size_t)m * 8, P.stream));
+    int grid = 0, tile = 0, ntile = 0;
+    sweep_shape(m, n, &grid, &tile, &ntile);
+    for (int w = 0; w < 3; w++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
-    for (int k = 0; k < iters; k++) k_sweep<<<ntile * nrg, 256, smem, P.stream>>>(c, tile, ntile);
+    for (int k = 0; k < iters; k++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     FLOCK_CK(cudaEventSynchronize(P.ev[1]));
     float ms = 0;
@@ -632,9 +737,9 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 // -------------------------------------------------------- batched solver ---
 // Size buckets by V = m + n.  Instances above the last edge run on the plain
 // path (their staged tree would not fit in shared memory).
-static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 3072};
+static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944};
 static const int kNumBuckets = 7;
-static const int kMaxStagedV = 3072;
+static const int kMaxStagedV = 2944;   // staged_bytes(2944, 2943) fits the 226 KB opt-in
 static const int kMaxChunk = 64;
 
 static int bucket_of(int V) {
@@ -697,7 +802,8 @@ struct BatchRunner {
         FLOCK_CK(cudaEventCreate(&ev_done));
         FLOCK_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
         FLOCK_CK(cudaFuncSetAttribute(k_bround, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
-        FLOCK_CK(cudaFuncSetAttribute(k_bsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
+        for (int t : {256, 512, 1024})
+            FLOCK_CK(cudaFuncSetAttribute(bsolve_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
         FLOCK_CK(d_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         FLOCK_CK(h_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         init = true;
@@ -794,7 +900,7 @@ struct BatchRunner {
             t = g_tuned_ok[b] ? g_tuned[b] : default_cfg(bmaxV[b]);
         }
         const char* f = getenv("FLOCK_BATCH_FORM");
-        if (f && !strcmp(f, "round")) t.persistent = 0;
+        if (f && !strcmp(f, "round")) { t.persistent = 0; t.threads = std::min(std::max(t.threads, 128), 256); }
         if (f && !strcmp(f, "persistent")) t.persistent = 1;
         return t;
     }
@@ -871,8 +977,10 @@ struct BatchRunner {
             if (cfg[b].persistent) {
                 const size_t smem = staged_bytes(bmaxV[b], bmaxM[b]);
                 FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
-                k_bsolve<<<grid_for(b, cfg[b], smem, (const void*)k_bsolve), cfg[b].threads, smem, st[b]>>>(a);
-                FLOCK_CK(cudaGetLastError());
+                const void* fn = bsolve_fn(cfg[b].threads);
+                void* kargs[] = {&a};
+                FLOCK_CK(cudaLaunchKernel(fn, dim3(grid_for(b, cfg[b], smem, fn)), dim3(cfg[b].threads), kargs, smem,
+                                          st[b]));
                 launches++;
                 continue;
             }
@@ -999,8 +1107,8 @@ struct BatchRunner {
 
     // Autotune each bucket with enough instances: the bucket alone is solved
     // once per candidate configuration (inputs resident) and the fastest wins.
-    // Block sizes are limited to the ones validated on the GPU for the
-    // bucket's sizes (128/256 up to V = 256, 256 above).
+    // Candidates: the persistent form at three block sizes scaled to the
+    // bucket's largest instance, and the round form at 128/256 threads.
     int autotune() {
         int rc = ensure_device();
         if (rc) return rc;
@@ -1013,10 +1121,14 @@ struct BatchRunner {
                 if (g_tuned_ok[b] || nb < 32) continue;
             }
             std::vector<TuneCfg> cands;
+            // persistent form: three block sizes around the bucket's size
+            const int V = bmaxV[b];
+            const int t0 = V <= 128 ? 32 : V <= 256 ? 64 : V <= 512 ? 128 : 256;
+            for (int t = t0; t <= 4 * t0; t *= 2) cands.push_back(TuneCfg{t, 1, 16, 1});
+            // round form (graph-captured chunks of k_bround)
             const int thr[2] = {128, 256};
             for (int ti = 0; ti < 2; ti++) {
                 if (thr[ti] == 128 && bmaxV[b] > 256) continue;
-                cands.push_back(TuneCfg{thr[ti], 1, 16, 1});
                 for (int gm = 1; gm <= 2; gm++)
                     for (int ch : {8, 32}) cands.push_back(TuneCfg{thr[ti], gm, ch, 0});
             }
@@ -1125,6 +1237,12 @@ int flock_bench_batch_rerun(float* ms, int32_t* launches) { return flock::batch_
  * m x n matrix (random costs and duals, inputs resident). */
 int flock_bench_sweep(int32_t m, int32_t n, int32_t iters, float* avg_ms, int32_t* tile) {
     return flock::bench_sweep(m, n, iters, avg_ms, tile);
+}
+
+/* Test hook: one reduced-cost sweep over host costs and duals, row keys back. */
+int flock_test_sweep(int32_t m, int32_t n, const int32_t* cost, const int64_t* pot, uint64_t* keys,
+                     int32_t cta_form, int32_t threads) {
+    return flock::test_sweep(m, n, cost, pot, keys, cta_form, threads);
 }
 
 }  // extern "C"

@@ -287,41 +287,103 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
         int32_t* t2 = lA; lA = lB; lB = t2;
         int64_t* t3 = xA; xA = xB; xB = t3;
     }
+    int wide = 0;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int64_t p = xA[v];
         c.depth[v] = lA[v];
-        c.pot[v] = xA[v];
+        c.pot[v] = p;
+        if (v >= I.m) c.v32[v - I.m] = narrow_dual(p, wide);
     }
-    if (pending && threadIdx.x == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+    wide = __syncthreads_or(wide);
+    if (threadIdx.x == 0) {
+        c.sc->narrow = !wide;
+        if (pending) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+    }
     __syncthreads();
 }
 
 // ---------------------------------------------------------------- sweep -----
+// Row best key with per-element int64 reduced costs over columns [j0, j1):
+// min over j of (clamp32(c_ij - u_i - v_j), j).  One warp, all lanes return it.
+// (row: the row's costs, vp: the column duals.)  Plain arguments keep the
+// rarely taken call from forcing the caller's context into local memory.
+__device__ __noinline__ uint64_t row_best_exact(const int32_t* row, int64_t u, const int64_t* vp, int j0, int j1) {
+    uint64_t best = kNoKey;
+    for (int j = j0 + (int)(threadIdx.x & 31); j < j1; j += 32) {
+        const int64_t r = (int64_t)row[j] - u - vp[j];
+        const uint64_t k = pack_i32(clamp32(r), (uint32_t)j);
+        best = k < best ? k : best;
+    }
+    return warp_min_u64(best);
+}
+
+// Narrow form: t = c_ij - v_j in int32 (exact while sc->narrow), running
+// minimum with the first column among equal values.
+__device__ __forceinline__ void min4(int32_t& bv, int32_t& bj, const int4 cv, const int4 vv, int j) {
+    int32_t t;
+    t = cv.x - vv.x; if (t < bv) { bv = t; bj = j; }
+    t = cv.y - vv.y; if (t < bv) { bv = t; bj = j + 1; }
+    t = cv.z - vv.z; if (t < bv) { bv = t; bj = j + 2; }
+    t = cv.w - vv.w; if (t < bv) { bv = t; bj = j + 3; }
+}
+
+// Turn the warp's narrow minimum over columns [j0, j1) of row i into the
+// row key.  The key equals row_best_exact's unless the winning column is a
+// zero-demand one or the reduced cost is below INT32_MIN; those rows are
+// recomputed exactly (all lanes agree on the branch).
+__device__ __forceinline__ uint64_t narrow_row_key(const Ctx& c, int i, int j0, int j1, int32_t bv, int32_t bj) {
+    const uint64_t kk = warp_min_u64(pack_i32(bv, (uint32_t)bj));
+    const int jw = (int)key_idx(kk);
+    const int64_t r = (int64_t)key_val(kk) - c.pot[i];
+    if (c.v32[jw] == kDead32 || r < INT32_MIN)
+        return row_best_exact(c.I.cost + (size_t)i * c.I.ldc, c.pot[i], c.pot + c.I.m, j0, j1);
+    return pack_i32(clamp32(r), (uint32_t)jw);
+}
+
 // CTA-local sweep: best (reduced cost, column) of every row into row_best[].
-// Rows are int4-vectorised: the row pitch is a multiple of 4 and 16-byte aligned.
+// Rows are int4-vectorised (row pitch a multiple of 4, 16-byte aligned);
+// each lane keeps four row loads in flight.
 __device__ void sweep_cta(const Ctx& c) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int64_t* vpot = c.pot + m;
+    if (!c.sc->narrow) {
+        for (int i = threadIdx.x >> 5; i < m; i += nw) {
+            const uint64_t k = row_best_exact(I.cost + (size_t)i * I.ldc, c.pot[i], c.pot + m, 0, n);
+            if (lane == 0) c.row_best[i] = k;
+        }
+        __syncthreads();
+        return;
+    }
+    const int nfull = n >> 2, tail = n & 3;
+    const int4* v4 = reinterpret_cast<const int4*>(c.v32);
     for (int i = threadIdx.x >> 5; i < m; i += nw) {
         const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
-        const int64_t u = c.pot[i];
-        uint64_t best = kNoKey;
-        for (int q = lane; q * 4 < n; q += 32) {
-            const int4 cv = row[q];
-            const int j = q * 4;
-            const int32_t cc[4] = {cv.x, cv.y, cv.z, cv.w};
-            #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                if (j + e < n) {
-                    const int64_t r = (int64_t)cc[e] - u - vpot[j + e];
-                    const uint64_t k = pack_i32(clamp32(r), (uint32_t)(j + e));
-                    best = k < best ? k : best;
-                }
-            }
+        int32_t bv = INT32_MAX, bj = INT32_MAX;
+        int q = lane;
+        for (; q + 96 < nfull; q += 128) {
+            const int4 a0 = row[q], a1 = row[q + 32], a2 = row[q + 64], a3 = row[q + 96];
+            min4(bv, bj, a0, v4[q], 4 * q);
+            min4(bv, bj, a1, v4[q + 32], 4 * (q + 32));
+            min4(bv, bj, a2, v4[q + 64], 4 * (q + 64));
+            min4(bv, bj, a3, v4[q + 96], 4 * (q + 96));
         }
-        best = warp_min_u64(best);
-        if (lane == 0) c.row_best[i] = best;
+        if (q + 32 < nfull) {
+            const int4 a0 = row[q], a1 = row[q + 32];
+            const int4 a2 = q + 64 < nfull ? row[q + 64] : make_int4(0, 0, 0, 0);
+            min4(bv, bj, a0, v4[q], 4 * q);
+            min4(bv, bj, a1, v4[q + 32], 4 * (q + 32));
+            if (q + 64 < nfull) min4(bv, bj, a2, v4[q + 64], 4 * (q + 64));
+        } else if (q < nfull) {
+            min4(bv, bj, row[q], v4[q], 4 * q);
+        }
+        if (lane < tail) {
+            const int j = 4 * nfull + lane;
+            const int32_t t = I.cost[(size_t)i * I.ldc + j] - c.v32[j];
+            if (t < bv) { bv = t; bj = j; }
+        }
+        const uint64_t k = narrow_row_key(c, i, 0, n, bv, bj);
+        if (lane == 0) c.row_best[i] = k;
     }
     __syncthreads();
 }
@@ -404,6 +466,9 @@ __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const Cy
     }
 }
 
+// Parallel mode: candidates walked per round (the rest wait for later rounds).
+constexpr int kMaxCand = 32;
+
 // One pricing round after sweep: choose candidates, claim, apply.
 __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
@@ -423,9 +488,42 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         best = block_min_u64(best, bs);
         if (threadIdx.x == 0 && best != kNoKey) { c.cand[0] = (int32_t)key_idx(best); bs.i[0] = 1; }
     } else {
+        // Candidates: the rows with the most negative best reduced costs, at
+        // most kMaxCand (plus ties of the boundary bin when the first bin
+        // alone exceeds it).  A 32-bin histogram over [rmin, 0) picks the
+        // threshold, so the set depends only on the values.  A candidate is
+        // applied only if no better candidate's cycle shares an edge with it,
+        // so leaving out weaker rows changes no decision among the rest; the
+        // cap bounds the cycle walks of a round.
+        int32_t rmin = 0;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             const uint64_t k = c.row_best[i];
-            if (k != kNoKey && key_val(k) < 0) c.cand[atomicAdd(&bs.i[0], 1)] = i;
+            if (k != kNoKey) rmin = min(rmin, key_val(k));
+        }
+        rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
+        if (rmin < 0) {
+            const int64_t span = -(int64_t)rmin;
+            if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
+            __syncthreads();
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const uint64_t k = c.row_best[i];
+                if (k != kNoKey && key_val(k) < 0)
+                    atomicAdd((unsigned long long*)&bs.red2[((int64_t)key_val(k) - rmin) * 32 / span], 1ull);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint64_t cum = bs.red2[0];
+                int last = 0;
+                for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)kMaxCand; b++) { cum += bs.red2[b]; last = b; }
+                bs.i[1] = last;
+            }
+            __syncthreads();
+            const int last = bs.i[1];
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const uint64_t k = c.row_best[i];
+                if (k != kNoKey && key_val(k) < 0 && ((int64_t)key_val(k) - rmin) * 32 / span <= last)
+                    c.cand[atomicAdd(&bs.i[0], 1)] = i;
+            }
         }
     }
     __syncthreads();

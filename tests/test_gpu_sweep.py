@@ -1,0 +1,117 @@
+"""Reduced-cost sweep parity: the grid-wide k_sweep and the CTA-local sweep of
+the batched form against an exact int64 restatement in numpy.
+
+The row key is min over j of (clamp32(c_ij - u_i - v_j), j), the smaller
+column winning ties.  Cases cover the int32 (narrow) form, ragged and tiny
+widths, several column tiles, zero-demand columns (dual kDeadPot), reduced
+costs below INT32_MIN (exact rescan) and duals too wide for int32.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import flock_gb300 as fg
+
+pytestmark = pytest.mark.gpu
+
+DEAD = -(1 << 61)
+
+
+def expected_keys(cost, pot):
+    m, n = cost.shape
+    u = pot[:m].astype(np.int64)
+    v = pot[m:].astype(np.int64)
+    r = cost.astype(np.int64) - u[:, None] - v[None, :]
+    rc = np.clip(r, -(1 << 31), (1 << 31) - 1)
+    hi = (rc.astype(np.int64) ^ np.int64(-(1 << 31))) & 0xFFFFFFFF   # (uint32)value ^ 0x80000000
+    keys = (hi.astype(np.uint64) << np.uint64(32)) | np.arange(n, dtype=np.uint64)[None, :]
+    return keys.min(axis=1)
+
+
+def gpu_keys(cost, pot, cta_form=0, threads=256):
+    L = fg.lib()
+    f = L.flock_test_sweep
+    f.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_int32, ctypes.c_int32]
+    cost = np.ascontiguousarray(cost, np.int32)
+    pot = np.ascontiguousarray(pot, np.int64)
+    m, n = cost.shape
+    keys = np.zeros(m, np.uint64)
+    rc = f(m, n, cost.ctypes.data, pot.ctypes.data, keys.ctypes.data, cta_form, threads)
+    assert rc == 0, L.flock_last_error()
+    return keys
+
+
+def case(seed, m, n, lo=1, hi=1000, plo=-500, phi=500):
+    rng = np.random.default_rng(seed)
+    cost = rng.integers(lo, hi + 1, size=(m, n), dtype=np.int64).astype(np.int32)
+    pot = rng.integers(plo, phi + 1, size=m + n, dtype=np.int64)
+    return cost, pot
+
+
+SHAPES = [(1, 1), (3, 2), (5, 3), (7, 4), (37, 53), (64, 1023), (9, 1024), (9, 1025), (4, 2050),
+          (300, 301), (2, 8192), (3, 8193), (2, 20003)]
+
+
+@pytest.mark.parametrize("m,n", SHAPES)
+def test_sweep_narrow(m, n):
+    cost, pot = case(m * 7919 + n, m, n)
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    if n <= 3000:
+        for thr in (32, 128, 256):
+            np.testing.assert_array_equal(gpu_keys(cost, pot, 1, thr), exp)
+
+
+@pytest.mark.parametrize("m,n", [(5, 7), (40, 1500), (3, 9000)])
+def test_sweep_ties_and_dead_columns(m, n):
+    cost = np.full((m, n), 5, np.int32)
+    pot = np.zeros(m + n, np.int64)
+    pot[m + 1::3] = DEAD              # zero-demand columns: never the row best while others are negative
+    pot[:m] = 7                       # every live reduced cost is -2: first live column wins
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    if n <= 3000:
+        np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 256), exp)
+    # a dead column holds the int32 minimum (cheaper cost, live duals at the
+    # window's lower edge): the row is recomputed exactly
+    dead = np.zeros(n, bool)
+    dead[1::3] = True
+    cost[:, dead] = 0
+    pot[:m] = 0
+    pot[m:][~dead] = -(1 << 30) + 2
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    if n <= 3000:
+        np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 128), exp)
+
+
+def test_sweep_clamped_rows():
+    """Reduced costs below INT32_MIN: several columns clamp, the first wins."""
+    cost, pot = case(11, 50, 3000)
+    pot[:25] = (1 << 40)              # huge row duals: every r < INT32_MIN in rows 0..24
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 256), exp)
+
+
+def test_sweep_wide_duals():
+    """A column dual outside the int32 window: the exact int64 form runs."""
+    cost, pot = case(12, 60, 2500, plo=-(1 << 20), phi=(1 << 20))
+    pot[60 + 17] = (1 << 35)
+    pot[60 + 2000] = -(1 << 33)
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 256), exp)
+
+
+def test_sweep_extreme_costs():
+    """Costs at the accepted limits +-2^30 with duals at the narrow window's edge."""
+    rng = np.random.default_rng(13)
+    m, n = 20, 777
+    cost = rng.choice(np.array([-(1 << 30), (1 << 30), 0, 1, -1], np.int64), size=(m, n)).astype(np.int32)
+    pot = rng.integers(-(1 << 30) + 2, (1 << 30) - 1, size=m + n, dtype=np.int64)
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 256), exp)
