@@ -31,6 +31,7 @@ struct BatchArgs {
     uint8_t* ws;                // per-instance working sets
     int32_t maxV, maxM;         // largest instance of the launch (shared-memory staging size)
     int32_t bfs_method, mode, max_rounds;
+    int32_t light;              // 1: stage only the per-step tree arrays (largest bucket)
 };
 
 struct Carver {

@@ -16,11 +16,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/flock.h"
@@ -30,7 +32,7 @@
 namespace flock {
 
 // ------------------------------------------------------------ kernels ------
-__global__ void __launch_bounds__(1024) k_setup(Ctx c, int bfs_method) {
+__global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method) {
     __shared__ BlockScratch bs;
     if (bfs_method == FLOCK_BFS_VOGEL) {
         vogel_cta(c, bs);
@@ -44,7 +46,7 @@ __global__ void __launch_bounds__(1024) k_setup(Ctx c, int bfs_method) {
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
-__global__ void __launch_bounds__(1024) k_vogel_only(Ctx c) {
+__global__ void __launch_bounds__(1024, 1) k_vogel_only(Ctx c) {
     __shared__ BlockScratch bs;
     vogel_cta(c, bs);
 }
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int
 // kSweepTile, two blocks per SM in total, no more blocks than work units.
 static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile);
 
-__global__ void __launch_bounds__(1024) k_pivot(Ctx c) {
+__global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
     __shared__ BlockScratch bs;
     if (c.sc->done) return;
     pivot_round_cta(c, bs);
@@ -134,7 +136,7 @@ __global__ void __launch_bounds__(1024) k_pivot(Ctx c) {
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
-__global__ void __launch_bounds__(1024) k_finalize(Ctx c) {
+__global__ void __launch_bounds__(1024, 1) k_finalize(Ctx c) {
     __shared__ BlockScratch bs;
     if (c.sc->status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) return;
     finalize_cta(c, bs);
@@ -264,31 +266,42 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
     }
 }
 
-// shared-memory staging of the arrays every pivot step touches
-__device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
-    Carver k{nullptr, 0, smem, 0};
-    c.parent = (int32_t*)k.S(4 * (size_t)V);
-    c.depth = (int32_t*)k.S(4 * (size_t)V);
-    c.flow = (int64_t*)k.S(8 * (size_t)V);
-    c.claim = (uint64_t*)k.S(8 * (size_t)V);
-    c.anc0 = (int32_t*)k.S(4 * (size_t)V);
-    c.anc1 = (int32_t*)k.S(4 * (size_t)V);
-    c.len0 = (int32_t*)k.S(4 * (size_t)V);
-    c.len1 = (int32_t*)k.S(4 * (size_t)V);
-    c.acc0 = (int64_t*)k.S(8 * (size_t)V);
-    c.acc1 = (int64_t*)k.S(8 * (size_t)V);
-    c.row_best = (uint64_t*)k.S(8 * (size_t)M);
-    c.pot = (int64_t*)k.S(8 * (size_t)V);
-    c.v32 = (int32_t*)k.S(4 * (size_t)V);
+// Shared-memory staging of the arrays every pivot step touches.  Light
+// staging (the largest bucket) keeps the pointer-jumping buffers and the
+// edge claims in the instance's global working set.
+__host__ __device__ inline size_t stage_layout(Ctx* c, unsigned char* smem, int V, int M, bool light) {
+    Carver k{nullptr, 0, smem ? smem : (unsigned char*)16, 0};
+    int32_t* parent = (int32_t*)k.S(4 * (size_t)V);
+    int32_t* depth = (int32_t*)k.S(4 * (size_t)V);
+    int64_t* flow = (int64_t*)k.S(8 * (size_t)V);
+    uint64_t* row_best = (uint64_t*)k.S(8 * (size_t)M);
+    int64_t* pot = (int64_t*)k.S(8 * (size_t)V);
+    int32_t* v32 = (int32_t*)k.S(4 * (size_t)V);
+    if (c) {
+        c->parent = parent; c->depth = depth; c->flow = flow; c->row_best = row_best; c->pot = pot; c->v32 = v32;
+    }
+    if (!light) {
+        uint64_t* claim = (uint64_t*)k.S(8 * (size_t)V);
+        int32_t* anc0 = (int32_t*)k.S(4 * (size_t)V);
+        int32_t* anc1 = (int32_t*)k.S(4 * (size_t)V);
+        int32_t* len0 = (int32_t*)k.S(4 * (size_t)V);
+        int32_t* len1 = (int32_t*)k.S(4 * (size_t)V);
+        int64_t* acc0 = (int64_t*)k.S(8 * (size_t)V);
+        int64_t* acc1 = (int64_t*)k.S(8 * (size_t)V);
+        if (c) {
+            c->claim = claim; c->anc0 = anc0; c->anc1 = anc1; c->len0 = len0; c->len1 = len1;
+            c->acc0 = acc0; c->acc1 = acc1;
+        }
+    }
+    return (k.so + 15) & ~size_t(15);
 }
 
-__host__ __device__ inline size_t staged_bytes(int V, int M) {
-    Carver k{nullptr, 0, (unsigned char*)16, 0};
-    k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
-    k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V);
-    k.S(8 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
-    k.S(4 * (size_t)V);
-    return (k.so + 15) & ~size_t(15);
+__device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M, bool light) {
+    stage_layout(&c, smem, V, M, light);
+}
+
+__host__ __device__ inline size_t staged_bytes(int V, int M, bool light) {
+    return stage_layout(nullptr, nullptr, V, M, light);
 }
 
 // Pricing rounds of one instance with its tree staged in shared memory:
@@ -298,7 +311,7 @@ __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch
     Ctx g;
     batch_ctx(a, d, g);
     Ctx c = g;
-    stage_hot(c, smem, a.maxV, a.maxM);
+    stage_hot(c, smem, a.maxV, a.maxM, a.light != 0);
     const int V = d.m + d.n;
     for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
     __syncthreads();
@@ -433,18 +446,59 @@ struct HostBuf {
 static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 static const int32_t kFailMask = ST_ITER_CAP | ST_TREE_CORRUPT | ST_SF_FAIL | ST_CERT_FAIL | ST_RANGE;
 
-int validate_instance(const flock_instance* I) {
-    if (!I || !I->supply || !I->demand || !I->cost || I->m < 1 || I->n < 1) { set_error("invalid instance"); return FLOCK_ERR_ARG; }
-    if ((int64_t)I->m + I->n > (1 << 28) || (int64_t)I->m * I->n > ((int64_t)1 << 34)) { set_error("instance too large"); return FLOCK_ERR_RANGE; }
+// Every check of validate_instance except the per-cost range check.
+static int validate_shape(const flock_instance* I, std::string* msg) {
+    if (!I || !I->supply || !I->demand || !I->cost || I->m < 1 || I->n < 1) { *msg = "invalid instance"; return FLOCK_ERR_ARG; }
+    if ((int64_t)I->m + I->n > (1 << 28) || (int64_t)I->m * I->n > ((int64_t)1 << 34)) { *msg = "instance too large"; return FLOCK_ERR_RANGE; }
     int64_t S = 0, D = 0;
-    for (int i = 0; i < I->m; i++) { if (I->supply[i] < 0) { set_error("negative supply"); return FLOCK_ERR_ARG; } S += I->supply[i]; }
-    for (int j = 0; j < I->n; j++) { if (I->demand[j] < 0) { set_error("negative demand"); return FLOCK_ERR_ARG; } D += I->demand[j]; }
-    if (S != D) { set_error("unbalanced instance"); return FLOCK_ERR_UNBALANCED; }
-    const size_t mn = (size_t)I->m * I->n;
-    for (size_t k = 0; k < mn; k++) {
-        const int32_t c = I->cost[k];
-        if (c > (1 << 30) || c < -(1 << 30)) { set_error("cost out of range"); return FLOCK_ERR_RANGE; }
+    for (int i = 0; i < I->m; i++) { if (I->supply[i] < 0) { *msg = "negative supply"; return FLOCK_ERR_ARG; } S += I->supply[i]; }
+    for (int j = 0; j < I->n; j++) { if (I->demand[j] < 0) { *msg = "negative demand"; return FLOCK_ERR_ARG; } D += I->demand[j]; }
+    if (S != D) { *msg = "unbalanced instance"; return FLOCK_ERR_UNBALANCED; }
+    return FLOCK_OK;
+}
+
+static bool costs_in_range(const int32_t* c, size_t cnt) {
+    int bad = 0;
+    for (size_t k = 0; k < cnt; k++) bad |= (c[k] > (1 << 30)) | (c[k] < -(1 << 30));
+    return !bad;
+}
+
+// Copy one cost row and check the accepted range |c| <= 2^30 in the same pass.
+static bool copy_costs_checked(int32_t* dst, const int32_t* src, int n) {
+    int bad = 0;
+    for (int j = 0; j < n; j++) {
+        const int32_t v = src[j];
+        dst[j] = v;
+        bad |= (v > (1 << 30)) | (v < -(1 << 30));
     }
+    return !bad;
+}
+
+// Run f(0..count-1) on up to hardware_concurrency() threads (dynamic chunks).
+template <class F>
+static void parallel_for(int count, const F& f) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nt = std::min(std::min(hw, 32), std::max(1, count / 16));
+    if (nt <= 1) { for (int k = 0; k < count; k++) f(k); return; }
+    std::atomic<int> next{0};
+    auto body = [&] {
+        for (;;) {
+            const int k0 = next.fetch_add(8);
+            if (k0 >= count) return;
+            for (int k = k0; k < std::min(count, k0 + 8); k++) f(k);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; t++) th.emplace_back(body);
+    body();
+    for (auto& t : th) t.join();
+}
+
+int validate_instance(const flock_instance* I) {
+    std::string msg;
+    const int rc = validate_shape(I, &msg);
+    if (rc) { set_error(msg); return rc; }
+    if (!costs_in_range(I->cost, (size_t)I->m * I->n)) { set_error("cost out of range"); return FLOCK_ERR_RANGE; }
     return FLOCK_OK;
 }
 
@@ -737,9 +791,12 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 // -------------------------------------------------------- batched solver ---
 // Size buckets by V = m + n.  Instances above the last edge run on the plain
 // path (their staged tree would not fit in shared memory).
-static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944};
-static const int kNumBuckets = 7;
-static const int kMaxStagedV = 2944;   // staged_bytes(2944, 2943) fits the 226 KB opt-in
+// The last bucket stages lightly (staged_bytes(4096, 4095, true) = 144 KB);
+// the others stage fully (staged_bytes(2944, 2943, false) fits 226 KB).
+static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944, 4096};
+static const int kNumBuckets = 8;
+static const int kMaxStagedV = 4096;
+static bool bucket_light(int b) { return b == kNumBuckets - 1; }
 static const int kMaxChunk = 64;
 
 static int bucket_of(int V) {
@@ -823,8 +880,13 @@ struct BatchRunner {
         plain_list.clear();
         total_cells = total_pot = total_cost = total_sd = total_ws = 0;
         std::vector<int64_t> cost_off(cnt), sd_off(cnt), ws_off(cnt);
+        // Validation in the order validate_instance uses, the O(m n) cost
+        // range check fused into the copy below (threads over instances);
+        // the first failing instance reports its first failing check.
+        std::vector<int> pre(cnt, FLOCK_OK);
+        std::vector<std::string> pre_msg(cnt);
         for (int k = 0; k < cnt; k++) {
-            if ((rc = validate_instance(&in[k]))) return rc;
+            if ((pre[k] = validate_shape(&in[k], &pre_msg[k]))) continue;
             const int m = in[k].m, n = in[k].n;
             m_of[k] = m; n_of[k] = n; V_of[k] = m + n;
             out_off[k] = total_cells; total_cells += m + n - 1;
@@ -837,17 +899,25 @@ struct BatchRunner {
         }
         FLOCK_CK(h_cost.ensure((size_t)total_cost * 4 + 16));
         FLOCK_CK(h_sd.ensure((size_t)total_sd * 4 + 16));
-        for (int k = 0; k < cnt; k++) {
-            if (V_of[k] > kMaxStagedV) continue;
-            const int m = m_of[k], n = n_of[k], ldc = (n + 3) & ~3;
+        std::vector<uint8_t> cost_bad(cnt, 0);
+        parallel_for(cnt, [&](int k) {
+            if (pre[k]) return;
+            const int m = m_of[k], n = n_of[k];
+            if (V_of[k] > kMaxStagedV) { cost_bad[k] = !costs_in_range(in[k].cost, (size_t)m * n); return; }
+            const int ldc = (n + 3) & ~3;
             int32_t* dst = h_cost.as<int32_t>() + cost_off[k];
-            if (ldc == n) memcpy(dst, in[k].cost, (size_t)m * n * 4);
-            else for (int i = 0; i < m; i++) {
-                memcpy(dst + (size_t)i * ldc, in[k].cost + (size_t)i * n, (size_t)n * 4);
-                memset(dst + (size_t)i * ldc + n, 0, (size_t)(ldc - n) * 4);
+            bool ok = true;
+            for (int i = 0; i < m; i++) {
+                ok &= copy_costs_checked(dst + (size_t)i * ldc, in[k].cost + (size_t)i * n, n);
+                for (int j = n; j < ldc; j++) dst[(size_t)i * ldc + j] = 0;
             }
+            cost_bad[k] = !ok;
             memcpy(h_sd.as<int32_t>() + sd_off[k], in[k].supply, (size_t)m * 4);
             memcpy(h_sd.as<int32_t>() + sd_off[k] + m, in[k].demand, (size_t)n * 4);
+        });
+        for (int k = 0; k < cnt; k++) {
+            if (pre[k]) { set_error(pre_msg[k]); return pre[k]; }
+            if (cost_bad[k]) { set_error("cost out of range"); return FLOCK_ERR_RANGE; }
         }
         // bucket, largest first inside each bucket (work stealing starts with the long solves)
         std::vector<int> order;
@@ -920,6 +990,7 @@ struct BatchRunner {
         a.sc = d_sc.as<Scalars>();
         a.ws = d_ws.as<uint8_t>();
         a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
+        a.light = bucket_light(b) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = opt.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : 1;
         a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
@@ -939,7 +1010,7 @@ struct BatchRunner {
     // Pricing rounds of bucket b as a CUDA graph: `chunk` x (zero the
     // counters, one k_bround launch).
     int capture_rounds(int b, const TuneCfg& t, cudaGraphExec_t* exec) {
-        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b]);
+        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b));
         const int grid = grid_for(b, t, smem, (const void*)k_bround);
         cudaStream_t s = st[b];
         cudaGraph_t g;
@@ -975,7 +1046,7 @@ struct BatchRunner {
             BatchArgs a = args_for(b);
             a.next = ctr(b);
             if (cfg[b].persistent) {
-                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b]);
+                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b));
                 FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
                 const void* fn = bsolve_fn(cfg[b].threads);
                 void* kargs[] = {&a};
@@ -1110,6 +1181,13 @@ struct BatchRunner {
     // Candidates: the persistent form at three block sizes scaled to the
     // bucket's largest instance, and the round form at 128/256 threads.
     int autotune() {
+        bool need = false;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            for (int b = 0; b < kNumBuckets; b++)
+                if (!g_tuned_ok[b] && bstart[b + 1] - bstart[b] >= 32) need = true;
+        }
+        if (!need) return FLOCK_OK;
         int rc = ensure_device();
         if (rc) return rc;
         if ((rc = upload())) return rc;

@@ -396,6 +396,38 @@ struct CycleResult {
     int32_t ok;
 };
 
+// Visit every tree edge on the path between vertices k and l: f(v, side)
+// for the edge whose child is v, side 0 on k's branch (in order from k
+// upward), 1 on l's branch (from l upward).  The endpoint depths are read
+// once: the deeper side climbs to equal depth, then both sides step
+// together, so a step costs one parent load per side and the two chains
+// overlap.  f returns false to stop.  Result: 0 done, 1 stopped by f,
+// -1 the parent/depth arrays are inconsistent.
+template <class F>
+__device__ __forceinline__ int walk_path(const Ctx& c, int k, int l, int V, F&& f) {
+    int x = k, y = l;
+    int dx = c.depth[x], dy = c.depth[y];
+    if ((unsigned)dx > (unsigned)V || (unsigned)dy > (unsigned)V) return -1;
+    for (; dx > dy; dx--) {
+        if (!f(x, 0)) return 1;
+        x = c.parent[x];
+        if (!FLOCK_IN(x, V)) return -1;
+    }
+    for (; dy > dx; dy--) {
+        if (!f(y, 1)) return 1;
+        y = c.parent[y];
+        if (!FLOCK_IN(y, V)) return -1;
+    }
+    for (int s = 0; x != y; s++) {
+        if (s > V) return -1;
+        if (!f(x, 0) || !f(y, 1)) return 1;
+        x = c.parent[x];
+        y = c.parent[y];
+        if (!FLOCK_IN(x, V) || !FLOCK_IN(y, V)) return -1;
+    }
+    return 0;
+}
+
 // Walk the cycle of entering cell (row k, column vertex l).  Edges on the
 // k side decrease when their child is a row, on the l side when the child is
 // a column.  Ties (impossible with the perturbation) resolve as Cunningham's
@@ -403,26 +435,20 @@ struct CycleResult {
 // If P != kNoKey every edge is claimed with atomicMin(claim, P).
 __device__ __forceinline__ CycleResult cycle_walk(const Ctx& c, int k, int l, uint64_t P, int V) {
     const int m = c.I.m;
-    int x = k, y = l;
     int64_t bk = INT64_MAX, bl = INT64_MAX;
     int qk = -1, ql = -1;
-    int steps = 0;
     CycleResult res;
     res.ok = 1;
-    while (x != y) {
-        if (++steps > 2 * V || !FLOCK_IN(x, V) || !FLOCK_IN(y, V)) { res.ok = 0; fail_check(c.sc, 11); break; }
-        const int dx = c.depth[x], dy = c.depth[y];
-        if (dx >= dy) {
-            if (x < m) { const int64_t f = c.flow[x]; if (f < bk) { bk = f; qk = x; } }
-            if (P != kNoKey) atomicMin((unsigned long long*)&c.claim[x], (unsigned long long)P);
-            x = c.parent[x];
+    const int w = walk_path(c, k, l, V, [&](int v, int side) {
+        if (side == 0) {
+            if (v < m) { const int64_t f = c.flow[v]; if (f < bk) { bk = f; qk = v; } }
+        } else {
+            if (v >= m) { const int64_t f = c.flow[v]; if (f <= bl) { bl = f; ql = v; } }
         }
-        if (dy >= dx) {
-            if (y >= m) { const int64_t f = c.flow[y]; if (f <= bl) { bl = f; ql = y; } }
-            if (P != kNoKey) atomicMin((unsigned long long*)&c.claim[y], (unsigned long long)P);
-            y = c.parent[y];
-        }
-    }
+        if (P != kNoKey) atomicMin((unsigned long long*)&c.claim[v], (unsigned long long)P);
+        return true;
+    });
+    if (w < 0) { res.ok = 0; fail_check(c.sc, 11); }
     if (bl <= bk) { res.theta = bl; res.q = ql; res.lside = 1; }
     else          { res.theta = bk; res.q = qk; res.lside = 0; }
     if (res.q < 0) res.ok = 0;
@@ -430,26 +456,19 @@ __device__ __forceinline__ CycleResult cycle_walk(const Ctx& c, int k, int l, ui
 }
 
 __device__ __forceinline__ bool cycle_owned(const Ctx& c, int k, int l, uint64_t P, int V) {
-    int x = k, y = l, steps = 0;
-    while (x != y) {
-        if (++steps > 2 * V || !FLOCK_IN(x, V) || !FLOCK_IN(y, V)) { fail_check(c.sc, 12); return false; }
-        const int dx = c.depth[x], dy = c.depth[y];
-        if (dx >= dy) { if (c.claim[x] != P) return false; x = c.parent[x]; }
-        if (dy >= dx) { if (c.claim[y] != P) return false; y = c.parent[y]; }
-    }
-    return true;
+    const int w = walk_path(c, k, l, V, [&](int v, int) { return c.claim[v] == P; });
+    if (w < 0) fail_check(c.sc, 12);
+    return w == 0;
 }
 
 __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const CycleResult& cr, int V) {
     const int m = c.I.m;
     const int64_t th = cr.theta;
-    int x = k, y = l, steps = 0;
-    while (x != y) {
-        if (++steps > 2 * V || !FLOCK_IN(x, V) || !FLOCK_IN(y, V)) { fail_check(c.sc, 13); return; }
-        const int dx = c.depth[x], dy = c.depth[y];
-        if (dx >= dy) { c.flow[x] += (x < m) ? -th : th; x = c.parent[x]; }
-        if (dy >= dx) { c.flow[y] += (y >= m) ? -th : th; y = c.parent[y]; }
-    }
+    const int w = walk_path(c, k, l, V, [&](int v, int side) {
+        c.flow[v] += (side == 0) == (v < m) ? -th : th;
+        return true;
+    });
+    if (w < 0) { fail_check(c.sc, 13); return; }
     // re-hang the subtree below the leaving edge at the entering cell
     int v = cr.lside ? l : k;
     int prev = cr.lside ? k : l;

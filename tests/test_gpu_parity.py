@@ -149,12 +149,13 @@ def test_batch_matches_plain():
 
 @pytest.mark.parametrize("form", ["persistent", "round"])
 def test_batch_forms_all_buckets(form, monkeypatch):
-    """Both batched forms on instances from every size bucket (V up to 3072)
-    plus two above it (plain path): certified optima equal to the plain
-    solver's, and the same pricing rounds in both forms."""
+    """Both batched forms on instances from every size bucket (V up to 4096,
+    the last bucket with light staging) plus one above it (plain path):
+    certified optima equal to the plain solver's, and the same pricing
+    rounds in both forms."""
     monkeypatch.setenv("FLOCK_BATCH_FORM", form)
     shapes = [(5, 7), (30, 30), (60, 60), (100, 150), (200, 300), (400, 500), (900, 1000),
-              (1500, 1500), (1000, 2072), (1600, 1600), (12, 40), (3, 3)]
+              (1500, 1444), (1000, 2072), (1600, 1600), (2000, 2000), (2100, 2000), (12, 40), (3, 3)]
     insts = [fg.generate(0, 500 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(shapes)]
     insts += fg.mixed_batch(17, 96, 10, 300)
     out = fg.batch_solve(insts)
@@ -164,3 +165,24 @@ def test_batch_forms_all_buckets(form, monkeypatch):
             p = fg.solve(inst)
             assert r.objective == p.objective, (k, inst.m, inst.n)
             assert r.iterations == p.iterations, (k, inst.m, inst.n)
+
+
+def test_batch_validation_first_failure():
+    """The batch reports the first failing instance's first failing check,
+    as validate_instance would one instance at a time."""
+    good = [fg.generate(0, 900 + k, 20 + k, 30, 1, 100, 10, 50) for k in range(8)]
+    bad_cost = fg.generate(0, 950, 25, 25, 1, 100, 10, 50)
+    bad_cost.cost = bad_cost.cost.copy()
+    bad_cost.cost[3, 7] = (1 << 30) + 1
+    bad_supply = fg.generate(0, 951, 25, 25, 1, 100, 10, 50)
+    bad_supply.supply = bad_supply.supply.copy()
+    bad_supply.supply[0] = -1
+    with pytest.raises(RuntimeError) as e1:
+        fg.batch_solve(good[:3] + [bad_cost] + good[3:5] + [bad_supply] + good[5:])
+    assert "cost out of range" in str(e1.value)
+    with pytest.raises(RuntimeError) as e2:
+        fg.batch_solve(good[:3] + [bad_supply] + good[3:5] + [bad_cost] + good[5:])
+    assert "negative supply" in str(e2.value)
+    # the runner still works after a rejected batch
+    out = fg.batch_solve(good)
+    assert all(r.status == 0 and r.certified for r in out)
