@@ -272,6 +272,7 @@ def extras(fg, insts, res, peaks) -> dict:
     gbs = sb / (ms * 1e-3) / 1e9
     out["sweep_8000"] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                          "ms": ms, "bytes": sb, "kernel": "k_sweep"}
+    out["served"] = served(fg)
     # CPU baseline: the oracle port of the reference path on all host cores
     try:
         import oracle
@@ -286,6 +287,72 @@ def extras(fg, insts, res, peaks) -> dict:
         out["cpu_baseline"]["objective_agreement"] = f"{agree}/{int((st == 0).sum())} optimal reference runs"
     except Exception as ex:  # the baseline is reported, never required
         out["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": str(ex)}
+    return out
+
+
+SERVE_POOL = 512                 # served stream: distinct instances (reused)
+SERVE_REQUESTS = 1024            # requests per offered rate
+SERVE_RATES = (0.25, 0.5, 1.0)   # offered load as fractions of batched capacity
+SERVE_PLAIN_SAMPLE = 16
+
+
+def served(fg) -> dict:
+    """Served form on an open-loop Poisson stream: m, n log-uniform in
+    [10, 2000], costs 1..1000, quantities 100..1000 (seeded).  Capacity is
+    the batched throughput on the same pool; each offered rate is a fraction
+    of it.  Latency = submit to result (server clock)."""
+    ms, ns = fg.generate_sizes(SEED + 4099, SERVE_POOL, 10, 2000)
+    pool = [fg.generate(0, SEED * 31 + k, int(ms[k]), int(ns[k]), 1, 1000, 100, 1000) for k in range(SERVE_POOL)]
+    fg.batch_solve(pool)                       # autotunes the buckets of this stream
+    t0 = time.perf_counter()
+    res = fg.batch_solve(pool)
+    cap = SERVE_POOL / (time.perf_counter() - t0)
+    if not all(r.status == 0 and r.certified for r in res):
+        raise SystemExit("served pool: non-certified batch result")
+    out = {"workload": "open-loop Poisson stream, m,n log-uniform [10,2000], costs 1..1000, quantities 100..1000, "
+                       f"pool of {SERVE_POOL} seeded instances, {SERVE_REQUESTS} requests per rate, 40 GB budget",
+           "capacity_solves_s": cap, "rates": []}
+    rng = np.random.default_rng(SEED)
+    for frac in SERVE_RATES:
+        lam = frac * cap
+        srv = fg.Server(memory_budget_bytes=40 << 30, max_inflight_batches=16, max_batch=512)
+        lat, bad = [], 0
+        t_start = time.perf_counter()
+        t_next = t_start
+        k = 0
+        while k < SERVE_REQUESTS:
+            now = time.perf_counter()
+            if now >= t_next:
+                srv.submit(pool[k % SERVE_POOL])
+                k += 1
+                t_next += rng.exponential(1.0 / lam)
+                continue
+            for (_, status, _, l_ms, st, cert) in srv.poll():
+                lat.append(l_ms)
+                bad += not (status == 0 and st == 0 and cert)
+            if t_next - time.perf_counter() > 0.0005:
+                time.sleep(0.0002)
+        srv.drain()
+        while len(lat) < SERVE_REQUESTS:
+            for (_, status, _, l_ms, st, cert) in srv.poll():
+                lat.append(l_ms)
+                bad += not (status == 0 and st == 0 and cert)
+        t_end = time.perf_counter()
+        srv.close()
+        lat.sort()
+        out["rates"].append({"offered_frac": frac, "offered_per_s": lam, "solves_s": SERVE_REQUESTS / (t_end - t_start),
+                             "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, (len(lat) * 99) // 100)],
+                             "non_certified": bad})
+    # the plain one-at-a-time GPU solver on a sample of the same stream
+    smp = pool[:SERVE_PLAIN_SAMPLE]
+    fg.solve(smp[0])
+    t0 = time.perf_counter()
+    for x in smp:
+        fg.solve(x)
+    plain = len(smp) / (time.perf_counter() - t0)
+    out["plain_solves_s"] = plain
+    out["plain_sample"] = f"first {len(smp)} instances of the pool"
+    out["served_vs_plain"] = max(r["solves_s"] for r in out["rates"]) / plain
     return out
 
 

@@ -99,6 +99,8 @@ def lib() -> ctypes.CDLL:
     L.flock_server_drain.argtypes = [ctypes.c_void_p]
     L.flock_server_destroy.argtypes = [ctypes.c_void_p]
     L.flock_default_server_config.argtypes = [P(CServerConfig)]
+    L.flock_server_request_bytes.argtypes = [i32, i32]
+    L.flock_server_request_bytes.restype = i64
     L.flock_default_options.argtypes = [P(COptions)]
     L.flock_bench_batch_rerun.argtypes = [P(ctypes.c_float), P(i32)]
     _lib = L
@@ -140,10 +142,18 @@ class Instance:
         return int(self.demand.shape[0])
 
     def c(self) -> CInstance:
+        # The C view points into the arrays; it is rebuilt whenever an array
+        # attribute was replaced (in-place edits need no rebuild).
+        key = (id(self.supply), id(self.demand), id(self.cost))
+        cached = self.__dict__.get("_c")
+        if cached is not None and cached[0] == key:
+            return cached[1]
         self.supply = _arr(self.supply)
         self.demand = _arr(self.demand)
         self.cost = _arr(self.cost).reshape(self.m, self.n)
-        return CInstance(self.m, self.n, _p(self.supply), _p(self.demand), _p(self.cost))
+        ci = CInstance(self.m, self.n, _p(self.supply), _p(self.demand), _p(self.cost))
+        self.__dict__["_c"] = ((id(self.supply), id(self.demand), id(self.cost)), ci)
+        return ci
 
 
 def generate(kind: int, seed: int, m: int, n: int, c_lo: int, c_hi: int, q_lo: int, q_hi: int) -> Instance:
@@ -300,7 +310,12 @@ def bench_batch_rerun() -> Tuple[float, int]:
 class Server:
     """Served form: continuous batching with a device-memory budget."""
 
-    def __init__(self, memory_budget_bytes: int = 40 << 30, max_inflight_batches: int = 4, max_batch: int = 512,
+    @staticmethod
+    def request_bytes(m: int, n: int) -> int:
+        """Device bytes one m x n request holds while served (its budget charge)."""
+        return int(lib().flock_server_request_bytes(m, n))
+
+    def __init__(self, memory_budget_bytes: int = 40 << 30, max_inflight_batches: int = 16, max_batch: int = 512,
                  bfs: str = "vogel", pivot: str = "parallel", verify: bool = True):
         L = lib()
         cfg = CServerConfig()

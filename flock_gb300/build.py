@@ -55,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         force = True
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "flock.h"))
-    units = [("kernels.cu", "kernels.o"), ("host.cpp", "host.o"), ("cli.cpp", "cli.o")]
+    units = [("kernels.cu", "kernels.o"), ("serve.cu", "serve.o"), ("host.cpp", "host.o"), ("cli.cpp", "cli.o")]
     jobs = []
     for src, obj in units:
         s = os.path.join(CSRC, src)
@@ -66,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
-    objs = [os.path.join(BUILD, "kernels.o"), os.path.join(BUILD, "host.o")]
+    objs = [os.path.join(BUILD, o) for o in ("kernels.o", "serve.o", "host.o")]
     if force or _stale(LIB, objs):
         tmp = LIB + ".tmp"
         _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])

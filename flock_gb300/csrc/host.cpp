@@ -1,6 +1,5 @@
-// host.cpp -- host-side parts of the C ABI: the .dat reader, the instance
-// generators and the serving loop (continuous batching with admission by a
-// device-memory budget).
+// host.cpp -- host-side parts of the C ABI: the .dat reader and the instance
+// generators.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -19,12 +18,6 @@
 
 namespace flock {
 void set_error(const std::string& s);
-struct BatchRunner;
-BatchRunner* batch_runner_new();
-void batch_runner_free(BatchRunner* r);
-int batch_runner_prepare(BatchRunner* r, int cnt, const flock_instance* insts, const flock_options* o);
-int batch_runner_solve(BatchRunner* r);
-void batch_runner_collect(BatchRunner* r, int k, flock_flow* flows, flock_stats* st);
 }  // namespace flock
 
 // ================================================================ reader ===
@@ -244,204 +237,6 @@ int flock_generate_sizes(uint64_t seed, int32_t count, int32_t lo, int32_t hi, i
         ms[k] = (int32_t)std::min<double>(hi, std::max<double>(lo, std::round(std::exp(um))));
         ns[k] = (int32_t)std::min<double>(hi, std::max<double>(lo, std::round(std::exp(un))));
     }
-    return FLOCK_OK;
-}
-
-}  // extern "C"
-
-// ================================================================ server ===
-// Requests are copied at submit.  A dispatcher thread admits waiting requests
-// (FIFO) into free launch slots while the summed resident estimate stays
-// within the budget.  Each slot has its own thread, batch runner and CUDA
-// streams, so a slot solving one group of requests overlaps on the device
-// with the other slots; requests arriving meanwhile are admitted into the
-// next slot that frees up.
-struct flock_server {
-    struct Req {
-        uint64_t ticket;
-        int32_t m, n;
-        std::vector<int32_t> s, d, c;
-        int64_t bytes;
-        std::chrono::steady_clock::time_point t_submit;
-    };
-    struct Done {
-        flock_result res;
-        std::vector<flock_flow> flows;
-    };
-    struct Slot {
-        flock::BatchRunner* runner = nullptr;
-        std::vector<Req> reqs;
-        bool busy = false;      // assigned requests, running or about to run
-        std::thread th;
-    };
-    flock_server_config cfg;
-    std::mutex mu;
-    std::condition_variable cv;        // dispatcher and slot threads wait here
-    std::condition_variable cv_done;   // drain waits here
-    std::deque<Req> pending;
-    std::deque<Done> done;
-    std::vector<Slot> slots;
-    int64_t resident = 0;
-    uint64_t next_ticket = 1;
-    int64_t submitted = 0, finished = 0;
-    bool stop = false;
-    std::thread dispatcher;
-
-    static int64_t estimate(int m, int n) {
-        const int64_t ldc = (n + 3) & ~3;
-        return 4 * (int64_t)m * ldc + 256 * (int64_t)(m + n) + 4096;
-    }
-
-    void slot_loop(int id) {
-        Slot& sl = slots[id];
-        std::unique_lock<std::mutex> lk(mu);
-        for (;;) {
-            cv.wait(lk, [&] { return stop || (sl.busy && !sl.reqs.empty()); });
-            if (!(sl.busy && !sl.reqs.empty())) { if (stop) return; continue; }
-            std::vector<Req> reqs = std::move(sl.reqs);
-            sl.reqs.clear();
-            lk.unlock();
-            std::vector<flock_instance> insts(reqs.size());
-            for (size_t k = 0; k < reqs.size(); k++)
-                insts[k] = {reqs[k].m, reqs[k].n, reqs[k].s.data(), reqs[k].d.data(), reqs[k].c.data()};
-            int rc = flock::batch_runner_prepare(sl.runner, (int)insts.size(), insts.data(), &cfg.options);
-            if (!rc) rc = flock::batch_runner_solve(sl.runner);
-            const auto now = std::chrono::steady_clock::now();
-            std::vector<Done> out(reqs.size());
-            for (size_t k = 0; k < reqs.size(); k++) {
-                Done& d = out[k];
-                memset(&d.res, 0, sizeof(d.res));
-                d.res.ticket = reqs[k].ticket;
-                if (rc) {
-                    d.res.status = rc;
-                } else {
-                    d.flows.assign((size_t)reqs[k].m + reqs[k].n - 1, flock_flow{0, 0, 0});
-                    flock::batch_runner_collect(sl.runner, (int)k, d.flows.data(), &d.res.stats);
-                    d.res.status = d.res.stats.status ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
-                }
-                d.res.latency_ms = std::chrono::duration<double, std::milli>(now - reqs[k].t_submit).count();
-                d.res.stats.ms_total = d.res.latency_ms;
-            }
-            lk.lock();
-            for (auto& r : reqs) resident -= r.bytes;
-            for (auto& d : out) done.push_back(std::move(d));
-            finished += (int64_t)reqs.size();
-            sl.busy = false;
-            cv.notify_all();
-            cv_done.notify_all();
-        }
-    }
-
-    void dispatch_loop() {
-        std::unique_lock<std::mutex> lk(mu);
-        for (;;) {
-            cv.wait(lk, [&] {
-                if (stop) return true;
-                if (pending.empty()) return false;
-                for (auto& sl : slots) if (!sl.busy) return true;
-                return false;
-            });
-            if (stop) return;
-            for (auto& sl : slots) {
-                if (sl.busy || pending.empty()) continue;
-                std::vector<Req> take;
-                while (!pending.empty() && (int)take.size() < cfg.max_batch &&
-                       resident + pending.front().bytes <= cfg.memory_budget_bytes) {
-                    resident += pending.front().bytes;
-                    take.push_back(std::move(pending.front()));
-                    pending.pop_front();
-                }
-                if (take.empty()) break;    // the budget is full: wait for a slot to retire
-                sl.reqs = std::move(take);
-                sl.busy = true;
-            }
-            cv.notify_all();
-            // nothing admitted (budget full): wait for a retirement
-            cv.wait_for(lk, std::chrono::milliseconds(1));
-        }
-    }
-};
-
-extern "C" {
-
-void flock_default_server_config(flock_server_config* cfg) {
-    if (!cfg) return;
-    cfg->memory_budget_bytes = (int64_t)40 << 30;
-    cfg->max_inflight_batches = 4;
-    cfg->max_batch = 512;
-    flock_default_options(&cfg->options);
-}
-
-int flock_server_create(const flock_server_config* cfg, flock_server** out) {
-    if (!out) return FLOCK_ERR_ARG;
-    flock_server* s = new flock_server();
-    if (cfg) s->cfg = *cfg; else flock_default_server_config(&s->cfg);
-    if (s->cfg.max_inflight_batches < 1) s->cfg.max_inflight_batches = 1;
-    if (s->cfg.max_batch < 1) s->cfg.max_batch = 1;
-    s->slots.resize(s->cfg.max_inflight_batches);
-    for (size_t k = 0; k < s->slots.size(); k++) {
-        s->slots[k].runner = flock::batch_runner_new();
-        s->slots[k].th = std::thread([s, k] { s->slot_loop((int)k); });
-    }
-    s->dispatcher = std::thread([s] { s->dispatch_loop(); });
-    *out = s;
-    return FLOCK_OK;
-}
-
-int flock_server_submit(flock_server* s, const flock_instance* inst, uint64_t* ticket) {
-    if (!s || !inst || !inst->supply || !inst->demand || !inst->cost || inst->m < 1 || inst->n < 1) return FLOCK_ERR_ARG;
-    flock_server::Req r;
-    r.m = inst->m; r.n = inst->n;
-    r.s.assign(inst->supply, inst->supply + inst->m);
-    r.d.assign(inst->demand, inst->demand + inst->n);
-    r.c.assign(inst->cost, inst->cost + (size_t)inst->m * inst->n);
-    r.bytes = flock_server::estimate(inst->m, inst->n);
-    if (r.bytes > s->cfg.memory_budget_bytes) { flock::set_error("request exceeds the memory budget"); return FLOCK_ERR_BUDGET; }
-    r.t_submit = std::chrono::steady_clock::now();
-    std::lock_guard<std::mutex> lk(s->mu);
-    r.ticket = s->next_ticket++;
-    if (ticket) *ticket = r.ticket;
-    s->pending.push_back(std::move(r));
-    s->submitted++;
-    s->cv.notify_all();
-    return FLOCK_OK;
-}
-
-int flock_server_poll(flock_server* s, flock_result* results, flock_flow** flows_out, int32_t max, int32_t* count) {
-    if (!s || !count || (max > 0 && !results)) return FLOCK_ERR_ARG;
-    std::lock_guard<std::mutex> lk(s->mu);
-    int k = 0;
-    while (k < max && !s->done.empty()) {
-        flock_server::Done& d = s->done.front();
-        results[k] = d.res;
-        if (flows_out && flows_out[k] && !d.flows.empty())
-            memcpy(flows_out[k], d.flows.data(), d.flows.size() * sizeof(flock_flow));
-        s->done.pop_front();
-        k++;
-    }
-    *count = k;
-    return FLOCK_OK;
-}
-
-int flock_server_drain(flock_server* s) {
-    if (!s) return FLOCK_ERR_ARG;
-    std::unique_lock<std::mutex> lk(s->mu);
-    s->cv_done.wait(lk, [s] { return s->finished >= s->submitted; });
-    return FLOCK_OK;
-}
-
-int flock_server_destroy(flock_server* s) {
-    if (!s) return FLOCK_ERR_ARG;
-    flock_server_drain(s);
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->stop = true;
-        s->cv.notify_all();
-    }
-    if (s->dispatcher.joinable()) s->dispatcher.join();
-    for (auto& sl : s->slots) if (sl.th.joinable()) sl.th.join();
-    for (auto& sl : s->slots) flock::batch_runner_free(sl.runner);
-    delete s;
     return FLOCK_OK;
 }
 

@@ -8,13 +8,17 @@
 
 namespace flock {
 
+// One instance of a batched or served launch, by absolute device pointers.
 struct BatchDesc {
     int32_t m, n, ldc, index;   // index: position in the caller's instance list
-    int64_t cost_off;           // into the cost arena (elements)
-    int64_t sd_off;             // supply at sd_off, demand at sd_off + m
-    int64_t out_off;            // first basis cell in the output arena
-    int64_t pot_off;            // first dual in the dual arena
-    int64_t ws_off;             // the instance's working set in the state arena (bytes)
+    const int32_t* cost;        // m x ldc, 16-byte aligned
+    const int32_t* sd;          // supplies (m) then demands (n)
+    uint8_t* ws;                // working set (carve_ctx layout), 256-byte aligned
+    int32_t* out;               // basis: src[V-1], dst[V-1], qty[V-1]
+    int32_t* bfs;               // initial allocation list: 3 ints per cell, V-1 cells
+    int64_t* pot;               // duals, V
+    Scalars* sc;
+    int32_t* done;              // optional completion flag in host-mapped memory
 };
 
 struct BatchArgs {
@@ -22,17 +26,13 @@ struct BatchArgs {
     int32_t count;
     int32_t* next;              // work-stealing counter of this launch (zeroed before it)
     int32_t* active;            // round kernel: instances still running after the round
-    const int32_t* cost;
-    const int32_t* sd;
-    int32_t* out_src; int32_t* out_dst; int32_t* out_qty;
-    int32_t* bfs_out;           // 3 ints per cell: Vogel / NW-corner allocation list
-    int64_t* pot_out;
-    Scalars* sc;
-    uint8_t* ws;                // per-instance working sets
     int32_t maxV, maxM;         // largest instance of the launch (shared-memory staging size)
     int32_t bfs_method, mode, max_rounds;
     int32_t light;              // 1: stage only the per-step tree arrays (largest bucket)
 };
+
+// A served request's device region: byte offsets of its arrays (256-aligned).
+struct ServeLayout { size_t cost, sd, ws, out, bfs, pot, sc, total; };
 
 struct Carver {
     uint8_t* g; size_t go;

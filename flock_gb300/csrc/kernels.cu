@@ -199,17 +199,18 @@ __global__ void k_fill_bench(int32_t* cost, size_t cells, int64_t* pot, int V) {
 //   k_bfinal  original flows, objective and the exact certificate
 __device__ __forceinline__ bool batch_desc_ok(const BatchArgs& a, const BatchDesc& d) {
     return d.m >= 1 && d.n >= 1 && d.m + d.n <= a.maxV && d.m <= a.maxM && d.ldc >= d.n && !(d.ldc & 3) &&
-           !(d.cost_off & 3) && !(d.ws_off & 255);
+           !((uintptr_t)d.cost & 15) && !((uintptr_t)d.ws & 255) && d.sd && d.out && d.bfs && d.pot && d.sc;
 }
 
 __device__ __forceinline__ void batch_ctx(const BatchArgs& a, const BatchDesc& d, Ctx& g) {
+    const int V1 = d.m + d.n - 1;
     g.I.m = d.m; g.I.n = d.n; g.I.ldc = d.ldc;
-    g.I.cost = a.cost + d.cost_off;
-    g.I.supply = a.sd + d.sd_off;
-    g.I.demand = a.sd + d.sd_off + d.m;
-    g.sc = a.sc + d.index;
-    g.out_src = a.out_src + d.out_off; g.out_dst = a.out_dst + d.out_off; g.out_qty = a.out_qty + d.out_off;
-    carve_ctx(g, a.ws + d.ws_off, d.m + d.n, d.m, nullptr, a.pot_out + d.pot_off);
+    g.I.cost = d.cost;
+    g.I.supply = d.sd;
+    g.I.demand = d.sd + d.m;
+    g.sc = d.sc;
+    g.out_src = d.out; g.out_dst = d.out + V1; g.out_qty = d.out + 2 * V1;
+    carve_ctx(g, d.ws, d.m + d.n, d.m, nullptr, d.pot);
 }
 
 // returns the next instance of this launch for the CTA, or -1
@@ -243,9 +244,9 @@ __device__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch&
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
     const int V = d.m + d.n;
     for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
-        a.bfs_out[3 * (d.out_off + k) + 0] = c.bfs_src[k];
-        a.bfs_out[3 * (d.out_off + k) + 1] = c.bfs_dst[k];
-        a.bfs_out[3 * (d.out_off + k) + 2] = c.bfs_qty[k];
+        d.bfs[3 * k + 0] = c.bfs_src[k];
+        d.bfs[3 * k + 1] = c.bfs_dst[k];
+        d.bfs[3 * k + 2] = c.bfs_qty[k];
     }
     __syncthreads();
     sf_init_cta(c, bs);
@@ -253,7 +254,7 @@ __device__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch&
 }
 
 __device__ __forceinline__ void bdesc_reject(const BatchArgs& a, const BatchDesc& d) {
-    if (threadIdx.x == 0) { a.sc[d.index].status = ST_TREE_CORRUPT; a.sc[d.index].fail_site = 1; a.sc[d.index].done = 1; }
+    if (threadIdx.x == 0 && d.sc) { d.sc->status = ST_TREE_CORRUPT; d.sc->fail_site = 1; d.sc->done = 1; }
 }
 
 __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
@@ -336,7 +337,7 @@ __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch
 }
 
 __device__ void bfinal_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs) {
-    if (a.sc[d.index].status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) return;   // uniform
+    if (d.sc->status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) return;   // uniform
     Ctx c;
     batch_ctx(a, d, c);
     finalize_cta(c, bs);
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
     for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) continue;
-        if (a.sc[d.index].done) continue;          // every thread reads the same value
+        if (d.sc->done) continue;          // every thread reads the same value
         brounds_one(a, d, bs, smem, 1);
     }
 }
@@ -367,6 +368,16 @@ __global__ void __launch_bounds__(256) k_bfinal(BatchArgs a) {
     }
 }
 
+// Served form: after the instance's results are in device memory, raise its
+// completion flag in host-mapped memory (the host polls it, then copies).
+__device__ __forceinline__ void publish_done(const BatchDesc& d) {
+    __syncthreads();
+    if (threadIdx.x == 0 && d.done) {
+        __threadfence_system();
+        *(volatile int32_t*)d.done = 1;
+    }
+}
+
 // Persistent form: a CTA takes the next instance of the bucket (largest
 // first) and runs it from the initial solution to the certificate, all
 // pricing rounds inside with the tree resident in shared memory.
@@ -377,10 +388,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
-        if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); continue; }
+        if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); publish_done(d); continue; }
         bsetup_one(a, d, bs);
-        if (!a.sc[d.index].done) brounds_one(a, d, bs, smem, 1 << 30);
+        if (!d.sc->done) brounds_one(a, d, bs, smem, 1 << 30);
         bfinal_one(a, d, bs);
+        publish_done(d);
     }
 }
 
@@ -841,7 +853,9 @@ struct BatchRunner {
     // per call
     int count = 0;
     std::vector<int> V_of, m_of, n_of, plain_list;
-    std::vector<int64_t> out_off, pot_off;
+    std::vector<int64_t> out_off, pot_off;   // basis cells / duals before instance k
+    std::vector<int64_t> cost_off, sd_off, ws_off;
+    std::vector<int> order_;                // staged instances, grouped by bucket
     int64_t total_cells = 0, total_pot = 0, total_cost = 0, total_sd = 0, total_ws = 0;
     std::vector<BatchDesc> descs;           // grouped by bucket
     int bstart[kNumBuckets + 1] = {};
@@ -879,7 +893,7 @@ struct BatchRunner {
         out_off.assign(cnt, 0); pot_off.assign(cnt, 0);
         plain_list.clear();
         total_cells = total_pot = total_cost = total_sd = total_ws = 0;
-        std::vector<int64_t> cost_off(cnt), sd_off(cnt), ws_off(cnt);
+        cost_off.assign(cnt, 0); sd_off.assign(cnt, 0); ws_off.assign(cnt, 0);
         // Validation in the order validate_instance uses, the O(m n) cost
         // range check fused into the copy below (threads over instances);
         // the first failing instance reports its first failing check.
@@ -927,16 +941,12 @@ struct BatchRunner {
             if (ba != bb) return ba < bb;
             return (int64_t)m_of[a] * n_of[a] > (int64_t)m_of[b] * n_of[b];
         });
+        order_ = order;
         descs.resize(order.size());
         for (int b = 0; b <= kNumBuckets; b++) bstart[b] = 0;
         for (int b = 0; b < kNumBuckets; b++) { bmaxV[b] = 0; bmaxM[b] = 0; }
         for (size_t q = 0; q < order.size(); q++) {
             const int k = order[q];
-            BatchDesc d;
-            d.m = m_of[k]; d.n = n_of[k]; d.ldc = (n_of[k] + 3) & ~3; d.index = k;
-            d.cost_off = cost_off[k]; d.sd_off = sd_off[k]; d.out_off = out_off[k]; d.pot_off = pot_off[k];
-            d.ws_off = ws_off[k];
-            descs[q] = d;
             const int b = bucket_of(V_of[k]);
             bstart[b + 1]++;
             bmaxV[b] = std::max(bmaxV[b], V_of[k]);
@@ -958,6 +968,19 @@ struct BatchRunner {
         FLOCK_CK(h_desc.ensure(std::max<size_t>(1, descs.size()) * sizeof(BatchDesc)));
         FLOCK_CK(h_out.ensure((size_t)total_cells * 12 + 16));
         FLOCK_CK(h_sc.ensure((size_t)count * sizeof(Scalars)));
+        for (size_t q = 0; q < order_.size(); q++) {
+            const int k = order_[q];
+            BatchDesc& d = descs[q];
+            d.m = m_of[k]; d.n = n_of[k]; d.ldc = (n_of[k] + 3) & ~3; d.index = k;
+            d.cost = d_cost.as<int32_t>() + cost_off[k];
+            d.sd = d_sd.as<int32_t>() + sd_off[k];
+            d.ws = d_ws.as<uint8_t>() + ws_off[k];
+            d.out = d_out.as<int32_t>() + 3 * out_off[k];
+            d.bfs = d_bfs.as<int32_t>() + 3 * out_off[k];
+            d.pot = d_pot.as<int64_t>() + pot_off[k];
+            d.sc = d_sc.as<Scalars>() + k;
+            d.done = nullptr;
+        }
         if (!descs.empty()) memcpy(h_desc.p, descs.data(), descs.size() * sizeof(BatchDesc));
         return FLOCK_OK;
     }
@@ -980,15 +1003,6 @@ struct BatchRunner {
         a.desc = d_desc.as<BatchDesc>() + bstart[b];
         a.count = bstart[b + 1] - bstart[b];
         a.next = nullptr; a.active = nullptr;
-        a.cost = d_cost.as<int32_t>();
-        a.sd = d_sd.as<int32_t>();
-        a.out_src = d_out.as<int32_t>();
-        a.out_dst = d_out.as<int32_t>() + total_cells;
-        a.out_qty = d_out.as<int32_t>() + 2 * total_cells;
-        a.bfs_out = d_bfs.as<int32_t>();
-        a.pot_out = d_pot.as<int64_t>();
-        a.sc = d_sc.as<Scalars>();
-        a.ws = d_ws.as<uint8_t>();
         a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
         a.light = bucket_light(b) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
@@ -1156,9 +1170,9 @@ struct BatchRunner {
         }
         const Scalars& S = h_sc.as<Scalars>()[k];
         const int V = V_of[k];
-        const int32_t* src = h_out.as<int32_t>() + out_off[k];
-        const int32_t* dst = src + total_cells;
-        const int32_t* qty = src + 2 * total_cells;
+        const int32_t* src = h_out.as<int32_t>() + 3 * out_off[k];
+        const int32_t* dst = src + (V - 1);
+        const int32_t* qty = src + 2 * (V - 1);
         const bool broken = S.status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE);
         if (flows && !broken) fill_flows_from_basis(V, src, dst, qty, flows);
         if (st_out) {
@@ -1217,8 +1231,15 @@ struct BatchRunner {
                 for (int x = 0; x < kNumBuckets; x++) cfg[x] = t;
                 float ms = 0;
                 if ((rc = run_device(cfg, &ms, b))) return rc;
+                if (getenv("FLOCK_TUNE_LOG"))
+                    fprintf(stderr, "  bucket %d candidate %s threads=%d grid_mult=%d chunk=%d: %.3f ms\n", b,
+                            t.persistent ? "persistent" : "rounds", t.threads, t.grid_mult, t.chunk, ms);
                 if (ms < best_ms) { best_ms = ms; best = t; }
             }
+            if (getenv("FLOCK_TUNE_LOG"))
+                fprintf(stderr, "flock autotune: bucket %d (%d instances, V <= %d): %s threads=%d grid_mult=%d chunk=%d  %.3f ms\n",
+                        b, nb, bmaxV[b], best.persistent ? "persistent" : "rounds", best.threads, best.grid_mult,
+                        best.chunk, best_ms);
             std::lock_guard<std::mutex> lk(g_tune_mu);
             g_tuned[b] = best;
             g_tuned_ok[b] = true;
@@ -1227,12 +1248,75 @@ struct BatchRunner {
     }
 };
 
-BatchRunner* batch_runner_new() { return new BatchRunner(); }
-void batch_runner_free(BatchRunner* r) { delete r; }
-int batch_runner_prepare(BatchRunner* r, int cnt, const flock_instance* insts, const flock_options* o) { return r->prepare(cnt, insts, o); }
-int batch_runner_solve(BatchRunner* r) { return r->solve_all(); }
-void batch_runner_collect(BatchRunner* r, int k, flock_flow* flows, flock_stats* st) { r->collect(k, flows, st); }
-int batch_runner_count(BatchRunner* r) { return r->count; }
+// ------------------------------------------------------------ served form ---
+// Helpers for the served form (serve.cu): a request's device region, the
+// launch of one admission group, and its result.
+ServeLayout serve_layout(int m, int n) {
+    const int V = m + n, ldc = (n + 3) & ~3;
+    ServeLayout L;
+    size_t o = 0;
+    L.cost = o; o = al256(o + (size_t)m * ldc * 4);
+    L.sd = o;   o = al256(o + (size_t)V * 4);
+    L.ws = o;   o = al256(o + instance_ws_bytes(V, m));
+    L.out = o;  o = al256(o + (size_t)3 * (V - 1) * 4);
+    L.bfs = o;  o = al256(o + (size_t)3 * (V - 1) * 4);
+    L.pot = o;  o = al256(o + (size_t)V * 8);
+    L.sc = o;   o = al256(o + sizeof(Scalars));
+    L.total = o;
+    return L;
+}
+
+int serve_init() {
+    for (int t : {256, 512, 1024})
+        FLOCK_CK(cudaFuncSetAttribute(bsolve_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
+    return FLOCK_OK;
+}
+
+// Block size of a served launch by its largest instance (latency first:
+// larger instances get more threads).
+static int serve_threads(int maxV) {
+    return maxV <= 128 ? 64 : maxV <= 512 ? 128 : maxV <= 1024 ? 256 : maxV <= 2944 ? 512 : 1024;
+}
+
+int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const flock_options& opt, int32_t* d_next,
+                 cudaStream_t s) {
+    if (count < 1 || maxV > kMaxStagedV) return FLOCK_ERR_ARG;
+    BatchArgs a;
+    a.desc = d_desc;
+    a.count = count;
+    a.next = d_next;
+    a.active = nullptr;
+    a.maxV = maxV; a.maxM = maxM;
+    a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
+    a.mode = opt.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : 1;
+    a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
+    a.light = maxV > kBucketEdges[kNumBuckets - 2] ? 1 : 0;
+    const size_t smem = staged_bytes(maxV, maxM, a.light != 0);
+    const int threads = serve_threads(maxV);
+    const void* fn = bsolve_fn(threads);
+    int per_sm = 0;
+    FLOCK_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    const int grid = std::max(1, std::min(count, std::max(1, per_sm) * num_sms()));
+    void* kargs[] = {&a};
+    FLOCK_CK(cudaLaunchKernel(fn, dim3(grid), dim3(threads), kargs, smem, s));
+    return FLOCK_OK;
+}
+
+void serve_collect(const Scalars& S, int V, const int32_t* out3, flock_flow* flows, flock_stats* st) {
+    const bool broken = S.status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE);
+    if (flows && !broken) fill_flows_from_basis(V, out3, out3 + (V - 1), out3 + 2 * (V - 1), flows);
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->notes = (S.status & ~kFailMask) | (S.fail_site << 8);
+        st->objective = S.objective;
+        st->iterations = S.rounds;
+        st->pivots = S.pivots;
+        st->active_flows = broken ? 0 : S.active;
+        st->status = (S.status & kFailMask) | (S.cert ? ST_CERT_FAIL : 0);
+        st->certified = (!broken && S.cert == 0) ? 1 : 0;
+        st->vogel_events = S.events;
+    }
+}
 
 static std::mutex g_batch_mu;
 static BatchRunner* g_batch = nullptr;

@@ -159,12 +159,16 @@ int flock_solve(const flock_instance* inst, const flock_options* opt, flock_flow
 int flock_batch_solve(int32_t count, const flock_instance* insts, const flock_options* opt,
                       flock_flow* flows, const int64_t* flow_offset, flock_stats* stats);
 
-/* Served form: continuous batching with admission by a device-memory budget. */
+/* Served form: continuous batching with admission by a device-memory budget.
+ * Requests are admitted in arrival order while their resident device state
+ * fits the budget; each admitted group is launched at once and overlaps with
+ * earlier launches; every instance retires (and frees its state) as soon as
+ * it is solved.  Instances with m + n > 4096 run on the plain solver. */
 typedef struct flock_server flock_server;
 typedef struct {
     int64_t memory_budget_bytes;   /* resident device state allowed (default 40 GiB) */
-    int32_t max_inflight_batches;  /* concurrent launches (streams), default 4 */
-    int32_t max_batch;             /* instances per launch, default 512 */
+    int32_t max_inflight_batches;  /* launch streams (at least 16 are used), default 16 */
+    int32_t max_batch;             /* instances admitted per launch group, default 512 */
     flock_options options;
 } flock_server_config;
 typedef struct {
@@ -176,6 +180,9 @@ typedef struct {
 
 void flock_default_server_config(flock_server_config* cfg);
 int flock_server_create(const flock_server_config* cfg, flock_server** out);
+/* Device bytes one m x n request holds while it is in the served form (its
+ * budget charge); -1 for m or n < 1. */
+int64_t flock_server_request_bytes(int32_t m, int32_t n);
 /* Copies the instance; the result's flows are returned by flock_server_poll. */
 int flock_server_submit(flock_server* s, const flock_instance* inst, uint64_t* ticket);
 /* Returns up to `max` finished results; flows of result k go to flows_out[k]

@@ -38,7 +38,7 @@ def test_served_results_equal_alone():
 def test_served_budget_serialises():
     """A budget that fits one request at a time still completes everything."""
     insts = fg.mixed_batch(5, 12, 20, 60)
-    big = max(4 * x.m * ((x.n + 3) // 4 * 4) + 256 * (x.m + x.n) + 4096 for x in insts)
+    big = max(fg.Server.request_bytes(x.m, x.n) for x in insts)
     srv = fg.Server(memory_budget_bytes=big, max_inflight_batches=2, max_batch=8)
     for x in insts:
         srv.submit(x)
@@ -47,3 +47,41 @@ def test_served_budget_serialises():
     srv.close()
     assert len(res) == len(insts)
     assert all(r[1] == 0 and r[5] for r in res)
+
+
+def test_served_backfill_no_head_of_line_blocking():
+    """A large instance is on the GPU; small requests that arrive after it are
+    admitted, overlap with it and retire before it does."""
+    big = fg.generate(0, 77, 1800, 1900, 1, 1000, 100, 1000)
+    small = [fg.generate(0, 78 + k, 20 + k, 25, 1, 1000, 100, 1000) for k in range(24)]
+    srv = fg.Server()
+    t_big = srv.submit(big)
+    time.sleep(0.02)
+    t_small = [srv.submit(x) for x in small]
+    order = []
+    res = {}
+    while len(order) < 1 + len(small):
+        for r in srv.poll():
+            order.append(r[0])
+            res[r[0]] = r
+        time.sleep(0.001)
+    srv.close()
+    assert all(res[t][1] == 0 and res[t][5] for t in order)
+    assert order[-1] == t_big, "small requests waited behind the large one"
+    assert max(res[t][3] for t in t_small) < res[t_big][3]
+    assert res[t_big][2] == fg.solve(big).objective
+
+
+def test_served_plain_path_request():
+    """m + n above the staged limit: solved by the plain solver inside the server."""
+    inst = fg.generate(0, 79, 2100, 2050, 1, 1000, 100, 1000)
+    small = fg.generate(0, 80, 30, 40, 1, 1000, 100, 1000)
+    srv = fg.Server()
+    srv.submit(inst)
+    srv.submit(small)
+    srv.drain()
+    res = srv.poll()
+    srv.close()
+    assert len(res) == 2 and all(r[1] == 0 and r[5] for r in res)
+    objs = sorted(r[2] for r in res)
+    assert objs == sorted([fg.solve(inst).objective, fg.solve(small).objective])
