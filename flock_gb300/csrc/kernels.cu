@@ -269,50 +269,50 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
 
 // Shared-memory staging of the arrays every pivot step touches.  Light
 // staging (the largest bucket) keeps the pointer-jumping buffers and the
-// edge claims in the instance's global working set.
-__host__ __device__ inline size_t stage_layout(Ctx* c, unsigned char* smem, int V, int M, bool light) {
-    Carver k{nullptr, 0, smem ? smem : (unsigned char*)16, 0};
-    int32_t* parent = (int32_t*)k.S(4 * (size_t)V);
-    int32_t* depth = (int32_t*)k.S(4 * (size_t)V);
-    int64_t* flow = (int64_t*)k.S(8 * (size_t)V);
-    uint64_t* row_best = (uint64_t*)k.S(8 * (size_t)M);
-    int64_t* pot = (int64_t*)k.S(8 * (size_t)V);
-    int32_t* v32 = (int32_t*)k.S(4 * (size_t)V);
-    if (c) {
-        c->parent = parent; c->depth = depth; c->flow = flow; c->row_best = row_best; c->pot = pot; c->v32 = v32;
+// edge claims in the instance's global working set.  Every pointer is carved
+// from the extern shared base and kLight is a compile-time constant, so the
+// compiler knows they address shared memory (shared loads and atomics rather
+// than generic ones).  staged_bytes() below must follow the same order.
+template <bool kLight>
+__device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
+    Carver k{nullptr, 0, smem, 0};
+    c.parent = (int32_t*)k.S(4 * (size_t)V);
+    c.depth = (int32_t*)k.S(4 * (size_t)V);
+    c.flow = (int64_t*)k.S(8 * (size_t)V);
+    c.row_best = (uint64_t*)k.S(8 * (size_t)M);
+    c.pot = (int64_t*)k.S(8 * (size_t)V);
+    c.v32 = (int32_t*)k.S(4 * (size_t)V);
+    if (!kLight) {
+        c.claim = (uint64_t*)k.S(8 * (size_t)V);
+        c.anc0 = (int32_t*)k.S(4 * (size_t)V);
+        c.anc1 = (int32_t*)k.S(4 * (size_t)V);
+        c.len0 = (int32_t*)k.S(4 * (size_t)V);
+        c.len1 = (int32_t*)k.S(4 * (size_t)V);
+        c.acc0 = (int64_t*)k.S(8 * (size_t)V);
+        c.acc1 = (int64_t*)k.S(8 * (size_t)V);
     }
+}
+
+inline size_t staged_bytes(int V, int M, bool light) {
+    Carver k{nullptr, 0, (unsigned char*)16, 0};
+    k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
+    k.S(4 * (size_t)V);
     if (!light) {
-        uint64_t* claim = (uint64_t*)k.S(8 * (size_t)V);
-        int32_t* anc0 = (int32_t*)k.S(4 * (size_t)V);
-        int32_t* anc1 = (int32_t*)k.S(4 * (size_t)V);
-        int32_t* len0 = (int32_t*)k.S(4 * (size_t)V);
-        int32_t* len1 = (int32_t*)k.S(4 * (size_t)V);
-        int64_t* acc0 = (int64_t*)k.S(8 * (size_t)V);
-        int64_t* acc1 = (int64_t*)k.S(8 * (size_t)V);
-        if (c) {
-            c->claim = claim; c->anc0 = anc0; c->anc1 = anc1; c->len0 = len0; c->len1 = len1;
-            c->acc0 = acc0; c->acc1 = acc1;
-        }
+        k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V);
+        k.S(8 * (size_t)V); k.S(8 * (size_t)V);
     }
     return (k.so + 15) & ~size_t(15);
 }
 
-__device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M, bool light) {
-    stage_layout(&c, smem, V, M, light);
-}
-
-__host__ __device__ inline size_t staged_bytes(int V, int M, bool light) {
-    return stage_layout(nullptr, nullptr, V, M, light);
-}
-
 // Pricing rounds of one instance with its tree staged in shared memory:
 // `max_here` rounds at most (1 for the round-kernel form), or until done.
+template <bool kLight>
 __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs, unsigned char* smem,
                             int max_here) {
     Ctx g;
     batch_ctx(a, d, g);
     Ctx c = g;
-    stage_hot(c, smem, a.maxV, a.maxM, a.light != 0);
+    stage_hot<kLight>(c, smem, a.maxV, a.maxM);
     const int V = d.m + d.n;
     for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
     __syncthreads();
@@ -354,7 +354,8 @@ __global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) continue;
         if (d.sc->done) continue;          // every thread reads the same value
-        brounds_one(a, d, bs, smem, 1);
+        if (a.light) brounds_one<true>(a, d, bs, smem, 1);
+        else brounds_one<false>(a, d, bs, smem, 1);
     }
 }
 
@@ -390,7 +391,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); publish_done(d); continue; }
         bsetup_one(a, d, bs);
-        if (!d.sc->done) brounds_one(a, d, bs, smem, 1 << 30);
+        if (!d.sc->done) {
+            if (a.light) brounds_one<true>(a, d, bs, smem, 1 << 30);
+            else brounds_one<false>(a, d, bs, smem, 1 << 30);
+        }
         bfinal_one(a, d, bs);
         publish_done(d);
     }
