@@ -59,7 +59,7 @@ ST_ITER_CAP, ST_TREE_CORRUPT, ST_SF_FAIL, ST_CERT_FAIL, ST_RANGE = 1, 2, 4, 32, 
 NOTE_VOGEL_UNDEF, NOTE_START_REPAIRED = 8, 16
 
 BFS = {"nwc": 0, "nwc_host": 0, "vogel": 1, "vam_host": 1}
-PIVOT = {"sequential": 0, "parallel_uv": 0, "parallel": 1, "parallel_ss": 1, "switch_hybrid": 1}
+PIVOT = {"sequential": 0, "parallel_uv": 0, "parallel": 1, "parallel_ss": 1, "switch": 2, "switch_hybrid": 2}
 
 
 class FlockError(RuntimeError):
@@ -249,7 +249,7 @@ def _result(st: CStats, flows: np.ndarray, u=None, v=None) -> Result:
                   float(st.ms_bfs), float(st.ms_simplex), u, v)
 
 
-def solve(inst: Instance, bfs: str = "vogel", pivot: str = "parallel", max_iterations: int = 0,
+def solve(inst: Instance, bfs: str = "vogel", pivot: str = "switch", max_iterations: int = 0,
           verify: bool = True, duals: bool = True, raise_on_error: bool = True) -> Result:
     ci = inst.c()
     opt = _options(bfs, pivot, max_iterations, verify)
@@ -277,7 +277,7 @@ def vogel(inst: Instance) -> Tuple[np.ndarray, int]:
     return flows, int(ev.value)
 
 
-def batch_solve(insts: Sequence[Instance], bfs: str = "vogel", pivot: str = "parallel",
+def batch_solve(insts: Sequence[Instance], bfs: str = "vogel", pivot: str = "switch",
                 max_iterations: int = 0, verify: bool = True) -> List[Result]:
     k = len(insts)
     arr = (CInstance * k)(*[x.c() for x in insts])
@@ -316,7 +316,7 @@ class Server:
         return int(lib().flock_server_request_bytes(m, n))
 
     def __init__(self, memory_budget_bytes: int = 40 << 30, max_inflight_batches: int = 16, max_batch: int = 512,
-                 bfs: str = "vogel", pivot: str = "parallel", verify: bool = True):
+                 bfs: str = "vogel", pivot: str = "switch", verify: bool = True):
         L = lib()
         cfg = CServerConfig()
         L.flock_default_server_config(ctypes.byref(cfg))
@@ -448,5 +448,6 @@ class ssModel_parallel(_Model):
 
 
 class switchModel_parallel(_Model):
-    """-a switch_hybrid (runs the parallel form; see include/flock/algos.h)."""
-    _pivot = "parallel"
+    """-a switch_hybrid: parallel rounds until one applies fewer than 10
+    pivots, then sequential ones (switch/switch_model_parallel.cu:182-184)."""
+    _pivot = "switch"

@@ -51,7 +51,7 @@ struct Scalars {
     int32_t active;        // nonzero flows in the result
     int32_t cert;          // certificate failure bits (0: optimal)
     int32_t max_rounds;
-    int32_t mode;          // 0 sequential (one pivot / round), 1 parallel multi-pivot
+    int32_t mode;          // 0 sequential (one pivot / round), 1 parallel multi-pivot, 2 switch (parallel, then 0)
     int32_t ncand;         // candidates in the last round
     int64_t objective;
     int64_t M;             // perturbation scale

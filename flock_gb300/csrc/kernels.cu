@@ -518,6 +518,11 @@ int validate_instance(const flock_instance* I) {
     return FLOCK_OK;
 }
 
+// Scalars::mode of a pivot method: 0 sequential, 1 parallel, 2 switch.
+static int pivot_mode(const flock_options& o) {
+    return o.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : o.pivot_method == FLOCK_PIVOT_PARALLEL ? 1 : 2;
+}
+
 static int threads_for(int V) {
     int t = ((V + 31) / 32) * 32;
     return std::max(128, std::min(1024, t));
@@ -609,7 +614,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     Ctx c;
     int32_t* out3 = nullptr;
     if ((rc = P.prepare(I, c, &out3))) return rc;
-    if ((rc = P.reset_scalars(c.sc, opt.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : 1, max_rounds))) return rc;
+    if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds))) return rc;
     const int nt = threads_for(V);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     k_setup<<<1, nt, 0, P.stream>>>(c, opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL);
@@ -1010,7 +1015,7 @@ struct BatchRunner {
         a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
         a.light = bucket_light(b) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
-        a.mode = opt.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : 1;
+        a.mode = pivot_mode(opt);
         a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
         return a;
     }
@@ -1292,7 +1297,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.active = nullptr;
     a.maxV = maxV; a.maxM = maxM;
     a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
-    a.mode = opt.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : 1;
+    a.mode = pivot_mode(opt);
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
     a.light = maxV > kBucketEdges[kNumBuckets - 2] ? 1 : 0;
     const size_t smem = staged_bytes(maxV, maxM, a.light != 0);
@@ -1372,7 +1377,7 @@ extern "C" {
 void flock_default_options(flock_options* opt) {
     if (!opt) return;
     opt->bfs_method = FLOCK_BFS_VOGEL;
-    opt->pivot_method = FLOCK_PIVOT_PARALLEL;
+    opt->pivot_method = FLOCK_PIVOT_SWITCH;
     opt->max_iterations = 0;
     opt->verify = 1;
 }

@@ -487,6 +487,9 @@ __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const Cy
 
 // Parallel mode: candidates walked per round (the rest wait for later rounds).
 constexpr int kMaxCand = 32;
+// Switch mode: a parallel round applying fewer pivots than this switches the
+// instance to sequential rounds (switch/switch_model_parallel.cu:182-184).
+constexpr int kSwitchPivots = 10;
 
 // One pricing round after sweep: choose candidates, claim, apply.
 __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
@@ -552,14 +555,18 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         __syncthreads();
         return;
     }
-    for (int v = threadIdx.x; v < V; v += blockDim.x) c.claim[v] = kNoKey;
-    __syncthreads();
+    // A single candidate always wins: no claims, no ownership pass.
+    const bool single = ncand == 1;
+    if (!single) {
+        for (int v = threadIdx.x; v < V; v += blockDim.x) c.claim[v] = kNoKey;
+        __syncthreads();
+    }
     int bad = 0;
     for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
         const int i = c.cand[t];
         const uint64_t key = c.row_best[i];
         const int l = m + (int)key_idx(key);
-        const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
+        const uint64_t P = single ? kNoKey : pack_i32(key_val(key), (uint32_t)i);
         const CycleResult cr = cycle_walk(c, i, l, P, V);
         c.cand_theta[t] = cr.theta;
         c.cand_q[t] = cr.q;
@@ -570,6 +577,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     int wins = 0;
     for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
         if (c.cand_info[t] & 4) continue;
+        if (single) { c.cand_info[t] |= 2; wins++; continue; }
         const int i = c.cand[t];
         const uint64_t key = c.row_best[i];
         const int l = m + (int)key_idx(key);
@@ -592,6 +600,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         c.sc->ncand = ncand;
         c.sc->last_winners = (int32_t)w;
         if (any_bad || w == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+        if (mode == 2 && w < kSwitchPivots) c.sc->mode = 0;
     }
     __syncthreads();
 }

@@ -66,11 +66,14 @@ typedef struct {
 } flock_flow;
 
 enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1 };            /* BFS_METHOD nwc_host / vam_host */
-enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1 }; /* -a parallel_uv / parallel_ss  */
+/* -a parallel_uv / parallel_ss / switch_hybrid.  SWITCH runs parallel rounds
+ * until one applies fewer than 10 pivots, then sequential ones
+ * (switch/switch_model_parallel.cu:182-184). */
+enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2 };
 
 typedef struct {
     int32_t bfs_method;      /* FLOCK_BFS_VOGEL (default) or FLOCK_BFS_NWC */
-    int32_t pivot_method;    /* FLOCK_PIVOT_PARALLEL (default) or FLOCK_PIVOT_SEQUENTIAL */
+    int32_t pivot_method;    /* FLOCK_PIVOT_SWITCH (default), _PARALLEL or _SEQUENTIAL */
     int32_t max_iterations;  /* cap on pricing rounds; <= 0: 1 << 30 */
     int32_t verify;          /* nonzero: run the exact certificate check (default on) */
 } flock_options;

@@ -148,10 +148,9 @@ class ssModel_parallel : public flock_detail::ModelBase {
 public:
     ssModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_PARALLEL) {}
 };
-// -a switch_hybrid: the reference switches from parallel to sequential pivots
-// when a round yields few pivots; the deconflicted round here always applies
-// at least the best pivot, so the hybrid runs the parallel form.
+// -a switch_hybrid: parallel rounds until one applies fewer than 10 pivots,
+// then sequential ones (switch/switch_model_parallel.cu:182-184).
 class switchModel_parallel : public flock_detail::ModelBase {
 public:
-    switchModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_PARALLEL) {}
+    switchModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_SWITCH) {}
 };

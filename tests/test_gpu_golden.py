@@ -44,7 +44,7 @@ def test_reference_fixtures(e):
                        np.array(e["cost"], np.int32).reshape(e["m"], e["n"]))
     if e["scale"] == 0:
         vogel_equal(inst, e)
-    for pivot in ("parallel", "sequential"):
+    for pivot in ("parallel", "sequential", "switch"):
         res = fg.solve(inst, pivot=pivot)
         certified(inst, res)
         if e["status"] == 0 and e["scale"] == 0:

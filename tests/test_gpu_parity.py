@@ -84,14 +84,14 @@ def test_vogel_euclid_shape():
     assert_vogel_parity(fg.config_instance("euclid8000", 5, m=200, n=300))
 
 
-@pytest.mark.parametrize("pivot", ["parallel", "sequential"])
+@pytest.mark.parametrize("pivot", ["parallel", "sequential", "switch"])
 def test_solve_tiny(pivot):
     for inst in tiny_instances(23, 150):
         res = fg.solve(inst, pivot=pivot)
         assert_optimal(inst, res)
 
 
-@pytest.mark.parametrize("pivot", ["parallel", "sequential"])
+@pytest.mark.parametrize("pivot", ["parallel", "sequential", "switch"])
 @pytest.mark.parametrize("seed", [0, 1])
 def test_solve_uniform100(pivot, seed):
     inst = fg.config_instance("uniform100", seed)
