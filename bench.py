@@ -240,7 +240,7 @@ def main():
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                     "kernel": "k_bround (batched pricing rounds)", "peak_src": peaks["src"],
+                     "kernel": "k_bsolve (persistent batched solve)", "peak_src": peaks["src"],
                      "note": "algorithmic bytes = sum over instances of pricing rounds x (4mn + 4(m+n)); "
                              "per-instance matrices are re-read from L2"},
         "clocks": clk,
