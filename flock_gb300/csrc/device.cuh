@@ -86,6 +86,11 @@ struct Ctx {
     int32_t* v32;      // n  column duals as int32 when sc->narrow (kDead32: zero-demand column)
     // pointer-jumping scratch (double buffered)
     int32_t* anc0; int32_t* anc1; int32_t* len0; int32_t* len1; int64_t* acc0; int64_t* acc1;
+    // binary-lifting table: level j (j < lift_cap) holds each vertex's
+    // 2^j-th ancestor (clamped at the root), V entries per level; the dual
+    // recompute writes it.  lift_cap == 0: no table (ping-pong anc0/anc1).
+    int32_t* lift;
+    int32_t lift_cap;
     // pricing
     uint64_t* row_best;   // m   packed (reduced cost, column) of the best cell per row
     uint64_t* claim;      // V   edge claims
@@ -106,6 +111,14 @@ struct Ctx {
     int32_t* order;       // V  (BFS order of the start tree)
     int32_t* uf;          // V  union-find
 };
+
+// Levels of the binary-lifting table for V vertices: every depth is < V, so
+// ceil(log2 V) doubling passes reach the root; levels 0..ceil(log2 V).
+__host__ __device__ __forceinline__ int lift_levels(int V) {
+    int l = 0;
+    while ((1 << l) < V) l++;
+    return l + 1;
+}
 
 // --------------------------------------------------------------- helpers ---
 // A column dual as the int32 sweep sees it; sets `wide` when it does not fit.

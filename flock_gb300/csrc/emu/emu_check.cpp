@@ -41,6 +41,8 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.parent = arr<int32_t>(keep, V); c.flow = arr<int64_t>(keep, V); c.depth = arr<int32_t>(keep, V);
     c.pot = arr<int64_t>(keep, V);
     c.v32 = arr<int32_t>(keep, V);
+    c.lift_cap = lift_levels(V);
+    c.lift = arr<int32_t>(keep, (size_t)V * c.lift_cap);
     c.anc0 = arr<int32_t>(keep, V); c.anc1 = arr<int32_t>(keep, V);
     c.len0 = arr<int32_t>(keep, V); c.len1 = arr<int32_t>(keep, V);
     c.acc0 = arr<int64_t>(keep, V); c.acc1 = arr<int64_t>(keep, V);

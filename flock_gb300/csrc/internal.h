@@ -29,6 +29,7 @@ struct BatchArgs {
     int32_t maxV, maxM;         // largest instance of the launch (shared-memory staging size)
     int32_t bfs_method, mode, max_rounds;
     int32_t light;              // 1: stage only the per-step tree arrays (largest bucket)
+    int32_t lift;               // 1: stage the binary-lifting table (parallel single pivots)
 };
 
 // A served request's device region: byte offsets of its arrays (256-aligned).
@@ -90,6 +91,8 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.csr_adj = (int32_t*)k.G(8 * v);
     c.order = (int32_t*)k.G(4 * v);
     c.uf = (int32_t*)k.G(4 * v);
+    c.lift_cap = lift_levels(V);
+    c.lift = (int32_t*)k.G(4 * v * (size_t)c.lift_cap);
     if (smem_bytes) *smem_bytes = k.so;
     if (global_bytes) *global_bytes = (k.go + 255) & ~size_t(255);
 }

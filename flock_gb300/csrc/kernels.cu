@@ -269,11 +269,13 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
 
 // Shared-memory staging of the arrays every pivot step touches.  Light
 // staging (the largest bucket) keeps the pointer-jumping buffers and the
-// edge claims in the instance's global working set.  Every pointer is carved
-// from the extern shared base and kLight is a compile-time constant, so the
-// compiler knows they address shared memory (shared loads and atomics rather
-// than generic ones).  staged_bytes() below must follow the same order.
-template <bool kLight>
+// edge claims in the instance's global working set.  kLift stages the
+// binary-lifting table (in place of the two pointer-jumping buffers), which
+// makes single-candidate pivots fully parallel.  Every pointer is carved
+// from the extern shared base and the flags are compile-time constants, so
+// the compiler knows they address shared memory (shared loads and atomics
+// rather than generic ones).  staged_bytes() below follows the same order.
+template <bool kLight, bool kLift>
 __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
     Carver k{nullptr, 0, smem, 0};
     c.parent = (int32_t*)k.S(4 * (size_t)V);
@@ -282,37 +284,58 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     c.row_best = (uint64_t*)k.S(8 * (size_t)M);
     c.pot = (int64_t*)k.S(8 * (size_t)V);
     c.v32 = (int32_t*)k.S(4 * (size_t)V);
-    if (!kLight) {
-        c.claim = (uint64_t*)k.S(8 * (size_t)V);
+    if (kLight) {
+        c.lift_cap = 0;
+        return;
+    }
+    c.claim = (uint64_t*)k.S(8 * (size_t)V);
+    c.len0 = (int32_t*)k.S(4 * (size_t)V);
+    c.len1 = (int32_t*)k.S(4 * (size_t)V);
+    c.acc0 = (int64_t*)k.S(8 * (size_t)V);
+    c.acc1 = (int64_t*)k.S(8 * (size_t)V);
+    if (kLift) {
+        c.lift_cap = lift_levels(V);
+        c.lift = (int32_t*)k.S(4 * (size_t)V * c.lift_cap);
+        c.anc0 = c.lift;
+        c.anc1 = c.lift;
+    } else {
         c.anc0 = (int32_t*)k.S(4 * (size_t)V);
         c.anc1 = (int32_t*)k.S(4 * (size_t)V);
-        c.len0 = (int32_t*)k.S(4 * (size_t)V);
-        c.len1 = (int32_t*)k.S(4 * (size_t)V);
-        c.acc0 = (int64_t*)k.S(8 * (size_t)V);
-        c.acc1 = (int64_t*)k.S(8 * (size_t)V);
+        c.lift = c.anc0;
+        c.lift_cap = 0;
     }
 }
 
-inline size_t staged_bytes(int V, int M, bool light) {
+inline size_t staged_bytes(int V, int M, bool light, bool lift) {
     Carver k{nullptr, 0, (unsigned char*)16, 0};
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
     k.S(4 * (size_t)V);
     if (!light) {
-        k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V);
-        k.S(8 * (size_t)V); k.S(8 * (size_t)V);
+        k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
+        if (lift) k.S(4 * (size_t)V * lift_levels(V));
+        else { k.S(4 * (size_t)V); k.S(4 * (size_t)V); }
     }
     return (k.so + 15) & ~size_t(15);
 }
 
+// Largest dynamic shared memory a staged launch may use.
+constexpr size_t kStageSmemMax = 226 * 1024;
+
+// Staging of a launch whose largest instance is maxV x (rows maxM): light
+// for the largest bucket, the lifting table whenever it fits.
+inline bool stage_lift(int maxV, int maxM, bool light) {
+    return !light && staged_bytes(maxV, maxM, false, true) <= kStageSmemMax;
+}
+
 // Pricing rounds of one instance with its tree staged in shared memory:
 // `max_here` rounds at most (1 for the round-kernel form), or until done.
-template <bool kLight>
+template <bool kLight, bool kLift>
 __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs, unsigned char* smem,
                             int max_here) {
     Ctx g;
     batch_ctx(a, d, g);
     Ctx c = g;
-    stage_hot<kLight>(c, smem, a.maxV, a.maxM);
+    stage_hot<kLight, kLift>(c, smem, a.maxV, a.maxM);
     const int V = d.m + d.n;
     for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
     __syncthreads();
@@ -354,8 +377,9 @@ __global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) continue;
         if (d.sc->done) continue;          // every thread reads the same value
-        if (a.light) brounds_one<true>(a, d, bs, smem, 1);
-        else brounds_one<false>(a, d, bs, smem, 1);
+        if (a.light) brounds_one<true, false>(a, d, bs, smem, 1);
+        else if (a.lift) brounds_one<false, true>(a, d, bs, smem, 1);
+        else brounds_one<false, false>(a, d, bs, smem, 1);
     }
 }
 
@@ -392,8 +416,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
         if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); publish_done(d); continue; }
         bsetup_one(a, d, bs);
         if (!d.sc->done) {
-            if (a.light) brounds_one<true>(a, d, bs, smem, 1 << 30);
-            else brounds_one<false>(a, d, bs, smem, 1 << 30);
+            if (a.light) brounds_one<true, false>(a, d, bs, smem, 1 << 30);
+            else if (a.lift) brounds_one<false, true>(a, d, bs, smem, 1 << 30);
+            else brounds_one<false, false>(a, d, bs, smem, 1 << 30);
         }
         bfinal_one(a, d, bs);
         publish_done(d);
@@ -1014,6 +1039,7 @@ struct BatchRunner {
         a.next = nullptr; a.active = nullptr;
         a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
         a.light = bucket_light(b) ? 1 : 0;
+        a.lift = stage_lift(bmaxV[b], bmaxM[b], a.light != 0) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = pivot_mode(opt);
         a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
@@ -1033,7 +1059,7 @@ struct BatchRunner {
     // Pricing rounds of bucket b as a CUDA graph: `chunk` x (zero the
     // counters, one k_bround launch).
     int capture_rounds(int b, const TuneCfg& t, cudaGraphExec_t* exec) {
-        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b));
+        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
         const int grid = grid_for(b, t, smem, (const void*)k_bround);
         cudaStream_t s = st[b];
         cudaGraph_t g;
@@ -1069,7 +1095,7 @@ struct BatchRunner {
             BatchArgs a = args_for(b);
             a.next = ctr(b);
             if (cfg[b].persistent) {
-                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b));
+                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
                 FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
                 const void* fn = bsolve_fn(cfg[b].threads);
                 void* kargs[] = {&a};
@@ -1300,7 +1326,8 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.mode = pivot_mode(opt);
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
     a.light = maxV > kBucketEdges[kNumBuckets - 2] ? 1 : 0;
-    const size_t smem = staged_bytes(maxV, maxM, a.light != 0);
+    a.lift = stage_lift(maxV, maxM, a.light != 0) ? 1 : 0;
+    const size_t smem = staged_bytes(maxV, maxM, a.light != 0, a.lift != 0);
     const int threads = serve_threads(maxV);
     const void* fn = bsolve_fn(threads);
     int per_sm = 0;

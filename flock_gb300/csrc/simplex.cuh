@@ -256,19 +256,24 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int V = I.m + I.n;
     const int root = c.sc->root;
+    // With a lifting table every doubling level is kept (level it+1 from
+    // level it); otherwise two buffers alternate.
+    const bool lifting = c.lift_cap > 0;
+    int32_t* aA = lifting ? c.lift : c.anc0;
+    int32_t* aB = lifting ? c.lift + V : c.anc1;
+    const int max_it = lifting ? c.lift_cap - 1 : 40;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
         const int p = c.parent[v];
-        if (p == -2) { c.anc0[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
-        else if (v == root) { c.anc0[v] = v; c.len0[v] = 0; c.acc0[v] = 0; }
-        else if (!FLOCK_IN(p, V) || (p < I.m) == (v < I.m)) { fail_check(c.sc, 20); c.anc0[v] = root; c.len0[v] = 0; c.acc0[v] = 0; }
-        else { c.anc0[v] = p; c.len0[v] = 1; c.acc0[v] = edge_cost(I, v, p); }
+        if (p == -2) { aA[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
+        else if (v == root) { aA[v] = v; c.len0[v] = 0; c.acc0[v] = 0; }
+        else if (!FLOCK_IN(p, V) || (p < I.m) == (v < I.m)) { fail_check(c.sc, 20); aA[v] = root; c.len0[v] = 0; c.acc0[v] = 0; }
+        else { aA[v] = p; c.len0[v] = 1; c.acc0[v] = edge_cost(I, v, p); }
     }
-    int32_t* aA = c.anc0; int32_t* aB = c.anc1;
     int32_t* lA = c.len0; int32_t* lB = c.len1;
     int64_t* xA = c.acc0; int64_t* xB = c.acc1;
     int pending = 1;
     __syncthreads();
-    for (int it = 0; it < 40 && pending; it++) {
+    for (int it = 0; it < max_it && pending; it++) {
         int mine = 0;
         for (int v = threadIdx.x; v < V; v += blockDim.x) {
             const int a = aA[v];
@@ -283,7 +288,8 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
             mine |= (aa != root);
         }
         pending = __syncthreads_or(mine);
-        int32_t* t1 = aA; aA = aB; aB = t1;
+        if (lifting) { aA = aB; aB = c.lift + (size_t)(it + 2) * V; }
+        else { int32_t* t1 = aA; aA = aB; aB = t1; }
         int32_t* t2 = lA; lA = lB; lB = t2;
         int64_t* t3 = xA; xA = xB; xB = t3;
     }
@@ -357,33 +363,43 @@ __device__ void sweep_cta(const Ctx& c) {
     }
     const int nfull = n >> 2, tail = n & 3;
     const int4* v4 = reinterpret_cast<const int4*>(c.v32);
-    for (int i = threadIdx.x >> 5; i < m; i += nw) {
-        const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
-        int32_t bv = INT32_MAX, bj = INT32_MAX;
+    // Two rows per warp pass (i and i + nw): twice the loads in flight.
+    for (int i = threadIdx.x >> 5; i < m; i += 2 * nw) {
+        const int i2 = i + nw;
+        const bool two = i2 < m;
+        const int4* ra = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
+        const int4* rb = reinterpret_cast<const int4*>(I.cost + (size_t)(two ? i2 : i) * I.ldc);
+        int32_t av = INT32_MAX, aj = INT32_MAX, bv = INT32_MAX, bj = INT32_MAX;
         int q = lane;
-        for (; q + 96 < nfull; q += 128) {
-            const int4 a0 = row[q], a1 = row[q + 32], a2 = row[q + 64], a3 = row[q + 96];
-            min4(bv, bj, a0, v4[q], 4 * q);
-            min4(bv, bj, a1, v4[q + 32], 4 * (q + 32));
-            min4(bv, bj, a2, v4[q + 64], 4 * (q + 64));
-            min4(bv, bj, a3, v4[q + 96], 4 * (q + 96));
+        for (; q + 32 < nfull; q += 64) {
+            const int4 a0 = ra[q], a1 = ra[q + 32], b0 = rb[q], b1 = rb[q + 32];
+            const int4 w0 = v4[q], w1 = v4[q + 32];
+            min4(av, aj, a0, w0, 4 * q);
+            min4(av, aj, a1, w1, 4 * (q + 32));
+            min4(bv, bj, b0, w0, 4 * q);
+            min4(bv, bj, b1, w1, 4 * (q + 32));
         }
-        if (q + 32 < nfull) {
-            const int4 a0 = row[q], a1 = row[q + 32];
-            const int4 a2 = q + 64 < nfull ? row[q + 64] : make_int4(0, 0, 0, 0);
-            min4(bv, bj, a0, v4[q], 4 * q);
-            min4(bv, bj, a1, v4[q + 32], 4 * (q + 32));
-            if (q + 64 < nfull) min4(bv, bj, a2, v4[q + 64], 4 * (q + 64));
-        } else if (q < nfull) {
-            min4(bv, bj, row[q], v4[q], 4 * q);
+        if (q < nfull) {
+            const int4 a0 = ra[q], b0 = rb[q], w0 = v4[q];
+            min4(av, aj, a0, w0, 4 * q);
+            min4(bv, bj, b0, w0, 4 * q);
         }
         if (lane < tail) {
             const int j = 4 * nfull + lane;
-            const int32_t t = I.cost[(size_t)i * I.ldc + j] - c.v32[j];
-            if (t < bv) { bv = t; bj = j; }
+            const int32_t vj = c.v32[j];
+            const int32_t ta = I.cost[(size_t)i * I.ldc + j] - vj;
+            if (ta < av) { av = ta; aj = j; }
+            if (two) {
+                const int32_t tb = I.cost[(size_t)i2 * I.ldc + j] - vj;
+                if (tb < bv) { bv = tb; bj = j; }
+            }
         }
-        const uint64_t k = narrow_row_key(c, i, 0, n, bv, bj);
-        if (lane == 0) c.row_best[i] = k;
+        const uint64_t ka = narrow_row_key(c, i, 0, n, av, aj);
+        if (lane == 0) c.row_best[i] = ka;
+        if (two) {      // warp-uniform
+            const uint64_t kb = narrow_row_key(c, i2, 0, n, bv, bj);
+            if (lane == 0) c.row_best[i2] = kb;
+        }
     }
     __syncthreads();
 }
@@ -485,6 +501,107 @@ __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const Cy
     }
 }
 
+// k-th ancestor of x from the lifting table (k below 2^(lift_cap-1));
+// -1 if the table leads outside the tree.
+__device__ __forceinline__ int kth_anc(const Ctx& c, int V, int x, int k) {
+    for (int j = 0; k; j++, k >>= 1) {
+        if (k & 1) {
+            x = c.lift[(size_t)j * V + x];
+            if (!FLOCK_IN(x, V)) return -1;
+        }
+    }
+    return x;
+}
+
+// int64 -> uint64 preserving order (for unsigned block reductions).
+__device__ __forceinline__ uint64_t oflow(int64_t f) { return (uint64_t)f ^ 0x8000000000000000ull; }
+
+// One pivot of entering cell (row k, column vertex l) with every step over
+// the cycle done by the whole CTA in parallel, using the lifting table.  A
+// tree edge (child v) is on the cycle iff v is an ancestor-or-self of
+// exactly one of k and l (the k-th ancestor test).  The leaving edge and
+// θ follow cycle_walk's rule exactly: on the k side the decreasing edges
+// are row children and ties go to the one nearest k (the deepest); on the
+// l side column children, ties to the one nearest the apex (the
+// shallowest); the l side wins ties between the sides.  The flows change by
+// ∓θ along the cycle and the segment from the leaving edge down to the
+// entering cell's endpoint is re-hung, as cycle_apply does.  Uses claim[]
+// (side marks) and len1/acc1 (new parents and flows) as scratch.  Returns
+// 1 if the pivot was applied (block-uniform).
+__device__ int single_pivot_lift(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
+    const int m = c.I.m;
+    const int dk = c.depth[k], dl = c.depth[l];
+    uint64_t mk = kNoKey, ml = kNoKey;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        int side = 0;                              // 1: k side, 2: l side
+        if (c.parent[v] >= 0) {
+            const int dv = c.depth[v];
+            const bool on_k = dv <= dk && kth_anc(c, V, k, dk - dv) == v;
+            const bool on_l = dv <= dl && kth_anc(c, V, l, dl - dv) == v;
+            if (on_k != on_l) side = on_k ? 1 : 2;
+        }
+        c.claim[v] = (uint64_t)side;
+        if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
+        if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
+    }
+    mk = block_min_u64(mk, bs);
+    ml = block_min_u64(ml, bs);
+    const bool lside = ml <= mk;                   // uniform
+    const uint64_t fmin = lside ? ml : mk;
+    // leaving edge: k side the deepest, l side the shallowest among the minima
+    uint64_t pick = lside ? kNoKey : 0ull;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const uint64_t sd = c.claim[v];
+        if (lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) {
+            if (oflow(c.flow[v]) == fmin) {
+                const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
+                if (lside) pick = key < pick ? key : pick;
+                else pick = key > pick ? key : pick;
+            }
+        }
+    }
+    pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
+    if (fmin == kNoKey || pick == kNoKey || (!lside && pick == 0)) {
+        if (threadIdx.x == 0) fail_check(c.sc, 16);
+        __syncthreads();
+        return 0;
+    }
+    const int q = (int)(uint32_t)pick;
+    const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
+    const int e = lside ? l : k, other = lside ? k : l;
+    const int de = lside ? dl : dk, dq = c.depth[q];
+    const uint64_t eside = lside ? 2 : 1;
+    // flows along the cycle; the re-hung segment's new parents and flows
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const uint64_t sd = c.claim[v];
+        if (sd) c.flow[v] += (sd == 1) == (v < m) ? -th : th;
+    }
+    __syncthreads();
+    int bad = 0;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        if (c.claim[v] != eside) continue;
+        const int dv = c.depth[v];
+        if (dv < dq) continue;                     // above the leaving edge
+        const int prev = v == e ? other : kth_anc(c, V, e, de - dv - 1);
+        if (!FLOCK_IN(prev, V)) { bad = 1; continue; }
+        c.len1[v] = prev;
+        c.acc1[v] = v == e ? th : c.flow[prev];
+    }
+    bad = __syncthreads_or(bad);
+    if (bad) {
+        if (threadIdx.x == 0) fail_check(c.sc, 17);
+        __syncthreads();
+        return 0;
+    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        if (c.claim[v] != eside || c.depth[v] < dq) continue;
+        c.parent[v] = c.len1[v];
+        c.flow[v] = c.acc1[v];
+    }
+    __syncthreads();
+    return 1;
+}
+
 // Parallel mode: candidates walked per round (the rest wait for later rounds).
 constexpr int kMaxCand = 32;
 // Switch mode: a parallel round applying fewer pivots than this switches the
@@ -552,6 +669,19 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     const int ncand = bs.i[0];
     if (ncand == 0) {
         if (threadIdx.x == 0) { c.sc->done = 1; c.sc->ncand = 0; }
+        __syncthreads();
+        return;
+    }
+    if (ncand == 1 && c.lift_cap > 0) {
+        const int i = c.cand[0];
+        const int ok = single_pivot_lift(c, bs, i, m + (int)key_idx(c.row_best[i]), V);
+        if (threadIdx.x == 0) {
+            c.sc->pivots += ok;
+            c.sc->ncand = 1;
+            c.sc->last_winners = ok;
+            if (!ok) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+            if (mode == 2) c.sc->mode = 0;
+        }
         __syncthreads();
         return;
     }
