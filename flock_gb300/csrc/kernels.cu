@@ -269,9 +269,10 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
 
 // Shared-memory staging of the arrays every pivot step touches.  Light
 // staging (the largest bucket) keeps the pointer-jumping buffers and the
-// edge claims in the instance's global working set.  kLift stages the
-// binary-lifting table (in place of the two pointer-jumping buffers), which
-// makes single-candidate pivots fully parallel.  Every pointer is carved
+// edge claims in the instance's global working set.  The binary-lifting
+// table (which replaces the two pointer-jumping ancestor buffers and makes
+// single-candidate pivots fully parallel) is staged when it fits (kLift),
+// else it stays in the global working set.  Every pointer is carved
 // from the extern shared base and the flags are compile-time constants, so
 // the compiler knows they address shared memory (shared loads and atomics
 // rather than generic ones).  staged_bytes() below follows the same order.
@@ -284,10 +285,9 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     c.row_best = (uint64_t*)k.S(8 * (size_t)M);
     c.pot = (int64_t*)k.S(8 * (size_t)V);
     c.v32 = (int32_t*)k.S(4 * (size_t)V);
-    if (kLight) {
-        c.lift_cap = 0;
-        return;
-    }
+    // Without kLift the lifting table stays in the instance's global working
+    // set (carved there by batch_ctx, stride and level count of the instance).
+    if (kLight) return;
     c.claim = (uint64_t*)k.S(8 * (size_t)V);
     c.len0 = (int32_t*)k.S(4 * (size_t)V);
     c.len1 = (int32_t*)k.S(4 * (size_t)V);
@@ -296,14 +296,9 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     if (kLift) {
         c.lift_cap = lift_levels(V);
         c.lift = (int32_t*)k.S(4 * (size_t)V * c.lift_cap);
-        c.anc0 = c.lift;
-        c.anc1 = c.lift;
-    } else {
-        c.anc0 = (int32_t*)k.S(4 * (size_t)V);
-        c.anc1 = (int32_t*)k.S(4 * (size_t)V);
-        c.lift = c.anc0;
-        c.lift_cap = 0;
     }
+    c.anc0 = c.lift;
+    c.anc1 = c.lift;
 }
 
 inline size_t staged_bytes(int V, int M, bool light, bool lift) {
@@ -313,7 +308,6 @@ inline size_t staged_bytes(int V, int M, bool light, bool lift) {
     if (!light) {
         k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
         if (lift) k.S(4 * (size_t)V * lift_levels(V));
-        else { k.S(4 * (size_t)V); k.S(4 * (size_t)V); }
     }
     return (k.so + 15) & ~size_t(15);
 }
@@ -899,6 +893,7 @@ struct BatchRunner {
     std::vector<flock_stats> plain_stats;
     std::vector<std::vector<flock_flow>> plain_flows;
     int32_t launches = 0;                   // kernels launched by the last run
+    bool packed = false;                    // every bucket packed into the staging buffers
 
     int setup() {
         if (init) return FLOCK_OK;
@@ -915,7 +910,10 @@ struct BatchRunner {
         return FLOCK_OK;
     }
 
-    // Validate and stage the instances into pinned host memory.
+    // Validate the instances and lay out the arenas.  Costs are packed into
+    // pinned memory per bucket just before that bucket is uploaded and
+    // launched (pack_bucket), so packing overlaps with the device work of the
+    // buckets launched before it.
     int prepare(int cnt, const flock_instance* in, const flock_options* opt_in) {
         int rc = setup();
         if (rc) return rc;
@@ -925,43 +923,22 @@ struct BatchRunner {
         count = cnt;
         V_of.assign(cnt, 0); m_of.assign(cnt, 0); n_of.assign(cnt, 0);
         out_off.assign(cnt, 0); pot_off.assign(cnt, 0);
+        cost_off.assign(cnt, 0); sd_off.assign(cnt, 0); ws_off.assign(cnt, 0);
         plain_list.clear();
         total_cells = total_pot = total_cost = total_sd = total_ws = 0;
-        cost_off.assign(cnt, 0); sd_off.assign(cnt, 0); ws_off.assign(cnt, 0);
-        // Validation in the order validate_instance uses, the O(m n) cost
-        // range check fused into the copy below (threads over instances);
-        // the first failing instance reports its first failing check.
+        // Validation in the order validate_instance uses: every shape check,
+        // then the O(m n) cost range check (threads over instances); the
+        // first failing instance reports its first failing check.  Nothing is
+        // launched before every instance has passed.
         std::vector<int> pre(cnt, FLOCK_OK);
         std::vector<std::string> pre_msg(cnt);
         for (int k = 0; k < cnt; k++) {
             if ((pre[k] = validate_shape(&in[k], &pre_msg[k]))) continue;
-            const int m = in[k].m, n = in[k].n;
-            m_of[k] = m; n_of[k] = n; V_of[k] = m + n;
-            out_off[k] = total_cells; total_cells += m + n - 1;
-            pot_off[k] = total_pot; total_pot += m + n;
-            if (m + n > kMaxStagedV) { plain_list.push_back(k); continue; }
-            const int ldc = (n + 3) & ~3;
-            cost_off[k] = total_cost; total_cost += (int64_t)m * ldc;
-            sd_off[k] = total_sd; total_sd += m + n;
-            ws_off[k] = total_ws; total_ws += (int64_t)instance_ws_bytes(m + n, m);
+            m_of[k] = in[k].m; n_of[k] = in[k].n; V_of[k] = in[k].m + in[k].n;
         }
-        FLOCK_CK(h_cost.ensure((size_t)total_cost * 4 + 16));
-        FLOCK_CK(h_sd.ensure((size_t)total_sd * 4 + 16));
         std::vector<uint8_t> cost_bad(cnt, 0);
         parallel_for(cnt, [&](int k) {
-            if (pre[k]) return;
-            const int m = m_of[k], n = n_of[k];
-            if (V_of[k] > kMaxStagedV) { cost_bad[k] = !costs_in_range(in[k].cost, (size_t)m * n); return; }
-            const int ldc = (n + 3) & ~3;
-            int32_t* dst = h_cost.as<int32_t>() + cost_off[k];
-            bool ok = true;
-            for (int i = 0; i < m; i++) {
-                ok &= copy_costs_checked(dst + (size_t)i * ldc, in[k].cost + (size_t)i * n, n);
-                for (int j = n; j < ldc; j++) dst[(size_t)i * ldc + j] = 0;
-            }
-            cost_bad[k] = !ok;
-            memcpy(h_sd.as<int32_t>() + sd_off[k], in[k].supply, (size_t)m * 4);
-            memcpy(h_sd.as<int32_t>() + sd_off[k] + m, in[k].demand, (size_t)n * 4);
+            if (!pre[k]) cost_bad[k] = !costs_in_range(in[k].cost, (size_t)m_of[k] * n_of[k]);
         });
         for (int k = 0; k < cnt; k++) {
             if (pre[k]) { set_error(pre_msg[k]); return pre[k]; }
@@ -969,13 +946,26 @@ struct BatchRunner {
         }
         // bucket, largest first inside each bucket (work stealing starts with the long solves)
         std::vector<int> order;
-        for (int k = 0; k < cnt; k++) if (V_of[k] <= kMaxStagedV) order.push_back(k);
+        for (int k = 0; k < cnt; k++) {
+            out_off[k] = total_cells; total_cells += V_of[k] - 1;
+            pot_off[k] = total_pot; total_pot += V_of[k];
+            if (V_of[k] <= kMaxStagedV) order.push_back(k); else plain_list.push_back(k);
+        }
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
             const int ba = bucket_of(V_of[a]), bb = bucket_of(V_of[b]);
             if (ba != bb) return ba < bb;
             return (int64_t)m_of[a] * n_of[a] > (int64_t)m_of[b] * n_of[b];
         });
         order_ = order;
+        // arenas in bucket order: each bucket's costs and quantities are contiguous
+        for (int k : order) {
+            const int m = m_of[k], n = n_of[k], ldc = (n + 3) & ~3;
+            cost_off[k] = total_cost; total_cost += (int64_t)m * ldc;
+            sd_off[k] = total_sd; total_sd += m + n;
+            ws_off[k] = total_ws; total_ws += (int64_t)instance_ws_bytes(m + n, m);
+        }
+        FLOCK_CK(h_cost.ensure((size_t)total_cost * 4 + 16));
+        FLOCK_CK(h_sd.ensure((size_t)total_sd * 4 + 16));
         descs.resize(order.size());
         for (int b = 0; b <= kNumBuckets; b++) bstart[b] = 0;
         for (int b = 0; b < kNumBuckets; b++) { bmaxV[b] = 0; bmaxM[b] = 0; }
@@ -987,6 +977,42 @@ struct BatchRunner {
             bmaxM[b] = std::max(bmaxM[b], m_of[k]);
         }
         for (int b = 0; b < kNumBuckets; b++) bstart[b + 1] += bstart[b];
+        packed = false;
+        return FLOCK_OK;
+    }
+
+    // Pack bucket b's costs (row pitch padded to 4) and quantities into the
+    // pinned staging buffers (threads over instances).
+    void pack_bucket(int b) {
+        parallel_for(bstart[b + 1] - bstart[b], [&](int q) {
+            const int k = order_[bstart[b] + q];
+            const int m = m_of[k], n = n_of[k], ldc = (n + 3) & ~3;
+            int32_t* dst = h_cost.as<int32_t>() + cost_off[k];
+            if (ldc == n) {
+                memcpy(dst, insts[k].cost, (size_t)m * n * 4);
+            } else {
+                for (int i = 0; i < m; i++) {
+                    memcpy(dst + (size_t)i * ldc, insts[k].cost + (size_t)i * n, (size_t)n * 4);
+                    for (int j = n; j < ldc; j++) dst[(size_t)i * ldc + j] = 0;
+                }
+            }
+            memcpy(h_sd.as<int32_t>() + sd_off[k], insts[k].supply, (size_t)m * 4);
+            memcpy(h_sd.as<int32_t>() + sd_off[k] + m, insts[k].demand, (size_t)n * 4);
+        });
+    }
+
+    // Pack and upload bucket b on stream s (its cost and quantity ranges are
+    // contiguous in both arenas).
+    int stage_bucket(int b, cudaStream_t s) {
+        if (bstart[b + 1] == bstart[b]) return FLOCK_OK;
+        pack_bucket(b);
+        const int k0 = order_[bstart[b]], k1 = order_[bstart[b + 1] - 1];
+        const int64_t c0 = cost_off[k0], c1 = cost_off[k1] + (int64_t)m_of[k1] * ((n_of[k1] + 3) & ~3);
+        const int64_t s0 = sd_off[k0], s1 = sd_off[k1] + V_of[k1];
+        FLOCK_CK(cudaMemcpyAsync(d_cost.as<int32_t>() + c0, h_cost.as<int32_t>() + c0, (size_t)(c1 - c0) * 4,
+                                 cudaMemcpyHostToDevice, s));
+        FLOCK_CK(cudaMemcpyAsync(d_sd.as<int32_t>() + s0, h_sd.as<int32_t>() + s0, (size_t)(s1 - s0) * 4,
+                                 cudaMemcpyHostToDevice, s));
         return FLOCK_OK;
     }
 
@@ -1080,7 +1106,9 @@ struct BatchRunner {
 
     // Solve every staged bucket (all buckets concurrently, one stream each).
     // Inputs must already be on the device.  Returns when all are done.
-    int run_device(const TuneCfg* cfg, float* ms, int only_bucket = -1) {
+    // stage: pack and upload each bucket's inputs on its stream right before
+    // its launch (the descriptors must already be on the device).
+    int run_device(const TuneCfg* cfg, float* ms, int only_bucket = -1, bool stage = false) {
         int rc;
         cudaStream_t s0 = st[0];
         FLOCK_CK(cudaEventRecord(ev_start, s0));
@@ -1094,6 +1122,7 @@ struct BatchRunner {
             if (!nb || (only_bucket >= 0 && b != only_bucket)) continue;
             BatchArgs a = args_for(b);
             a.next = ctr(b);
+            if (stage && (rc = stage_bucket(b, st[b]))) return rc;
             if (cfg[b].persistent) {
                 const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
                 FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
@@ -1148,8 +1177,13 @@ struct BatchRunner {
         return FLOCK_OK;
     }
 
+    // Upload every staged input (packing the buckets not packed yet).
     int upload() {
         cudaStream_t s0 = st[0];
+        if (!packed) {
+            for (int b = 0; b < kNumBuckets; b++) pack_bucket(b);
+            packed = true;
+        }
         if (total_cost) FLOCK_CK(cudaMemcpyAsync(d_cost.p, h_cost.p, (size_t)total_cost * 4, cudaMemcpyHostToDevice, s0));
         if (total_sd) FLOCK_CK(cudaMemcpyAsync(d_sd.p, h_sd.p, (size_t)total_sd * 4, cudaMemcpyHostToDevice, s0));
         if (!descs.empty())
@@ -1173,8 +1207,19 @@ struct BatchRunner {
         if (rc) return rc;
         TuneCfg cfg[kNumBuckets];
         for (int b = 0; b < kNumBuckets; b++) cfg[b] = cfg_for(b);
-        if ((rc = upload())) return rc;
-        if ((rc = run_device(cfg, &last_ms))) return rc;
+        if (packed) {
+            if ((rc = upload())) return rc;
+            if ((rc = run_device(cfg, &last_ms))) return rc;
+        } else {
+            // descriptors first, then each bucket packed, uploaded and
+            // launched in turn (largest first) so host packing overlaps with
+            // the device work already launched
+            if (!descs.empty())
+                FLOCK_CK(cudaMemcpyAsync(d_desc.p, h_desc.p, descs.size() * sizeof(BatchDesc), cudaMemcpyHostToDevice,
+                                         st[0]));
+            if ((rc = run_device(cfg, &last_ms, -1, true))) return rc;
+            packed = true;
+        }
         if ((rc = download())) return rc;
         plain_stats.assign(plain_list.size(), flock_stats{});
         plain_flows.assign(plain_list.size(), {});
@@ -1371,19 +1416,20 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
     if (!at || strcmp(at, "0") != 0) { if ((rc = R.autotune())) return rc; }
     if ((rc = R.solve_all())) return rc;
     const float ms = R.last_ms;
-    int worst = FLOCK_OK;
-    int64_t off = 0;
-    for (int k = 0; k < cnt; k++) {
-        flock_flow* f = flows ? flows + (flow_offset ? flow_offset[k] : off) : nullptr;
-        off += R.V_of[k] - 1;
+    std::vector<int64_t> off(cnt);
+    int64_t o = 0;
+    for (int k = 0; k < cnt; k++) { off[k] = flow_offset ? flow_offset[k] : o; o += R.V_of[k] - 1; }
+    std::atomic<int> bad{0};
+    const double total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    parallel_for(cnt, [&](int k) {
         flock_stats s;
-        R.collect(k, f, &s);
-        s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        R.collect(k, flows ? flows + off[k] : nullptr, &s);
+        s.ms_total = total;
         s.ms_simplex = ms;
         if (stats) stats[k] = s;
-        if (s.status) worst = FLOCK_ERR_NOT_OPTIMAL;
-    }
-    return worst;
+        if (s.status) bad.store(1);
+    });
+    return bad.load() ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
 }
 
 // Device-only timing hook for the benchmark: solve the last staged batch
