@@ -34,7 +34,8 @@ class CFlow(ctypes.Structure):
 
 
 class COptions(ctypes.Structure):
-    _fields_ = [("bfs_method", i32), ("pivot_method", i32), ("max_iterations", i32), ("verify", i32)]
+    _fields_ = [("bfs_method", i32), ("pivot_method", i32), ("max_iterations", i32), ("verify", i32),
+                ("pricing", i32)]
 
 
 class CStats(ctypes.Structure):
@@ -239,8 +240,11 @@ class Result:
         return self.status == 0
 
 
-def _options(bfs="vogel", pivot="parallel", max_iterations=0, verify=True) -> COptions:
-    return COptions(BFS[bfs], PIVOT[pivot], int(max_iterations), 1 if verify else 0)
+PRICING = {"full": 0, "partial": 1}
+
+
+def _options(bfs="vogel", pivot="switch", max_iterations=0, verify=True, pricing="full") -> COptions:
+    return COptions(BFS[bfs], PIVOT[pivot], int(max_iterations), 1 if verify else 0, PRICING[pricing])
 
 
 def _result(st: CStats, flows: np.ndarray, u=None, v=None) -> Result:
@@ -278,13 +282,13 @@ def vogel(inst: Instance) -> Tuple[np.ndarray, int]:
 
 
 def batch_solve(insts: Sequence[Instance], bfs: str = "vogel", pivot: str = "switch",
-                max_iterations: int = 0, verify: bool = True) -> List[Result]:
+                max_iterations: int = 0, verify: bool = True, pricing: str = "full") -> List[Result]:
     k = len(insts)
     arr = (CInstance * k)(*[x.c() for x in insts])
     total = sum(x.m + x.n - 1 for x in insts)
     flows = np.zeros((max(total, 1), 3), np.int32)
     stats = (CStats * k)()
-    opt = _options(bfs, pivot, max_iterations, verify)
+    opt = _options(bfs, pivot, max_iterations, verify, pricing)
     rc = lib().flock_batch_solve(k, arr, ctypes.byref(opt), flows.ctypes.data_as(P(CFlow)), None, stats)
     if rc and rc != FLOCK_ERR_NOT_OPTIMAL:
         raise _err(rc)
@@ -316,14 +320,14 @@ class Server:
         return int(lib().flock_server_request_bytes(m, n))
 
     def __init__(self, memory_budget_bytes: int = 40 << 30, max_inflight_batches: int = 16, max_batch: int = 512,
-                 bfs: str = "vogel", pivot: str = "switch", verify: bool = True):
+                 bfs: str = "vogel", pivot: str = "switch", verify: bool = True, pricing: str = "full"):
         L = lib()
         cfg = CServerConfig()
         L.flock_default_server_config(ctypes.byref(cfg))
         cfg.memory_budget_bytes = memory_budget_bytes
         cfg.max_inflight_batches = max_inflight_batches
         cfg.max_batch = max_batch
-        cfg.options = _options(bfs, pivot, 0, verify)
+        cfg.options = _options(bfs, pivot, 0, verify, pricing)
         self._h = ctypes.c_void_p()
         rc = L.flock_server_create(ctypes.byref(cfg), ctypes.byref(self._h))
         if rc:

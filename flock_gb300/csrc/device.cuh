@@ -39,6 +39,8 @@ constexpr int64_t kDeadPot = -(int64_t(1) << 61);   // dual of a zero-demand col
 // (zero-demand) column is stored as kDead32 and re-checked exactly.
 constexpr int32_t kDead32 = -((1 << 30) - 1);
 constexpr uint64_t kNoKey = ~0ull;
+constexpr int kPPRows = 64;      // partial pricing: candidate rows kept by a full sweep
+constexpr int kPPRefresh = 32;   // partial pricing: rounds between full sweeps
 
 struct Scalars {
     int32_t status;
@@ -59,7 +61,9 @@ struct Scalars {
     int32_t last_winners;
     int32_t fail_site;     // first failed internal check (0: none), see fail_check
     int32_t narrow;        // 1: every live column dual fits the int32 sweep (v32 valid)
-    int32_t pad_;
+    int32_t pricing;       // 0 full sweeps, 1 partial pricing (candidate rows)
+    int32_t pp_n;          // partial pricing: candidate rows in prow[]
+    int32_t pp_age;        // partial pricing: rounds since the last full sweep
 };
 
 // One instance as the kernels see it.
@@ -104,6 +108,7 @@ struct Ctx {
     int32_t* res;         // V  residual supply (rows) / demand (columns)
     int4* top2;           // V  (c1, c2, j1, j2) two cheapest uncovered crossing cells
     int32_t* rescan;      // V  list of lines whose top2 must be rebuilt
+    int32_t* prow;        // kPPRows  partial pricing: candidate rows
     // start-tree scratch
     int64_t* bsum;        // V
     int32_t* csr_start;   // V+1

@@ -2,7 +2,8 @@
 // an emulated CTA (cuda_emu.h) with every working array in its own heap
 // allocation, so that AddressSanitizer reports any out-of-bounds access of the
 // device logic.  Instances come from the library's generator.
-//   emu_check <seed> <count> <lo> <hi> <first> <last> [mode]
+//   emu_check <seed> <count> <lo> <hi> <first> <last> [mode] [pricing: 0 full, 1 partial, 2 partial + row keys
+//   scrambled between rounds]
 #define FLOCK_EMU
 #include <cstdio>
 #include <cstdlib>
@@ -20,7 +21,7 @@ template <class T> static T* arr(std::vector<std::unique_ptr<char[]>>& keep, siz
     return (T*)keep.back().get();
 }
 
-static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int32_t* cost, int mode,
+static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int32_t* cost, int mode, int pricing,
                      Scalars* out) {
     std::vector<std::unique_ptr<char[]>> keep;
     const int V = m + n, ldc = (n + 3) & ~3;
@@ -34,6 +35,7 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     Scalars* sc = arr<Scalars>(keep, 1);
     memset(sc, 0, sizeof(Scalars));
     sc->mode = mode;
+    sc->pricing = pricing ? 1 : 0;
     sc->max_rounds = 1 << 30;
     c.sc = sc;
     c.bfs_src = arr<int32_t>(keep, V); c.bfs_dst = arr<int32_t>(keep, V); c.bfs_qty = arr<int32_t>(keep, V);
@@ -41,6 +43,7 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.parent = arr<int32_t>(keep, V); c.flow = arr<int64_t>(keep, V); c.depth = arr<int32_t>(keep, V);
     c.pot = arr<int64_t>(keep, V);
     c.v32 = arr<int32_t>(keep, V);
+    c.prow = arr<int32_t>(keep, kPPRows);
     c.lift_cap = lift_levels(V);
     c.lift = arr<int32_t>(keep, (size_t)V * c.lift_cap);
     c.anc0 = arr<int32_t>(keep, V); c.anc1 = arr<int32_t>(keep, V);
@@ -60,9 +63,16 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
         __syncthreads();
         sf_init_cta(c, bs);
         if (!c.sc->done) tree_recompute_cta(c, bs);
+        uint64_t junk = 0x9E3779B97F4A7C15ull;
         for (;;) {
             if (c.sc->done) break;
-            sweep_cta(c);
+            // pricing 2: row keys do not survive between rounds (as in the
+            // round form, which stages them afresh): fill them with garbage
+            if (pricing == 2 && threadIdx.x == 0)
+                for (int i = 0; i < m; i++) { junk = junk * 6364136223846793005ull + 1442695040888963407ull; c.row_best[i] = junk; }
+            __syncthreads();
+            if (c.sc->pricing) sweep_partial_cta(c, bs);
+            else sweep_cta(c);
             pivot_round_cta(c, bs);
             if (threadIdx.x == 0) c.sc->rounds++;
             __syncthreads();
@@ -85,6 +95,7 @@ int main(int argc, char** argv) {
     const int count = atoi(argv[2]), lo = atoi(argv[3]), hi = atoi(argv[4]);
     const int first = atoi(argv[5]), last = atoi(argv[6]);
     const int mode = argc > 7 ? atoi(argv[7]) : 1;
+    const int pricing = argc > 8 ? atoi(argv[8]) : 0;
     std::vector<int32_t> ms(count), ns(count);
     flock_generate_sizes(seed, count, lo, hi, ms.data(), ns.data());
     int bad = 0;
@@ -93,7 +104,7 @@ int main(int argc, char** argv) {
         std::vector<int32_t> s(m), d(n), c((size_t)m * n);
         flock_generate(0, seed * 1000003ull + k + 1, m, n, 1, 1000, 100, 1000, s.data(), d.data(), c.data());
         Scalars r;
-        const int mism = solve_one(m, n, s.data(), d.data(), c.data(), mode, &r);
+        const int mism = solve_one(m, n, s.data(), d.data(), c.data(), mode, pricing, &r);
         const bool ok = r.status == 0 && r.cert == 0 && mism == 0;
         if (!ok) bad++;
         printf("k=%d m=%d n=%d obj=%lld rounds=%d pivots=%d status=%d cert=%d fail_site=%d barrier_mismatch=%d %s\n",

@@ -30,6 +30,7 @@ struct BatchArgs {
     int32_t bfs_method, mode, max_rounds;
     int32_t light;              // 1: stage only the per-step tree arrays (largest bucket)
     int32_t lift;               // 1: stage the binary-lifting table (parallel single pivots)
+    int32_t pricing;            // Scalars::pricing of every instance
 };
 
 // A served request's device region: byte offsets of its arrays (256-aligned).
@@ -86,6 +87,7 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.res = (int32_t*)k.G(4 * v);
     c.top2 = (int4*)k.G(16 * v);
     c.rescan = (int32_t*)k.G(4 * v);
+    c.prow = (int32_t*)k.G(4 * (size_t)kPPRows);
     c.bsum = (int64_t*)k.G(8 * v);
     c.csr_start = (int32_t*)k.G(4 * (v + 1));
     c.csr_adj = (int32_t*)k.G(8 * v);

@@ -232,6 +232,7 @@ __device__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch&
         memset(&z, 0, sizeof(z));
         z.max_rounds = a.max_rounds;
         z.mode = a.mode;
+        z.pricing = a.pricing;
         *c.sc = z;
     }
     __syncthreads();
@@ -336,7 +337,8 @@ __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch
     for (int r = 0; r < max_here; r++) {
         tree_recompute_cta(c, bs);
         if (!c.sc->done) {
-            sweep_cta(c);
+            if (c.sc->pricing) sweep_partial_cta(c, bs);
+            else sweep_cta(c);
             pivot_round_cta(c, bs);
         }
         if (threadIdx.x == 0) {
@@ -1068,6 +1070,7 @@ struct BatchRunner {
         a.lift = stage_lift(bmaxV[b], bmaxM[b], a.light != 0) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = pivot_mode(opt);
+        a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
         a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
         return a;
     }
@@ -1369,6 +1372,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.maxV = maxV; a.maxM = maxM;
     a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
     a.mode = pivot_mode(opt);
+    a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
     a.light = maxV > kBucketEdges[kNumBuckets - 2] ? 1 : 0;
     a.lift = stage_lift(maxV, maxM, a.light != 0) ? 1 : 0;
@@ -1453,6 +1457,7 @@ void flock_default_options(flock_options* opt) {
     opt->pivot_method = FLOCK_PIVOT_SWITCH;
     opt->max_iterations = 0;
     opt->verify = 1;
+    opt->pricing = FLOCK_PRICING_FULL;
 }
 
 const char* flock_last_error(void) { return flock::g_err.c_str(); }

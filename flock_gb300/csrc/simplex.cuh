@@ -346,15 +346,19 @@ __device__ __forceinline__ uint64_t narrow_row_key(const Ctx& c, int i, int j0, 
     return pack_i32(clamp32(r), (uint32_t)jw);
 }
 
-// CTA-local sweep: best (reduced cost, column) of every row into row_best[].
-// Rows are int4-vectorised (row pitch a multiple of 4, 16-byte aligned);
-// each lane keeps four row loads in flight.
-__device__ void sweep_cta(const Ctx& c) {
+// CTA-local sweep of the rows list[0..cnt) (all rows 0..cnt-1 when list is
+// null): best (reduced cost, column) of each into row_best[].  Rows are
+// int4-vectorised (row pitch a multiple of 4, 16-byte aligned); a warp takes
+// two rows per pass for more loads in flight.  A listed row outside the
+// instance is an internal error (recorded, skipped).
+__device__ void sweep_rows_cta(const Ctx& c, const int32_t* list, int cnt) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     if (!c.sc->narrow) {
-        for (int i = threadIdx.x >> 5; i < m; i += nw) {
+        for (int t = threadIdx.x >> 5; t < cnt; t += nw) {
+            const int i = list ? list[t] : t;
+            if (!FLOCK_IN(i, m)) { if (lane == 0) fail_check(c.sc, 19); continue; }
             const uint64_t k = row_best_exact(I.cost + (size_t)i * I.ldc, c.pot[i], c.pot + m, 0, n);
             if (lane == 0) c.row_best[i] = k;
         }
@@ -363,12 +367,14 @@ __device__ void sweep_cta(const Ctx& c) {
     }
     const int nfull = n >> 2, tail = n & 3;
     const int4* v4 = reinterpret_cast<const int4*>(c.v32);
-    // Two rows per warp pass (i and i + nw): twice the loads in flight.
-    for (int i = threadIdx.x >> 5; i < m; i += 2 * nw) {
-        const int i2 = i + nw;
-        const bool two = i2 < m;
+    for (int t = threadIdx.x >> 5; t < cnt; t += 2 * nw) {
+        const int t2 = t + nw;
+        const int i = list ? list[t] : t;
+        int i2 = t2 < cnt ? (list ? list[t2] : t2) : i;
+        if (!FLOCK_IN(i, m) || !FLOCK_IN(i2, m)) { if (lane == 0) fail_check(c.sc, 19); continue; }
+        const bool two = t2 < cnt;
         const int4* ra = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
-        const int4* rb = reinterpret_cast<const int4*>(I.cost + (size_t)(two ? i2 : i) * I.ldc);
+        const int4* rb = reinterpret_cast<const int4*>(I.cost + (size_t)i2 * I.ldc);
         int32_t av = INT32_MAX, aj = INT32_MAX, bv = INT32_MAX, bj = INT32_MAX;
         int q = lane;
         for (; q + 32 < nfull; q += 64) {
@@ -401,6 +407,77 @@ __device__ void sweep_cta(const Ctx& c) {
             if (lane == 0) c.row_best[i2] = kb;
         }
     }
+    __syncthreads();
+}
+
+__device__ void sweep_cta(const Ctx& c) { sweep_rows_cta(c, nullptr, c.I.m); }
+
+// Partial pricing (candidate rows).  A full sweep keeps the kPPRows rows
+// with the most negative best reduced costs in prow[] (chosen by a 32-bin
+// histogram threshold and then by row index, so the set depends only on the
+// values) and clears every other row's key; the next rounds re-price only
+// those rows, every other row's key cleared first (row_best need not survive
+// between rounds: the round form stages it afresh in every launch).  A full
+// sweep runs again when the candidates hold no negative reduced cost any more
+// or after kPPRefresh rounds, so a round without a negative key
+// (optimality) is always a full sweep.
+__device__ void sweep_partial_cta(const Ctx& c, BlockScratch& bs) {
+    const int m = c.I.m;
+    const int pn = c.sc->pp_n, age = c.sc->pp_age;
+    int full = pn <= 0 || pn > kPPRows || age >= kPPRefresh;
+    if (!full) {
+        for (int i = threadIdx.x; i < m; i += blockDim.x) c.row_best[i] = kNoKey;
+        __syncthreads();
+        sweep_rows_cta(c, c.prow, pn);
+        int neg = 0;
+        for (int t = threadIdx.x; t < pn; t += blockDim.x) {
+            const int i = c.prow[t];
+            if (FLOCK_IN(i, m)) neg |= key_val(c.row_best[i]) < 0;
+        }
+        full = !__syncthreads_or(neg);
+    }
+    if (full) {
+        sweep_rows_cta(c, nullptr, m);
+        int32_t rmin = 0;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
+        rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
+        const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
+        int last = -1;                                             // highest histogram bin kept
+        if (rmin < 0) {
+            if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
+            __syncthreads();
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int32_t v = key_val(c.row_best[i]);
+                if (v < 0) atomicAdd((unsigned long long*)&bs.red2[((int64_t)v - rmin) * 32 / span], 1ull);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint64_t cum = bs.red2[0];
+                int l = 0;
+                for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)kPPRows; b++) { cum += bs.red2[b]; l = b; }
+                bs.i[1] = l;
+            }
+            __syncthreads();
+            last = bs.i[1];
+        }
+        // candidates in row order: exclusive scan of the selection flags (cand[] as scratch)
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int32_t v = key_val(c.row_best[i]);
+            c.cand[i] = (v < 0 && ((int64_t)v - rmin) * 32 / span <= last) ? 1 : 0;
+        }
+        __syncthreads();
+        const int32_t total = block_exclusive_scan_i32(c.cand, m, bs);   // ends with a barrier
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int32_t v = key_val(c.row_best[i]);
+            const bool sel = v < 0 && ((int64_t)v - rmin) * 32 / span <= last;
+            const int slot = c.cand[i];
+            if (sel && slot < kPPRows) c.prow[slot] = i;
+            else c.row_best[i] = kNoKey;
+        }
+        if (threadIdx.x == 0) { c.sc->pp_n = min(total, kPPRows); c.sc->pp_age = 0; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c.sc->pp_age++;
     __syncthreads();
 }
 
@@ -615,10 +692,14 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     const int mode = c.sc->mode;
     if (threadIdx.x == 0) bs.i[0] = 0;
     __syncthreads();
+    // a candidate key whose column is outside the instance is an internal
+    // error: recorded, never used as an index
+    const uint32_t ncols = (uint32_t)I.n;
     if (mode == 0) {
         uint64_t best = kNoKey;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             const uint64_t k = c.row_best[i];
+            if (k != kNoKey && key_val(k) < 0 && key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
             if (k != kNoKey && key_val(k) < 0) {
                 const uint64_t P = pack_i32(key_val(k), (uint32_t)i);
                 best = P < best ? P : best;
@@ -637,6 +718,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         int32_t rmin = 0;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             const uint64_t k = c.row_best[i];
+            if (k != kNoKey && key_val(k) < 0 && key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
             if (k != kNoKey) rmin = min(rmin, key_val(k));
         }
         rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
@@ -646,7 +728,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
             __syncthreads();
             for (int i = threadIdx.x; i < m; i += blockDim.x) {
                 const uint64_t k = c.row_best[i];
-                if (k != kNoKey && key_val(k) < 0)
+                if (k != kNoKey && key_val(k) < 0 && key_idx(k) < ncols)
                     atomicAdd((unsigned long long*)&bs.red2[((int64_t)key_val(k) - rmin) * 32 / span], 1ull);
             }
             __syncthreads();
@@ -660,7 +742,8 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
             const int last = bs.i[1];
             for (int i = threadIdx.x; i < m; i += blockDim.x) {
                 const uint64_t k = c.row_best[i];
-                if (k != kNoKey && key_val(k) < 0 && ((int64_t)key_val(k) - rmin) * 32 / span <= last)
+                if (k != kNoKey && key_val(k) < 0 && key_idx(k) < ncols &&
+                    ((int64_t)key_val(k) - rmin) * 32 / span <= last)
                     c.cand[atomicAdd(&bs.i[0], 1)] = i;
             }
         }

@@ -70,12 +70,21 @@ enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1 };            /* BFS_METHOD nwc_ho
  * until one applies fewer than 10 pivots, then sequential ones
  * (switch/switch_model_parallel.cu:182-184). */
 enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2 };
+/* Pricing.  FULL: every round sweeps every cell (the reference's Dantzig rule,
+ * uv_model_parallel.cu:151-200).  PARTIAL (no counterpart in the reference):
+ * a full sweep keeps the 64 rows with the most negative reduced costs as
+ * candidates and the following rounds re-price only those rows, until they
+ * hold no negative reduced cost or 32 rounds have passed; optimality is only
+ * declared after a full sweep.  Batched and served forms; the plain solver
+ * always uses FULL.  The optimum is the same; the pivot sequence differs. */
+enum { FLOCK_PRICING_FULL = 0, FLOCK_PRICING_PARTIAL = 1 };
 
 typedef struct {
     int32_t bfs_method;      /* FLOCK_BFS_VOGEL (default) or FLOCK_BFS_NWC */
     int32_t pivot_method;    /* FLOCK_PIVOT_SWITCH (default), _PARALLEL or _SEQUENTIAL */
     int32_t max_iterations;  /* cap on pricing rounds; <= 0: 1 << 30 */
     int32_t verify;          /* nonzero: run the exact certificate check (default on) */
+    int32_t pricing;         /* FLOCK_PRICING_FULL (default) or FLOCK_PRICING_PARTIAL */
 } flock_options;
 
 /* Failures reported in flock_stats.status (bit set; 0 = optimal). */

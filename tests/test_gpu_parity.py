@@ -186,3 +186,23 @@ def test_batch_validation_first_failure():
     # the runner still works after a rejected batch
     out = fg.batch_solve(good)
     assert all(r.status == 0 and r.certified for r in out)
+
+
+@pytest.mark.parametrize("form", ["persistent", "round"])
+def test_batch_partial_pricing_all_buckets(form, monkeypatch):
+    """Partial pricing (candidate rows) in both batched forms on every size
+    bucket plus one instance above it: certified optima equal to full
+    pricing's.  The round form restages row keys in every launch, so it also
+    covers rounds whose non-candidate keys start out as garbage."""
+    monkeypatch.setenv("FLOCK_BATCH_FORM", form)
+    shapes = [(5, 7), (30, 30), (60, 60), (100, 150), (200, 300), (400, 500), (900, 1000),
+              (1500, 1444), (1000, 2072), (1600, 1600), (2100, 2000), (12, 40), (3, 3)]
+    insts = [fg.generate(0, 600 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(shapes)]
+    insts += fg.mixed_batch(23, 96, 10, 300)
+    insts.append(fg.config_instance("degenerate1000", 1, m=400, n=300))
+    full = fg.batch_solve(insts)
+    part = fg.batch_solve(insts, pricing="partial")
+    for k, (f, p) in enumerate(zip(full, part)):
+        assert f.status == 0 and f.certified, k
+        assert p.status == 0 and p.certified, (k, insts[k].m, insts[k].n, p.status, p.notes)
+        assert p.objective == f.objective, (k, insts[k].m, insts[k].n)
