@@ -243,7 +243,7 @@ class Result:
 PRICING = {"full": 0, "partial": 1}
 
 
-def _options(bfs="vogel", pivot="switch", max_iterations=0, verify=True, pricing="full") -> COptions:
+def _options(bfs="vogel", pivot="switch", max_iterations=0, verify=True, pricing="partial") -> COptions:
     return COptions(BFS[bfs], PIVOT[pivot], int(max_iterations), 1 if verify else 0, PRICING[pricing])
 
 
@@ -282,7 +282,7 @@ def vogel(inst: Instance) -> Tuple[np.ndarray, int]:
 
 
 def batch_solve(insts: Sequence[Instance], bfs: str = "vogel", pivot: str = "switch",
-                max_iterations: int = 0, verify: bool = True, pricing: str = "full") -> List[Result]:
+                max_iterations: int = 0, verify: bool = True, pricing: str = "partial") -> List[Result]:
     k = len(insts)
     arr = (CInstance * k)(*[x.c() for x in insts])
     total = sum(x.m + x.n - 1 for x in insts)
@@ -320,7 +320,7 @@ class Server:
         return int(lib().flock_server_request_bytes(m, n))
 
     def __init__(self, memory_budget_bytes: int = 40 << 30, max_inflight_batches: int = 16, max_batch: int = 512,
-                 bfs: str = "vogel", pivot: str = "switch", verify: bool = True, pricing: str = "full"):
+                 bfs: str = "vogel", pivot: str = "switch", verify: bool = True, pricing: str = "partial"):
         L = lib()
         cfg = CServerConfig()
         L.flock_default_server_config(ctypes.byref(cfg))

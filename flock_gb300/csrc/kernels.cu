@@ -1457,7 +1457,7 @@ void flock_default_options(flock_options* opt) {
     opt->pivot_method = FLOCK_PIVOT_SWITCH;
     opt->max_iterations = 0;
     opt->verify = 1;
-    opt->pricing = FLOCK_PRICING_FULL;
+    opt->pricing = FLOCK_PRICING_PARTIAL;
 }
 
 const char* flock_last_error(void) { return flock::g_err.c_str(); }

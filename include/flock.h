@@ -71,7 +71,8 @@ enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1 };            /* BFS_METHOD nwc_ho
  * (switch/switch_model_parallel.cu:182-184). */
 enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2 };
 /* Pricing.  FULL: every round sweeps every cell (the reference's Dantzig rule,
- * uv_model_parallel.cu:151-200).  PARTIAL (no counterpart in the reference):
+ * uv_model_parallel.cu:151-200).  PARTIAL (the default; no counterpart in the
+ * reference):
  * a full sweep keeps the 64 rows with the most negative reduced costs as
  * candidates and the following rounds re-price only those rows, until they
  * hold no negative reduced cost or 32 rounds have passed; optimality is only
@@ -84,7 +85,7 @@ typedef struct {
     int32_t pivot_method;    /* FLOCK_PIVOT_SWITCH (default), _PARALLEL or _SEQUENTIAL */
     int32_t max_iterations;  /* cap on pricing rounds; <= 0: 1 << 30 */
     int32_t verify;          /* nonzero: run the exact certificate check (default on) */
-    int32_t pricing;         /* FLOCK_PRICING_FULL (default) or FLOCK_PRICING_PARTIAL */
+    int32_t pricing;         /* FLOCK_PRICING_PARTIAL (default) or FLOCK_PRICING_FULL */
 } flock_options;
 
 /* Failures reported in flock_stats.status (bit set; 0 = optimal). */

@@ -158,7 +158,7 @@ def test_batch_forms_all_buckets(form, monkeypatch):
               (1500, 1444), (1000, 2072), (1600, 1600), (2000, 2000), (2100, 2000), (12, 40), (3, 3)]
     insts = [fg.generate(0, 500 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(shapes)]
     insts += fg.mixed_batch(17, 96, 10, 300)
-    out = fg.batch_solve(insts)
+    out = fg.batch_solve(insts, pricing="full")      # the plain solver prices fully
     for k, (inst, r) in enumerate(zip(insts, out)):
         assert r.status == 0 and r.certified, (k, inst.m, inst.n, r.status)
         if inst.m * inst.n <= 300 * 300 or k < len(shapes):
@@ -200,7 +200,7 @@ def test_batch_partial_pricing_all_buckets(form, monkeypatch):
     insts = [fg.generate(0, 600 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(shapes)]
     insts += fg.mixed_batch(23, 96, 10, 300)
     insts.append(fg.config_instance("degenerate1000", 1, m=400, n=300))
-    full = fg.batch_solve(insts)
+    full = fg.batch_solve(insts, pricing="full")
     part = fg.batch_solve(insts, pricing="partial")
     for k, (f, p) in enumerate(zip(full, part)):
         assert f.status == 0 and f.certified, k
