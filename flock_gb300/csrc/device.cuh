@@ -58,6 +58,7 @@ struct Scalars {
     int64_t objective;
     int64_t M;             // perturbation scale
     int64_t neg_cells;     // certificate: cells with negative reduced cost
+    int64_t cells;         // cost cells priced by the CTA sweeps (all rounds)
     int32_t last_winners;
     int32_t fail_site;     // first failed internal check (0: none), see fail_check
     int32_t narrow;        // 1: every live column dual fits the int32 sweep (v32 valid)

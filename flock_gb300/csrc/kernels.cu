@@ -1436,6 +1436,18 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
     return bad.load() ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
 }
 
+// Benchmark hook: cost cells priced by the CTA sweeps of the last batch
+// (every instance solved by the batched kernels).
+int batch_cells(int64_t* cells) {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    if (!g_batch || !cells) return FLOCK_ERR_ARG;
+    int64_t t = 0;
+    for (int k = 0; k < g_batch->count; k++)
+        if (g_batch->V_of[k] <= kMaxStagedV) t += g_batch->h_sc.as<Scalars>()[k].cells;
+    *cells = t;
+    return FLOCK_OK;
+}
+
 // Device-only timing hook for the benchmark: solve the last staged batch
 // again with its inputs already resident.  Returns the kernel time in ms.
 int batch_rerun_device(float* ms, int32_t* launches) {
@@ -1481,6 +1493,10 @@ int flock_batch_solve(int32_t count, const flock_instance* insts, const flock_op
 /* Benchmark hook (not part of the public header): rerun the last batch with
  * its inputs resident on the device and report the device time. */
 int flock_bench_batch_rerun(float* ms, int32_t* launches) { return flock::batch_rerun_device(ms, launches); }
+
+/* Benchmark hook: cost cells priced by the batched kernels' sweeps in the last
+ * batch (after a re-solve, the re-solve's count). */
+int flock_bench_batch_cells(int64_t* cells) { return flock::batch_cells(cells); }
 
 /* Benchmark hook: average device time of the fused reduced-cost sweep on an
  * m x n matrix (random costs and duals, inputs resident). */

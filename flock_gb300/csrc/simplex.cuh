@@ -355,6 +355,7 @@ __device__ void sweep_rows_cta(const Ctx& c, const int32_t* list, int cnt) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
     const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) c.sc->cells += (int64_t)cnt * n;
     if (!c.sc->narrow) {
         for (int t = threadIdx.x >> 5; t < cnt; t += nw) {
             const int i = list ? list[t] : t;
