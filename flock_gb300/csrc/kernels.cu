@@ -1054,6 +1054,16 @@ struct BatchRunner {
             std::lock_guard<std::mutex> lk(g_tune_mu);
             t = g_tuned_ok[b] ? g_tuned[b] : default_cfg(bmaxV[b]);
         }
+        // FLOCK_BATCH_THREADS="b:t,b:t": block size of bucket b (diagnostics).
+        if (const char* bt = getenv("FLOCK_BATCH_THREADS")) {
+            for (const char* p = bt; *p;) {
+                int bb = -1, tt = 0, used = 0;
+                if (sscanf(p, "%d:%d%n", &bb, &tt, &used) != 2) break;
+                if (bb == b && (tt == 32 || tt == 64 || tt == 128 || tt == 256 || tt == 512 || tt == 1024)) t.threads = tt;
+                p += used;
+                if (*p == ',') p++;
+            }
+        }
         const char* f = getenv("FLOCK_BATCH_FORM");
         if (f && !strcmp(f, "round")) { t.persistent = 0; t.threads = std::min(std::max(t.threads, 128), 256); }
         if (f && !strcmp(f, "persistent")) t.persistent = 1;
@@ -1274,7 +1284,8 @@ struct BatchRunner {
     }
 
     // Autotune each bucket with enough instances: the bucket alone is solved
-    // once per candidate configuration (inputs resident) and the fastest wins.
+    // once per candidate configuration (inputs resident) and the fastest wins;
+    // then the block sizes are refined with all buckets running together.
     // Candidates: the persistent form at three block sizes scaled to the
     // bucket's largest instance, and the round form at 128/256 threads.
     int autotune() {
@@ -1327,6 +1338,50 @@ struct BatchRunner {
             g_tuned[b] = best;
             g_tuned_ok[b] = true;
         }
+        return tune_jointly();
+    }
+
+    // Second stage: the buckets share the GPU in a real solve, where a block
+    // size that is fastest for a bucket alone (its longest instance finishes
+    // first) can cost throughput.  One coordinate-descent pass over the
+    // buckets, largest first, tries each persistent bucket's block sizes with
+    // every bucket running; a change is kept when the whole batch gets at
+    // least 2 % faster.
+    int tune_jointly() {
+        TuneCfg cur[kNumBuckets];
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            for (int b = 0; b < kNumBuckets; b++) cur[b] = g_tuned_ok[b] ? g_tuned[b] : default_cfg(bmaxV[b]);
+        }
+        int rc;
+        float best_ms = 0;
+        if ((rc = run_device(cur, &best_ms))) return rc;
+        if ((rc = run_device(cur, &best_ms))) return rc;
+        for (int b = kNumBuckets - 1; b >= 0; b--) {
+            const int nb = bstart[b + 1] - bstart[b];
+            if (nb < 32 || !cur[b].persistent) continue;
+            const int V = bmaxV[b];
+            const int t0 = V <= 128 ? 32 : V <= 256 ? 64 : V <= 512 ? 128 : 256;
+            for (int t = t0; t <= 4 * t0; t *= 2) {
+                if (t == cur[b].threads) continue;
+                TuneCfg trial[kNumBuckets];
+                for (int x = 0; x < kNumBuckets; x++) trial[x] = cur[x];
+                trial[b].threads = t;
+                float ms = 0;
+                if ((rc = run_device(trial, &ms))) return rc;
+                if (getenv("FLOCK_TUNE_LOG"))
+                    fprintf(stderr, "  joint: bucket %d threads=%d: %.3f ms (current %.3f ms)\n", b, t, ms, best_ms);
+                if (ms < 0.98f * best_ms) { best_ms = ms; cur[b] = trial[b]; }
+            }
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (int b = 0; b < kNumBuckets; b++)
+            if (g_tuned_ok[b]) g_tuned[b] = cur[b];
+        if (getenv("FLOCK_TUNE_LOG"))
+            for (int b = 0; b < kNumBuckets; b++)
+                if (g_tuned_ok[b])
+                    fprintf(stderr, "flock autotune (joint): bucket %d: %s threads=%d\n", b,
+                            cur[b].persistent ? "persistent" : "rounds", cur[b].threads);
         return FLOCK_OK;
     }
 };
