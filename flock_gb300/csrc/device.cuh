@@ -39,6 +39,11 @@ constexpr int64_t kDeadPot = -(int64_t(1) << 61);   // dual of a zero-demand col
 // (zero-demand) column is stored as kDead32 and re-checked exactly.
 constexpr int32_t kDead32 = -((1 << 30) - 1);
 constexpr uint64_t kNoKey = ~0ull;
+// Vertices a thread handles at once in the pointer-jumping and
+// k-th-ancestor passes (loads of independent vertices interleaved): the
+// default of the batched kernels (64 registers) and the plain solver's.
+constexpr int kJump = 2;
+constexpr int kJumpPlain = 4;
 constexpr int kPPRows = 64;      // partial pricing: candidate rows kept by a full sweep
 constexpr int kPPRefresh = 32;   // partial pricing: rounds between full sweeps
 

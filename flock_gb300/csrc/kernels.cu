@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method) {
     }
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
     sf_init_cta(c, bs);
-    if (!c.sc->done) tree_recompute_cta(c, bs);
+    if (!c.sc->done) tree_recompute_cta<kJumpPlain>(c, bs);
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
@@ -126,13 +126,13 @@ static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile);
 __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
     __shared__ BlockScratch bs;
     if (c.sc->done) return;
-    pivot_round_cta(c, bs);
+    pivot_round_cta<kJumpPlain>(c, bs);
     if (threadIdx.x == 0) {
         c.sc->rounds++;
         if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
     }
     __syncthreads();
-    if (!c.sc->done) tree_recompute_cta(c, bs);
+    if (!c.sc->done) tree_recompute_cta<kJumpPlain>(c, bs);
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 

@@ -252,6 +252,7 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
 
 // --------------------------------------------------------------- duals ------
 // depth[] and pot[] from parent[] by pointer jumping: pot[v] = acc + (-1)^len pot[anc].
+template <int J = kJump>
 __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int V = I.m + I.n;
@@ -275,17 +276,42 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
     __syncthreads();
     for (int it = 0; it < max_it && pending; it++) {
         int mine = 0;
-        for (int v = threadIdx.x; v < V; v += blockDim.x) {
-            const int a = aA[v];
-            if (a < 0 || a == root) { aB[v] = a; lB[v] = lA[v]; xB[v] = xA[v]; continue; }
-            if (!FLOCK_IN(a, V)) { fail_check(c.sc, 21); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
-            const int aa = aA[a];
-            if (!FLOCK_IN(aa, V)) { fail_check(c.sc, 22); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
-            const int la = lA[v];
-            aB[v] = aa;
-            lB[v] = la + lA[a];
-            xB[v] = xA[v] + ((la & 1) ? -xA[a] : xA[a]);
-            mine |= (aa != root);
+        // J vertices per thread per step with their loads interleaved
+        // (a thread's vertices are independent chains): when V exceeds the
+        // block, one dependent-load latency covers all of them.
+        for (int base = threadIdx.x; base < V; base += J * blockDim.x) {
+            int vv[J], a[J], kind[J], aa[J], la[J], lb[J];
+            int64_t xa[J], xb[J];
+            #pragma unroll
+            for (int u = 0; u < J; u++) {
+                vv[u] = base + u * blockDim.x;
+                a[u] = vv[u] < V ? aA[vv[u]] : 0;
+            }
+            #pragma unroll
+            for (int u = 0; u < J; u++) {
+                const int v = vv[u], x = a[u];
+                // 0: no vertex, 1: at the root or dead, 2: bad ancestor, 3: jump
+                kind[u] = v >= V ? 0 : (x < 0 || x == root) ? 1 : !FLOCK_IN(x, V) ? 2 : 3;
+                la[u] = kind[u] == 1 || kind[u] == 3 ? lA[v] : 0;
+                xa[u] = kind[u] == 1 || kind[u] == 3 ? xA[v] : 0;
+                aa[u] = kind[u] == 3 ? aA[x] : 0;
+                lb[u] = kind[u] == 3 ? lA[x] : 0;
+                xb[u] = kind[u] == 3 ? xA[x] : 0;
+            }
+            #pragma unroll
+            for (int u = 0; u < J; u++) {
+                const int v = vv[u];
+                if (kind[u] == 1) { aB[v] = a[u]; lB[v] = la[u]; xB[v] = xa[u]; }
+                else if (kind[u] == 2 || (kind[u] == 3 && !FLOCK_IN(aa[u], V))) {
+                    fail_check(c.sc, kind[u] == 2 ? 21 : 22);
+                    aB[v] = root; lB[v] = 0; xB[v] = 0;
+                } else if (kind[u] == 3) {
+                    aB[v] = aa[u];
+                    lB[v] = la[u] + lb[u];
+                    xB[v] = xa[u] + ((la[u] & 1) ? -xb[u] : xb[u]);
+                    mine |= (aa[u] != root);
+                }
+            }
         }
         pending = __syncthreads_or(mine);
         if (lifting) { aA = aB; aB = c.lift + (size_t)(it + 2) * V; }
@@ -606,22 +632,56 @@ __device__ __forceinline__ uint64_t oflow(int64_t f) { return (uint64_t)f ^ 0x80
 // entering cell's endpoint is re-hung, as cycle_apply does.  Uses claim[]
 // (side marks) and len1/acc1 (new parents and flows) as scratch.  Returns
 // 1 if the pivot was applied (block-uniform).
+template <int J = kJump>
 __device__ int single_pivot_lift(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
     const int m = c.I.m;
     const int dk = c.depth[k], dl = c.depth[l];
     uint64_t mk = kNoKey, ml = kNoKey;
-    for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        int side = 0;                              // 1: k side, 2: l side
-        if (c.parent[v] >= 0) {
-            const int dv = c.depth[v];
-            const bool on_k = dv <= dk && kth_anc(c, V, k, dk - dv) == v;
-            const bool on_l = dv <= dl && kth_anc(c, V, l, dl - dv) == v;
-            if (on_k != on_l) side = on_k ? 1 : 2;
+    int lbad = 0;
+    // J vertices per thread at a time; their k-th ancestor lookups go
+    // level by level together (independent chains, one latency per level).
+    for (int base = threadIdx.x; base < V; base += J * blockDim.x) {
+        int vv[J], rk[J], rl[J], xk[J], xl[J];
+        #pragma unroll
+        for (int u = 0; u < J; u++) {
+            const int v = base + u * blockDim.x;
+            vv[u] = v;
+            rk[u] = rl[u] = -1;                     // -1: no test; else steps still to climb
+            xk[u] = k; xl[u] = l;
+            if (v < V && c.parent[v] >= 0) {
+                const int dv = c.depth[v];
+                if (dv <= dk) rk[u] = dk - dv;
+                if (dv <= dl) rl[u] = dl - dv;
+            }
         }
-        c.claim[v] = (uint64_t)side;
-        if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
-        if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
+        for (int j = 0; j < c.lift_cap; j++) {
+            int more = 0;
+            #pragma unroll
+            for (int u = 0; u < J; u++) {
+                if (rk[u] > 0) {
+                    if (rk[u] & 1) { xk[u] = c.lift[(size_t)j * V + xk[u]]; if (!FLOCK_IN(xk[u], V)) { lbad = 1; rk[u] = -1; } }
+                    if (rk[u] > 0) { rk[u] >>= 1; more |= rk[u] > 0; }
+                }
+                if (rl[u] > 0) {
+                    if (rl[u] & 1) { xl[u] = c.lift[(size_t)j * V + xl[u]]; if (!FLOCK_IN(xl[u], V)) { lbad = 1; rl[u] = -1; } }
+                    if (rl[u] > 0) { rl[u] >>= 1; more |= rl[u] > 0; }
+                }
+            }
+            if (!more) break;
+        }
+        #pragma unroll
+        for (int u = 0; u < J; u++) {
+            const int v = vv[u];
+            if (v >= V) continue;
+            const bool on_k = rk[u] == 0 && xk[u] == v;
+            const bool on_l = rl[u] == 0 && xl[u] == v;
+            const int side = on_k != on_l ? (on_k ? 1 : 2) : 0;   // 1: k side, 2: l side
+            c.claim[v] = (uint64_t)side;
+            if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
+            if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
+        }
     }
+    if (lbad) fail_check(c.sc, 16);
     mk = block_min_u64(mk, bs);
     ml = block_min_u64(ml, bs);
     const bool lside = ml <= mk;                   // uniform
@@ -687,6 +747,7 @@ constexpr int kMaxCand = 32;
 constexpr int kSwitchPivots = 10;
 
 // One pricing round after sweep: choose candidates, claim, apply.
+template <int J = kJump>
 __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int m = I.m, V = m + I.n;
@@ -758,7 +819,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     }
     if (ncand == 1 && c.lift_cap > 0) {
         const int i = c.cand[0];
-        const int ok = single_pivot_lift(c, bs, i, m + (int)key_idx(c.row_best[i]), V);
+        const int ok = single_pivot_lift<J>(c, bs, i, m + (int)key_idx(c.row_best[i]), V);
         if (threadIdx.x == 0) {
             c.sc->pivots += ok;
             c.sc->ncand = 1;
