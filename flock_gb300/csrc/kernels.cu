@@ -1471,9 +1471,12 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
     BatchRunner& R = *g_batch;
     int rc = R.prepare(cnt, insts, opt);
     if (rc) return rc;
+    const auto t1 = std::chrono::steady_clock::now();
     const char* at = getenv("FLOCK_AUTOTUNE");
     if (!at || strcmp(at, "0") != 0) { if ((rc = R.autotune())) return rc; }
+    const auto t2 = std::chrono::steady_clock::now();
     if ((rc = R.solve_all())) return rc;
+    const auto t3 = std::chrono::steady_clock::now();
     const float ms = R.last_ms;
     std::vector<int64_t> off(cnt);
     int64_t o = 0;
@@ -1488,6 +1491,14 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
         if (stats) stats[k] = s;
         if (s.status) bad.store(1);
     });
+    if (getenv("FLOCK_TIMING")) {
+        auto ms_ = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double, std::milli>(b - a).count();
+        };
+        fprintf(stderr, "flock_batch_solve: validate+layout %.2f ms, autotune %.2f ms, stage+solve+download %.2f ms "
+                        "(device %.2f ms), collect %.2f ms\n", ms_(t0, t1), ms_(t1, t2), ms_(t2, t3), ms, 
+                ms_(t3, std::chrono::steady_clock::now()));
+    }
     return bad.load() ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
 }
 
