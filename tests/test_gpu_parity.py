@@ -206,3 +206,26 @@ def test_batch_partial_pricing_all_buckets(form, monkeypatch):
         assert f.status == 0 and f.certified, k
         assert p.status == 0 and p.certified, (k, insts[k].m, insts[k].n, p.status, p.notes)
         assert p.objective == f.objective, (k, insts[k].m, insts[k].n)
+
+
+@pytest.mark.parametrize("bfs,pivot,pricing", [("nwc", "switch", "partial"), ("vogel", "sequential", "full"),
+                                               ("vogel", "parallel", "partial"), ("nwc", "parallel", "full")])
+def test_batch_option_combinations(bfs, pivot, pricing):
+    """Every start / pivot / pricing combination of the batched form gives the
+    plain solver's certified optimum on a mixed batch."""
+    insts = fg.mixed_batch(41, 80, 10, 400)
+    out = fg.batch_solve(insts, bfs=bfs, pivot=pivot, pricing=pricing)
+    for k, (inst, r) in enumerate(zip(insts, out)):
+        assert r.status == 0 and r.certified, (k, inst.m, inst.n, r.status)
+        assert r.objective == fg.solve(inst).objective, (k, inst.m, inst.n)
+
+
+def test_batch_iteration_cap_reported():
+    """A round cap below what an instance needs stops it with ST_ITER_CAP and
+    FLOCK_ERR_NOT_OPTIMAL, without disturbing the instances that finish."""
+    big = fg.generate(0, 42, 200, 220, 1, 1000, 100, 1000)
+    small = fg.generate(0, 43, 3, 3, 1, 1000, 100, 1000)
+    need = fg.solve(small).iterations
+    out = fg.batch_solve([big, small], max_iterations=need + 2, pricing="full")
+    assert out[0].status & fg.ST_ITER_CAP and not out[0].certified
+    assert out[1].status == 0 and out[1].certified and out[1].objective == fg.solve(small).objective
