@@ -28,7 +28,8 @@ struct BatchArgs {
     int32_t* active;            // round kernel: instances still running after the round
     int32_t maxV, maxM;         // largest instance of the launch (shared-memory staging size)
     int32_t bfs_method, mode, max_rounds;
-    int32_t stage;              // shared-memory staging variant of the rounds (kStage*)
+    int32_t light;              // 1: stage only the per-step tree arrays (largest bucket)
+    int32_t lift;               // 1: stage the binary-lifting table (parallel single pivots)
     int32_t pricing;            // Scalars::pricing of every instance
 };
 

@@ -268,44 +268,33 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
     }
 }
 
-// Shared-memory staging of the arrays a pricing round touches, in four
-// variants (compile-time, so that every staged pointer is carved from the
-// extern shared base and the compiler emits shared loads and atomics, not
-// generic ones; staged_bytes() below follows the same order):
-//   kStageFull      parent, depth, flow, row keys, duals, int32 duals, claims,
-//                   pointer-jumping buffers; the binary-lifting table stays in
-//                   the instance's global working set
-//   kStageFullLift  the same plus the lifting table
-//   kStageLeanLift  parent, depth, row keys, int32 duals and the lifting table;
-//                   flows, duals, claims and the jumping accumulators global
-//                   (instances too large for kStageFullLift)
-//   kStageLight     parent, depth, flow, row keys, duals, int32 duals; the rest
-//                   global (the largest bucket)
-enum : int { kStageFull = 0, kStageFullLift = 1, kStageLeanLift = 2, kStageLight = 3 };
-
-template <int kStage>
+// Shared-memory staging of the arrays every pivot step touches.  Light
+// staging (the largest bucket) keeps the pointer-jumping buffers and the
+// edge claims in the instance's global working set.  The binary-lifting
+// table (which replaces the two pointer-jumping ancestor buffers and makes
+// single-candidate pivots fully parallel) is staged when it fits (kLift),
+// else it stays in the global working set.  Every pointer is carved
+// from the extern shared base and the flags are compile-time constants, so
+// the compiler knows they address shared memory (shared loads and atomics
+// rather than generic ones).  staged_bytes() below follows the same order.
+template <bool kLight, bool kLift>
 __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
     Carver k{nullptr, 0, smem, 0};
     c.parent = (int32_t*)k.S(4 * (size_t)V);
     c.depth = (int32_t*)k.S(4 * (size_t)V);
-    if (kStage != kStageLeanLift) c.flow = (int64_t*)k.S(8 * (size_t)V);
+    c.flow = (int64_t*)k.S(8 * (size_t)V);
     c.row_best = (uint64_t*)k.S(8 * (size_t)M);
-    if (kStage != kStageLeanLift) c.pot = (int64_t*)k.S(8 * (size_t)V);
+    c.pot = (int64_t*)k.S(8 * (size_t)V);
     c.v32 = (int32_t*)k.S(4 * (size_t)V);
-    if (kStage == kStageLight) return;
-    if (kStage == kStageLeanLift) {
-        c.lift_cap = lift_levels(V);
-        c.lift = (int32_t*)k.S(4 * (size_t)V * c.lift_cap);
-        c.anc0 = c.lift;
-        c.anc1 = c.lift;
-        return;
-    }
+    // Without kLift the lifting table stays in the instance's global working
+    // set (carved there by batch_ctx, stride and level count of the instance).
+    if (kLight) return;
     c.claim = (uint64_t*)k.S(8 * (size_t)V);
     c.len0 = (int32_t*)k.S(4 * (size_t)V);
     c.len1 = (int32_t*)k.S(4 * (size_t)V);
     c.acc0 = (int64_t*)k.S(8 * (size_t)V);
     c.acc1 = (int64_t*)k.S(8 * (size_t)V);
-    if (kStage == kStageFullLift) {
+    if (kLift) {
         c.lift_cap = lift_levels(V);
         c.lift = (int32_t*)k.S(4 * (size_t)V * c.lift_cap);
     }
@@ -313,17 +302,13 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     c.anc1 = c.lift;
 }
 
-inline size_t staged_bytes(int V, int M, int stage) {
+inline size_t staged_bytes(int V, int M, bool light, bool lift) {
     Carver k{nullptr, 0, (unsigned char*)16, 0};
-    k.S(4 * (size_t)V); k.S(4 * (size_t)V);
-    if (stage != kStageLeanLift) k.S(8 * (size_t)V);
-    k.S(8 * (size_t)M);
-    if (stage != kStageLeanLift) k.S(8 * (size_t)V);
+    k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
     k.S(4 * (size_t)V);
-    if (stage == kStageLeanLift) k.S(4 * (size_t)V * lift_levels(V));
-    if (stage == kStageFull || stage == kStageFullLift) {
+    if (!light) {
         k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
-        if (stage == kStageFullLift) k.S(4 * (size_t)V * lift_levels(V));
+        if (lift) k.S(4 * (size_t)V * lift_levels(V));
     }
     return (k.so + 15) & ~size_t(15);
 }
@@ -331,30 +316,23 @@ inline size_t staged_bytes(int V, int M, int stage) {
 // Largest dynamic shared memory a staged launch may use.
 constexpr size_t kStageSmemMax = 226 * 1024;
 
-// Staging of a launch whose largest instance is maxV x (rows maxM): light for
-// the largest bucket, else the lifting table with everything (when it fits),
-// else the lean variant with the table (when it fits), else no table.
-inline int stage_for(int maxV, int maxM, bool light) {
-    if (light) return kStageLight;
-    if (staged_bytes(maxV, maxM, kStageFullLift) <= kStageSmemMax) return kStageFullLift;
-    if (staged_bytes(maxV, maxM, kStageLeanLift) <= kStageSmemMax) return kStageLeanLift;
-    return kStageFull;
+// Staging of a launch whose largest instance is maxV x (rows maxM): light
+// for the largest bucket, the lifting table whenever it fits.
+inline bool stage_lift(int maxV, int maxM, bool light) {
+    return !light && staged_bytes(maxV, maxM, false, true) <= kStageSmemMax;
 }
 
 // Pricing rounds of one instance with its tree staged in shared memory:
 // `max_here` rounds at most (1 for the round-kernel form), or until done.
-template <int kStage>
+template <bool kLight, bool kLift>
 __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs, unsigned char* smem,
                             int max_here) {
     Ctx g;
     batch_ctx(a, d, g);
     Ctx c = g;
-    stage_hot<kStage>(c, smem, a.maxV, a.maxM);
+    stage_hot<kLight, kLift>(c, smem, a.maxV, a.maxM);
     const int V = d.m + d.n;
-    for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        c.parent[v] = g.parent[v];
-        if (kStage != kStageLeanLift) c.flow[v] = g.flow[v];
-    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
     __syncthreads();
     for (int r = 0; r < max_here; r++) {
         tree_recompute_cta(c, bs);
@@ -372,8 +350,7 @@ __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch
         if (c.sc->done) break;       // written before the barrier: every thread reads the same value
     }
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        g.parent[v] = c.parent[v];
-        if (kStage != kStageLeanLift) { g.flow[v] = c.flow[v]; g.pot[v] = c.pot[v]; }
+        g.parent[v] = c.parent[v]; g.flow[v] = c.flow[v]; g.pot[v] = c.pot[v];
     }
     __syncthreads();
 }
@@ -396,12 +373,9 @@ __global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) continue;
         if (d.sc->done) continue;          // every thread reads the same value
-        switch (a.stage) {
-            case kStageLight: brounds_one<kStageLight>(a, d, bs, smem, 1); break;
-            case kStageLeanLift: brounds_one<kStageLeanLift>(a, d, bs, smem, 1); break;
-            case kStageFullLift: brounds_one<kStageFullLift>(a, d, bs, smem, 1); break;
-            default: brounds_one<kStageFull>(a, d, bs, smem, 1); break;
-        }
+        if (a.light) brounds_one<true, false>(a, d, bs, smem, 1);
+        else if (a.lift) brounds_one<false, true>(a, d, bs, smem, 1);
+        else brounds_one<false, false>(a, d, bs, smem, 1);
     }
 }
 
@@ -438,12 +412,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
         if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); publish_done(d); continue; }
         bsetup_one(a, d, bs);
         if (!d.sc->done) {
-            switch (a.stage) {
-                case kStageLight: brounds_one<kStageLight>(a, d, bs, smem, 1 << 30); break;
-                case kStageLeanLift: brounds_one<kStageLeanLift>(a, d, bs, smem, 1 << 30); break;
-                case kStageFullLift: brounds_one<kStageFullLift>(a, d, bs, smem, 1 << 30); break;
-                default: brounds_one<kStageFull>(a, d, bs, smem, 1 << 30); break;
-            }
+            if (a.light) brounds_one<true, false>(a, d, bs, smem, 1 << 30);
+            else if (a.lift) brounds_one<false, true>(a, d, bs, smem, 1 << 30);
+            else brounds_one<false, false>(a, d, bs, smem, 1 << 30);
         }
         bfinal_one(a, d, bs);
         publish_done(d);
@@ -862,8 +833,8 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 // -------------------------------------------------------- batched solver ---
 // Size buckets by V = m + n.  Instances above the last edge run on the plain
 // path (their staged tree would not fit in shared memory).
-// The last bucket stages lightly (staged_bytes(4096, 4095, light) = 144 KB);
-// the others stage at least fully (staged_bytes(2944, 2943, full) fits 226 KB).
+// The last bucket stages lightly (staged_bytes(4096, 4095, true) = 144 KB);
+// the others stage fully (staged_bytes(2944, 2943, false) fits 226 KB).
 static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944, 4096};
 static const int kNumBuckets = 8;
 static const int kMaxStagedV = 4096;
@@ -1105,7 +1076,8 @@ struct BatchRunner {
         a.count = bstart[b + 1] - bstart[b];
         a.next = nullptr; a.active = nullptr;
         a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
-        a.stage = stage_for(bmaxV[b], bmaxM[b], bucket_light(b));
+        a.light = bucket_light(b) ? 1 : 0;
+        a.lift = stage_lift(bmaxV[b], bmaxM[b], a.light != 0) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = pivot_mode(opt);
         a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
@@ -1126,7 +1098,7 @@ struct BatchRunner {
     // Pricing rounds of bucket b as a CUDA graph: `chunk` x (zero the
     // counters, one k_bround launch).
     int capture_rounds(int b, const TuneCfg& t, cudaGraphExec_t* exec) {
-        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], stage_for(bmaxV[b], bmaxM[b], bucket_light(b)));
+        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
         const int grid = grid_for(b, t, smem, (const void*)k_bround);
         cudaStream_t s = st[b];
         cudaGraph_t g;
@@ -1165,7 +1137,7 @@ struct BatchRunner {
             a.next = ctr(b);
             if (stage && (rc = stage_bucket(b, st[b]))) return rc;
             if (cfg[b].persistent) {
-                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], stage_for(bmaxV[b], bmaxM[b], bucket_light(b)));
+                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
                 FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
                 const void* fn = bsolve_fn(cfg[b].threads);
                 void* kargs[] = {&a};
@@ -1457,8 +1429,9 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.mode = pivot_mode(opt);
     a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
-    a.stage = stage_for(maxV, maxM, maxV > kBucketEdges[kNumBuckets - 2]);
-    const size_t smem = staged_bytes(maxV, maxM, a.stage);
+    a.light = maxV > kBucketEdges[kNumBuckets - 2] ? 1 : 0;
+    a.lift = stage_lift(maxV, maxM, a.light != 0) ? 1 : 0;
+    const size_t smem = staged_bytes(maxV, maxM, a.light != 0, a.lift != 0);
     const int threads = serve_threads(maxV);
     const void* fn = bsolve_fn(threads);
     int per_sm = 0;
