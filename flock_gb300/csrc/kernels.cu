@@ -136,6 +136,264 @@ __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
+// ------------------------------------------------- grid pivot round -------
+// The plain solver's pivot round for large instances, spread over the whole
+// GPU: one pivot per round (Dantzig's rule: the most negative row key, first
+// row among ties), every step a grid-wide kernel, the kernel boundaries the
+// only synchronisation.  The steps follow single_pivot_lift and
+// tree_recompute_cta exactly (same cycle membership test, tie rules, re-hang
+// and pointer-jumping passes); a pass kernel whose predecessor left no vertex
+// pending returns at once, so a round costs the passes its tree needs.
+struct GridPivot {
+    uint64_t best;          // entering candidate: (reduced cost, row)
+    uint64_t mk, ml;        // per side: minimum order-preserving flow
+    uint64_t qk, ql;        // per side: leaving edge (depth << 32 | child)
+    int32_t wide;           // a column dual left the int32 window
+    int32_t pend[48];       // pointer-jumping pass it left vertices pending
+};
+
+constexpr int kGridPivotV = 4096;     // plain instances with m + n >= this use the grid round
+
+__global__ void __launch_bounds__(1024, 1) k_gselect(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    if (c.sc->done) return;
+    const int m = c.I.m;
+    const uint32_t ncols = (uint32_t)c.I.n;
+    uint64_t best = kNoKey;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const uint64_t k = c.row_best[i];
+        if (k != kNoKey && key_val(k) < 0) {
+            if (key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
+            const uint64_t P = pack_i32(key_val(k), (uint32_t)i);
+            best = P < best ? P : best;
+        }
+    }
+    best = block_min_u64(best, bs);
+    if (threadIdx.x == 0) {
+        gp->best = best;
+        gp->mk = gp->ml = kNoKey;
+        gp->qk = 0;
+        gp->ql = kNoKey;
+        gp->wide = 0;
+        c.sc->rounds++;
+        c.sc->ncand = best == kNoKey ? 0 : 1;
+        if (best == kNoKey) c.sc->done = 1;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    if (c.sc->done) return;
+    const int m = c.I.m, V = m + c.I.n;
+    const int k = (int)key_idx(gp->best);
+    const int l = m + (int)key_idx(c.row_best[k]);
+    const int dk = c.depth[k], dl = c.depth[l];
+    uint64_t mk = kNoKey, ml = kNoKey;
+    int lbad = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        int side = 0;
+        if (c.parent[v] >= 0) {
+            const int dv = c.depth[v];
+            int xk = dv <= dk ? kth_anc(c, V, k, dk - dv) : -1;
+            int xl = dv <= dl ? kth_anc(c, V, l, dl - dv) : -1;
+            if ((dv <= dk && xk < 0) || (dv <= dl && xl < 0)) lbad = 1;
+            const bool on_k = xk == v, on_l = xl == v;
+            if (on_k != on_l) side = on_k ? 1 : 2;
+        }
+        c.claim[v] = (uint64_t)side;
+        if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
+        if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
+    }
+    mk = block_min_u64(mk, bs);
+    ml = block_min_u64(ml, bs);
+    lbad = __syncthreads_or(lbad);
+    if (threadIdx.x == 0) {
+        if (mk != kNoKey) atomicMin((unsigned long long*)&gp->mk, (unsigned long long)mk);
+        if (ml != kNoKey) atomicMin((unsigned long long*)&gp->ml, (unsigned long long)ml);
+        if (lbad) fail_check(c.sc, 16);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    if (c.sc->done) return;
+    const int m = c.I.m, V = m + c.I.n;
+    const bool lside = gp->ml <= gp->mk;
+    const uint64_t fmin = lside ? gp->ml : gp->mk;
+    if (fmin == kNoKey) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
+        return;
+    }
+    uint64_t pick = lside ? kNoKey : 0ull;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const uint64_t sd = c.claim[v];
+        if ((lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) && oflow(c.flow[v]) == fmin) {
+            const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
+            if (lside) pick = key < pick ? key : pick;
+            else pick = key > pick ? key : pick;
+        }
+    }
+    pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
+    if (threadIdx.x == 0) {
+        if (lside && pick != kNoKey) atomicMin((unsigned long long*)&gp->ql, (unsigned long long)pick);
+        if (!lside && pick != 0) atomicMax((unsigned long long*)&gp->qk, (unsigned long long)pick);
+    }
+}
+
+// The pivot's parameters, read by every thread of the apply and commit steps.
+struct GridPivotArgs {
+    bool ok, lside;
+    int q, e, other, de, dq;
+    uint64_t eside;
+    int64_t th;
+};
+
+__device__ __forceinline__ GridPivotArgs grid_pivot_args(const Ctx& c, const GridPivot* gp) {
+    GridPivotArgs p;
+    const int m = c.I.m, V = m + c.I.n;
+    p.lside = gp->ml <= gp->mk;
+    const uint64_t fmin = p.lside ? gp->ml : gp->mk;
+    const uint64_t pick = p.lside ? gp->ql : gp->qk;
+    p.ok = fmin != kNoKey && (p.lside ? pick != kNoKey : pick != 0);
+    p.q = (int)(uint32_t)pick;
+    p.ok = p.ok && FLOCK_IN(p.q, V);
+    p.th = (int64_t)(fmin ^ 0x8000000000000000ull);
+    const int k = (int)key_idx(gp->best);
+    const int l = m + (int)key_idx(c.row_best[k]);
+    p.e = p.lside ? l : k;
+    p.other = p.lside ? k : l;
+    p.de = c.depth[p.e];
+    p.dq = p.ok ? c.depth[p.q] : 0;
+    p.eside = p.lside ? 2 : 1;
+    return p;
+}
+
+// Flows along the cycle change by -/+theta; the segment from the leaving edge
+// down to the entering endpoint gets its new parents and flows in len1/acc1
+// (its own flows are read here and replaced in k_gcommit, so no vertex reads
+// a flow that this kernel writes).
+__global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
+    if (c.sc->done) return;
+    const int m = c.I.m, V = m + c.I.n;
+    const GridPivotArgs p = grid_pivot_args(c, gp);
+    if (!p.ok) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
+        return;
+    }
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const uint64_t sd = c.claim[v];
+        if (!sd) continue;
+        const int64_t delta = (sd == 1) == (v < m) ? -p.th : p.th;
+        if (sd == p.eside && c.depth[v] >= p.dq) {
+            const int prev = v == p.e ? p.other : kth_anc(c, V, p.e, p.de - c.depth[v] - 1);
+            if (!FLOCK_IN(prev, V)) { fail_check(c.sc, 17); continue; }
+            c.len1[v] = prev;
+            c.acc1[v] = v == p.e ? p.th : c.flow[prev] + ((p.eside == 1) == (prev < m) ? -p.th : p.th);
+        } else {
+            c.flow[v] += delta;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_gcommit(Ctx c, GridPivot* gp) {
+    if (c.sc->done) return;
+    const int m = c.I.m, V = m + c.I.n;
+    const GridPivotArgs p = grid_pivot_args(c, gp);
+    if (!p.ok) return;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        if (c.claim[v] != p.eside || c.depth[v] < p.dq) continue;
+        c.parent[v] = c.len1[v];
+        c.flow[v] = c.acc1[v];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        c.sc->pivots++;
+        c.sc->last_winners = 1;
+    }
+}
+
+// Dual recompute over the grid: level 0 of the lifting table, then one kernel
+// per doubling pass, then the depths, duals and int32 duals.
+__global__ void __launch_bounds__(256) k_gjump_init(Ctx c, GridPivot* gp) {
+    if (c.sc->done) return;
+    const InstDev& I = c.I;
+    const int V = I.m + I.n, root = c.sc->root;
+    if (blockIdx.x == 0 && threadIdx.x < 48) gp->pend[threadIdx.x] = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const int p = c.parent[v];
+        if (p == -2) { c.lift[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
+        else if (v == root) { c.lift[v] = v; c.len0[v] = 0; c.acc0[v] = 0; }
+        else if (!FLOCK_IN(p, V) || (p < I.m) == (v < I.m)) { fail_check(c.sc, 20); c.lift[v] = root; c.len0[v] = 0; c.acc0[v] = 0; }
+        else { c.lift[v] = p; c.len0[v] = 1; c.acc0[v] = edge_cost(I, v, p); }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_gjump(Ctx c, GridPivot* gp, int it) {
+    __shared__ int s_any;
+    if (c.sc->done) return;
+    if (it > 0 && gp->pend[it - 1] == 0) return;        // the tree was done a pass ago
+    const int V = c.I.m + c.I.n, root = c.sc->root;
+    const int32_t* aA = c.lift + (size_t)it * V;
+    int32_t* aB = c.lift + (size_t)(it + 1) * V;
+    const int32_t* lA = (it & 1) ? c.len1 : c.len0;
+    int32_t* lB = (it & 1) ? c.len0 : c.len1;
+    const int64_t* xA = (it & 1) ? c.acc1 : c.acc0;
+    int64_t* xB = (it & 1) ? c.acc0 : c.acc1;
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    int mine = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const int a = aA[v];
+        if (a < 0 || a == root) { aB[v] = a; lB[v] = lA[v]; xB[v] = xA[v]; continue; }
+        if (!FLOCK_IN(a, V)) { fail_check(c.sc, 21); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
+        const int aa = aA[a];
+        if (!FLOCK_IN(aa, V)) { fail_check(c.sc, 22); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
+        const int la = lA[v];
+        aB[v] = aa;
+        lB[v] = la + lA[a];
+        xB[v] = xA[v] + ((la & 1) ? -xA[a] : xA[a]);
+        mine |= (aa != root);
+    }
+    if (mine) s_any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0 && s_any) atomicOr(&gp->pend[it], 1);
+}
+
+__global__ void __launch_bounds__(256) k_gjump_final(Ctx c, GridPivot* gp) {
+    __shared__ int s_wide;
+    if (c.sc->done) return;
+    const int m = c.I.m, V = m + c.I.n;
+    const int passes = c.lift_cap - 1;
+    int p = -1;                                           // final level
+    for (int it = 0; it < passes; it++)
+        if (gp->pend[it] == 0) { p = it + 1; break; }
+    if (p < 0) {                                          // still pending: not a tree
+        if (blockIdx.x == 0 && threadIdx.x == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+        return;
+    }
+    const int32_t* lF = (p & 1) ? c.len1 : c.len0;
+    const int64_t* xF = (p & 1) ? c.acc1 : c.acc0;
+    if (threadIdx.x == 0) s_wide = 0;
+    __syncthreads();
+    int wide = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const int64_t pv = xF[v];
+        c.depth[v] = lF[v];
+        c.pot[v] = pv;
+        if (v >= m) c.v32[v - m] = narrow_dual(pv, wide);
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) c.row_best[i] = kNoKey;
+    if (wide) s_wide = 1;
+    __syncthreads();
+    if (threadIdx.x == 0 && s_wide) atomicOr(&gp->wide, 1);
+}
+
+// End of a grid round: the int32 dual flag and the round cap.
+__global__ void k_gend(Ctx c, GridPivot* gp) {
+    if (threadIdx.x != 0 || c.sc->done) return;
+    c.sc->narrow = gp->wide ? 0 : 1;
+    if (c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
+}
+
 __global__ void __launch_bounds__(1024, 1) k_finalize(Ctx c) {
     __shared__ BlockScratch bs;
     if (c.sc->status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) return;
@@ -553,6 +811,7 @@ static int threads_for(int V) {
 struct PlainSolver {
     std::mutex mu;
     DevBuf ws, cost, sd;
+    GridPivot* gp = nullptr;        // grid pivot round state (large instances)
     HostBuf h_sc;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -578,8 +837,9 @@ struct PlainSolver {
         carve_ctx(probe, nullptr, V, m, nullptr, nullptr, nullptr, &gbytes);
         const size_t extra_off = al256(gbytes);
         const size_t out_bytes = al256((size_t)3 * V * 4);
-        FLOCK_CK(ws.ensure(extra_off + out_bytes + al256(sizeof(Scalars))));
+        FLOCK_CK(ws.ensure(extra_off + out_bytes + al256(sizeof(Scalars)) + al256(sizeof(GridPivot))));
         carve_ctx(c, ws.as<uint8_t>(), V, m, nullptr, nullptr);
+        gp = ws.as<GridPivot>(extra_off + out_bytes + al256(sizeof(Scalars)));
         c.out_src = ws.as<int32_t>(extra_off);
         c.out_dst = c.out_src + V;
         c.out_qty = c.out_dst + V;
@@ -656,7 +916,21 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
             FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
             for (int r = 0; r < chunk; r++) {
                 k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
-                k_pivot<<<1, nt, 0, P.stream>>>(c);
+                if (V < kGridPivotV) {
+                    k_pivot<<<1, nt, 0, P.stream>>>(c);
+                    continue;
+                }
+                // large instance: the pivot round over the whole GPU
+                const int gg = std::max(1, std::min((V + 255) / 256, 2 * num_sms()));
+                k_gselect<<<1, 1024, 0, P.stream>>>(c, P.gp);
+                k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                k_gapply<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                k_gcommit<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                k_gjump_init<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                for (int it = 0; it < c.lift_cap - 1; it++) k_gjump<<<gg, 256, 0, P.stream>>>(c, P.gp, it);
+                k_gjump_final<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                k_gend<<<1, 32, 0, P.stream>>>(c, P.gp);
             }
             FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
             FLOCK_CK(cudaGraphInstantiate(&exec, g, 0));

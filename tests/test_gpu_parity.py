@@ -229,3 +229,19 @@ def test_batch_iteration_cap_reported():
     out = fg.batch_solve([big, small], max_iterations=need + 2, pricing="full")
     assert out[0].status & fg.ST_ITER_CAP and not out[0].certified
     assert out[1].status == 0 and out[1].certified and out[1].objective == fg.solve(small).objective
+
+
+@pytest.mark.parametrize("kind", ["uniform", "degenerate"])
+def test_plain_grid_round_matches_batched(kind):
+    """m + n = 4096: the plain solver runs its grid-wide pivot rounds, the
+    batched form its persistent kernel; both certified, same optimum."""
+    if kind == "uniform":
+        inst = fg.generate(0, 77, 2048, 2048, 1, 1000, 100, 1000)
+    else:
+        inst = fg.config_instance("degenerate1000", 7, m=2048, n=2048)
+    for pivot in ("switch", "sequential"):
+        p = fg.solve(inst, pivot=pivot)
+        assert p.status == 0 and p.certified, (pivot, p.status, p.notes)
+        b = fg.batch_solve([inst], pricing="full")[0]
+        assert b.status == 0 and b.certified
+        assert p.objective == b.objective
