@@ -245,3 +245,18 @@ def test_plain_grid_round_matches_batched(kind):
         b = fg.batch_solve([inst], pricing="full")[0]
         assert b.status == 0 and b.certified
         assert p.objective == b.objective
+
+
+def test_lp_optimum_cross_check():
+    """GPU optima (plain and batched) equal an independent LP solver's
+    (HiGHS) on medium instances, including a degenerate one."""
+    pytest.importorskip("scipy")
+    from lp_check import lp_optimum
+    insts = [fg.generate(0, 4000 + k, 60 + 40 * k, 90 + 25 * k, 1, 1000, 100, 1000) for k in range(4)]
+    insts.append(fg.config_instance("degenerate1000", 9, m=150, n=120))
+    batch = fg.batch_solve(insts)
+    for k, inst in enumerate(insts):
+        opt = lp_optimum(inst.supply, inst.demand, inst.cost)
+        p = fg.solve(inst)
+        assert p.status == 0 and p.certified and p.objective == opt, k
+        assert batch[k].status == 0 and batch[k].certified and batch[k].objective == opt, k

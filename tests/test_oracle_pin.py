@@ -135,3 +135,21 @@ def test_certificate_checker_plants(orc):
     assert oracle.certify(s, d, c, flows, u2, v)[0] & 8
     u3 = u.copy(); u3[int(flows[0, 0])] -= 1
     assert oracle.certify(s, d, c, flows, u3, v)[0] & 16
+
+
+def test_reference_path_matches_lp_optimum(orc):
+    """The restated reference CPU path against an independent LP solver
+    (HiGHS) on seeded instances where it terminates by optimality."""
+    pytest.importorskip("scipy")
+    from lp_check import lp_optimum
+    import flock_gb300 as fg
+    checked = 0
+    for seed in range(12):
+        m, n = 8 + 3 * seed, 12 + 2 * seed
+        inst = fg.generate(0, 3000 + seed, m, n, 1, 100, 10, 100)
+        r = oracle.solve_ref(inst.supply, inst.demand, inst.cost.astype(np.float32))
+        if oracle.verdict(inst.supply, inst.demand, inst.cost, r) != "optimal":
+            continue
+        assert round(r["objective"]) == lp_optimum(inst.supply, inst.demand, inst.cost), seed
+        checked += 1
+    assert checked >= 8
