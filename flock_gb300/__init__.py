@@ -94,6 +94,9 @@ def lib() -> ctypes.CDLL:
     L.flock_dat_shape.argtypes = [ctypes.c_char_p, P(i32), P(i32)]
     L.flock_dat_scale.argtypes = [ctypes.c_char_p, P(i32)]
     L.flock_read_dat.argtypes = [ctypes.c_char_p, i32, i32, i32, P(i32), P(i32), P(i32)]
+    L.flock_write_bin.argtypes = [ctypes.c_char_p, P(CInstance)]
+    L.flock_bin_shape.argtypes = [ctypes.c_char_p, P(i32), P(i32)]
+    L.flock_read_bin.argtypes = [ctypes.c_char_p, i32, i32, P(i32), P(i32), P(i32)]
     L.flock_server_create.argtypes = [P(CServerConfig), P(ctypes.c_void_p)]
     L.flock_server_submit.argtypes = [ctypes.c_void_p, P(CInstance), P(ctypes.c_uint64)]
     L.flock_server_poll.argtypes = [ctypes.c_void_p, P(CResult), P(P(CFlow)), i32, P(i32)]
@@ -215,6 +218,29 @@ def read_dat(path: str, scale: Optional[int] = None) -> Tuple[Instance, int]:
     if rc:
         raise _err(rc)
     return Instance(s, d, c), scale
+
+
+def write_bin(inst: Instance, path: str) -> None:
+    """Binary instance file (int32 little-endian; see include/flock.h)."""
+    rc = lib().flock_write_bin(path.encode(), ctypes.byref(inst.c()))
+    if rc:
+        raise _err(rc)
+
+
+def read_bin(path: str) -> Instance:
+    L = lib()
+    m, n = i32(), i32()
+    bp = path.encode()
+    rc = L.flock_bin_shape(bp, ctypes.byref(m), ctypes.byref(n))
+    if rc:
+        raise _err(rc)
+    s = np.empty(m.value, np.int32)
+    d = np.empty(n.value, np.int32)
+    c = np.empty((m.value, n.value), np.int32)
+    rc = L.flock_read_bin(bp, m.value, n.value, _p(s), _p(d), _p(c))
+    if rc:
+        raise _err(rc)
+    return Instance(s, d, c)
 
 
 # ------------------------------------------------------------- solving ---

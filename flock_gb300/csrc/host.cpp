@@ -39,18 +39,86 @@ struct Tok {
     }
 };
 
-int load(const char* path, Tok& t) {
+// Reads the file (its first `limit` bytes when limit > 0).
+int load(const char* path, Tok& t, long limit = 0) {
     if (!path) return FLOCK_ERR_ARG;
     FILE* f = fopen(path, "rb");
     if (!f) { flock::set_error(std::string("input file not found: ") + path); return FLOCK_ERR_FILE; }
     fseek(f, 0, SEEK_END);
     long sz = ftell(f);
     fseek(f, 0, SEEK_SET);
+    if (limit > 0 && sz > limit) sz = limit;
     t.buf.resize(sz > 0 ? (size_t)sz : 0);
     size_t got = sz > 0 ? fread(t.buf.data(), 1, (size_t)sz, f) : 0;
     fclose(f);
     if ((long)got != sz) { flock::set_error("short read"); return FLOCK_ERR_FILE; }
     return FLOCK_OK;
+}
+
+inline bool is_space(char ch) { return ch == ' ' || ch == '\t' || ch == '\n' || ch == '\r'; }
+
+// The cost section in parallel.  The bytes from `from` on are cut into
+// chunks at whitespace; each chunk's tokens are counted, a prefix sum gives
+// each chunk its first token index, and every chunk parses its tokens into
+// place.  Only the first `count` tokens are used (as the sequential reader,
+// which stops after them); fewer is a parse error.  visit(k, s, len) handles
+// token k and returns 0 or an error code; the error of the lowest token index
+// wins, so the result equals a sequential left-to-right pass.
+template <class F>
+int parallel_tokens(const std::vector<char>& buf, size_t from, int64_t count, const F& visit) {
+    const size_t end = buf.size();
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const size_t bytes = end > from ? end - from : 0;
+    int T = (int)std::min<size_t>(std::min(hw, 64), std::max<size_t>(1, bytes / (1 << 20)));
+    std::vector<size_t> cut(T + 1);
+    cut[0] = from;
+    cut[T] = end;
+    for (int t = 1; t < T; t++) {
+        size_t p = from + bytes * t / T;
+        while (p < end && !is_space(buf[p])) p++;     // a chunk starts at whitespace
+        cut[t] = std::max(p, cut[t - 1]);
+    }
+    std::vector<int64_t> cnt(T, 0);
+    auto count_tokens = [&](int t) {
+        int64_t c = 0;
+        bool in = false;
+        for (size_t p = cut[t]; p < cut[t + 1]; p++) {
+            const bool sp = is_space(buf[p]);
+            if (!sp && !in) c++;
+            in = !sp;
+        }
+        cnt[t] = c;
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; t++) th.emplace_back(count_tokens, t);
+    count_tokens(0);
+    for (auto& x : th) x.join();
+    th.clear();
+    std::vector<int64_t> first(T + 1, 0);
+    for (int t = 0; t < T; t++) first[t + 1] = first[t] + cnt[t];
+    std::vector<int64_t> err_at(T, INT64_MAX);
+    std::vector<int> err_rc(T, 0);
+    auto parse_chunk = [&](int t) {
+        int64_t k = first[t];
+        size_t p = cut[t];
+        while (p < cut[t + 1] && k < count) {
+            while (p < cut[t + 1] && is_space(buf[p])) p++;
+            if (p >= cut[t + 1]) break;
+            const size_t b = p;
+            while (p < cut[t + 1] && !is_space(buf[p])) p++;
+            const int rc = visit(k, buf.data() + b, p - b);
+            if (rc) { err_at[t] = k; err_rc[t] = rc; return; }
+            k++;
+        }
+    };
+    for (int t = 1; t < T; t++) th.emplace_back(parse_chunk, t);
+    parse_chunk(0);
+    for (auto& x : th) x.join();
+    int64_t best = INT64_MAX;
+    int rc = 0;
+    for (int t = 0; t < T; t++) if (err_at[t] < best) { best = err_at[t]; rc = err_rc[t]; }
+    if (!rc && first[T] < count) rc = FLOCK_ERR_PARSE;      // the file ends early
+    return rc;
 }
 
 // integer token (supplies, demands, sizes)
@@ -106,7 +174,7 @@ extern "C" {
 
 int flock_dat_shape(const char* path, int32_t* m, int32_t* n) {
     Tok t;
-    int rc = load(path, t);
+    int rc = load(path, t, 4096);
     if (rc) return rc;
     const char* s; size_t l; int64_t a, b;
     if (!t.next(&s, &l) || !parse_int(s, l, &a)) return FLOCK_ERR_PARSE;
@@ -125,13 +193,16 @@ int flock_dat_scale(const char* path, int32_t* scale) {
     if (!t.next(&s, &l) || !parse_int(s, l, &a)) return FLOCK_ERR_PARSE;
     if (!t.next(&s, &l) || !parse_int(s, l, &b)) return FLOCK_ERR_PARSE;
     for (int64_t k = 0; k < a + b; k++) if (!t.next(&s, &l) || !parse_int(s, l, &x)) return FLOCK_ERR_PARSE;
-    int best = 0;
-    for (int64_t k = 0; k < a * b; k++) {
+    std::atomic<int> best{0};
+    rc = parallel_tokens(t.buf, t.p, a * b, [&](int64_t, const char* s2, size_t l2) {
         bool inexact = false; int fd = 0; int64_t v;
-        if (!t.next(&s, &l) || !parse_scaled(s, l, 0, &v, &inexact, &fd)) return FLOCK_ERR_PARSE;
-        best = std::max(best, fd);
-    }
-    if (scale) *scale = best;
+        if (!parse_scaled(s2, l2, 0, &v, &inexact, &fd)) return (int)FLOCK_ERR_PARSE;
+        int cur = best.load(std::memory_order_relaxed);
+        while (fd > cur && !best.compare_exchange_weak(cur, fd, std::memory_order_relaxed)) {}
+        return 0;
+    });
+    if (rc) return rc;
+    if (scale) *scale = best.load();
     return FLOCK_OK;
 }
 
@@ -154,15 +225,104 @@ int flock_read_dat(const char* path, int32_t scale, int32_t m, int32_t n,
         demand[j] = (int32_t)x;
     }
     const int64_t mn = (int64_t)m * n;
-    for (int64_t k = 0; k < mn; k++) {
+    rc = parallel_tokens(t.buf, t.p, mn, [&](int64_t k, const char* s2, size_t l2) {
         bool inexact = false;
-        if (!t.next(&s, &l) || !parse_scaled(s, l, scale, &x, &inexact, nullptr)) { flock::set_error("bad cost token"); return FLOCK_ERR_PARSE; }
-        if (inexact) { flock::set_error("cost not integral at this decimal scale"); return FLOCK_ERR_INEXACT; }
-        if (x > (1 << 30) || x < -(1 << 30)) { flock::set_error("cost out of range"); return FLOCK_ERR_RANGE; }
-        cost[k] = (int32_t)x;
+        int64_t v;
+        if (!parse_scaled(s2, l2, scale, &v, &inexact, nullptr)) return (int)FLOCK_ERR_PARSE;
+        if (inexact) return (int)FLOCK_ERR_INEXACT;
+        if (v > (1 << 30) || v < -(1 << 30)) return (int)FLOCK_ERR_RANGE;
+        cost[k] = (int32_t)v;
+        return 0;
+    });
+    if (rc == FLOCK_ERR_PARSE) flock::set_error("bad or missing cost token");
+    if (rc == FLOCK_ERR_INEXACT) flock::set_error("cost not integral at this decimal scale");
+    if (rc == FLOCK_ERR_RANGE) flock::set_error("cost out of range");
+    return rc;
+}
+
+// ========================================================== binary file ===
+// "FLKBIN01", int32 m, int32 n, then m supplies, n demands and m*n costs,
+// int32 little-endian, costs row-major.
+namespace {
+const char kBinMagic[8] = {'F', 'L', 'K', 'B', 'I', 'N', '0', '1'};
+
+bool little_endian() {
+    const uint32_t one = 1;
+    unsigned char b;
+    memcpy(&b, &one, 1);
+    return b == 1;
+}
+
+int bin_open(const char* path, FILE** f, int32_t* m, int32_t* n) {
+    if (!path) return FLOCK_ERR_ARG;
+    if (!little_endian()) { flock::set_error("binary instance files need a little-endian host"); return FLOCK_ERR_ARG; }
+    *f = fopen(path, "rb");
+    if (!*f) { flock::set_error(std::string("input file not found: ") + path); return FLOCK_ERR_FILE; }
+    char magic[8];
+    int32_t hdr[2];
+    if (fread(magic, 1, 8, *f) != 8 || memcmp(magic, kBinMagic, 8) != 0 || fread(hdr, 4, 2, *f) != 2 ||
+        hdr[0] < 1 || hdr[1] < 1 || hdr[0] > (1 << 28) || hdr[1] > (1 << 28)) {
+        fclose(*f);
+        flock::set_error("not a flock binary instance file");
+        return FLOCK_ERR_PARSE;
     }
+    fseek(*f, 0, SEEK_END);
+    const int64_t want = 16 + 4 * ((int64_t)hdr[0] + hdr[1] + (int64_t)hdr[0] * hdr[1]);
+    if ((int64_t)ftell(*f) != want) {
+        fclose(*f);
+        flock::set_error("binary instance file has the wrong size");
+        return FLOCK_ERR_PARSE;
+    }
+    fseek(*f, 16, SEEK_SET);
+    *m = hdr[0];
+    *n = hdr[1];
     return FLOCK_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int flock_write_bin(const char* path, const flock_instance* inst) {
+    if (!path || !inst || !inst->supply || !inst->demand || !inst->cost || inst->m < 1 || inst->n < 1) return FLOCK_ERR_ARG;
+    if (!little_endian()) { flock::set_error("binary instance files need a little-endian host"); return FLOCK_ERR_ARG; }
+    FILE* f = fopen(path, "wb");
+    if (!f) { flock::set_error(std::string("cannot write: ") + path); return FLOCK_ERR_FILE; }
+    const int32_t hdr[2] = {inst->m, inst->n};
+    const size_t mn = (size_t)inst->m * inst->n;
+    const bool ok = fwrite(kBinMagic, 1, 8, f) == 8 && fwrite(hdr, 4, 2, f) == 2 &&
+                    fwrite(inst->supply, 4, (size_t)inst->m, f) == (size_t)inst->m &&
+                    fwrite(inst->demand, 4, (size_t)inst->n, f) == (size_t)inst->n && fwrite(inst->cost, 4, mn, f) == mn;
+    if (fclose(f) != 0 || !ok) { flock::set_error(std::string("short write: ") + path); return FLOCK_ERR_FILE; }
+    return FLOCK_OK;
+}
+
+int flock_bin_shape(const char* path, int32_t* m, int32_t* n) {
+    FILE* f = nullptr;
+    int32_t a = 0, b = 0;
+    const int rc = bin_open(path, &f, &a, &b);
+    if (rc) return rc;
+    fclose(f);
+    if (m) *m = a;
+    if (n) *n = b;
+    return FLOCK_OK;
+}
+
+int flock_read_bin(const char* path, int32_t m, int32_t n, int32_t* supply, int32_t* demand, int32_t* cost) {
+    if (!supply || !demand || !cost) return FLOCK_ERR_ARG;
+    FILE* f = nullptr;
+    int32_t a = 0, b = 0;
+    int rc = bin_open(path, &f, &a, &b);
+    if (rc) return rc;
+    if (a != m || b != n) { fclose(f); flock::set_error("shape mismatch"); return FLOCK_ERR_ARG; }
+    const size_t mn = (size_t)m * n;
+    const bool ok = fread(supply, 4, (size_t)m, f) == (size_t)m && fread(demand, 4, (size_t)n, f) == (size_t)n &&
+                    fread(cost, 4, mn, f) == mn;
+    fclose(f);
+    if (!ok) { flock::set_error("short read"); return FLOCK_ERR_FILE; }
+    return FLOCK_OK;
+}
+
+}  // extern "C"
 
 // ============================================================= generator ===
 // splitmix64 stream + Lemire's bounded integers: the same integers on every

@@ -129,6 +129,15 @@ int flock_dat_scale(const char* path, int32_t* scale);
 int flock_read_dat(const char* path, int32_t decimal_scale, int32_t m, int32_t n,
                    int32_t* supply, int32_t* demand, int32_t* cost);
 
+/* Binary instance file (no counterpart in the reference; for large instances,
+ * where the text format's parse dominates): "FLKBIN01", int32 m, int32 n, then
+ * m supplies, n demands and m*n costs as int32 little-endian, costs row-major.
+ * The costs are stored as the solver takes them (no decimal scaling); reading
+ * returns them unchecked (flock_solve validates). */
+int flock_write_bin(const char* path, const flock_instance* inst);
+int flock_bin_shape(const char* path, int32_t* m, int32_t* n);
+int flock_read_bin(const char* path, int32_t m, int32_t n, int32_t* supply, int32_t* demand, int32_t* cost);
+
 /* Vogel's approximation on the GPU with the reference's exact semantics.
  * Writes m+n-1 allocations in allocation order.  *events as flock_stats. */
 int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events);

@@ -148,3 +148,76 @@ def test_server_budget_rejection():
         s.submit(inst)
     assert ex.value.status == fg.FLOCK_ERR_BUDGET
     s.close()
+
+
+def _write_dat(path, s, d, tokens):
+    with open(path, "w") as f:
+        f.write(f"{len(s)} {len(d)}\n")
+        f.write(" ".join(str(x) for x in s) + "\n")
+        f.write(" ".join(str(x) for x in d) + "\n")
+        for k in range(0, len(tokens), 997):
+            f.write(" ".join(tokens[k:k + 997]) + "\n")
+
+
+def test_reader_parallel_large(tmp_path):
+    """A multi-megabyte file (parsed in several chunks): decimal costs read
+    exactly at the smallest exact scale."""
+    rng = np.random.default_rng(5)
+    m, n = 700, 650
+    cents = rng.integers(0, 100000, size=m * n)
+    toks = [f"{c // 100}.{c % 100:02d}" for c in cents]
+    s = rng.integers(1, 50, size=m)
+    d = np.zeros(n, np.int64)
+    d[:] = s.sum() // n
+    d[-1] += s.sum() - d.sum()
+    p = str(tmp_path / "big.dat")
+    _write_dat(p, s, d, toks)
+    assert os.path.getsize(p) > 2 << 20                # several parse chunks
+    inst, scale = fg.read_dat(p)
+    assert scale == 2 or (scale < 2 and np.all(cents % 10 == 0))
+    np.testing.assert_array_equal(inst.cost.ravel(), cents // (10 ** (2 - scale)))
+    np.testing.assert_array_equal(inst.supply, s)
+    np.testing.assert_array_equal(inst.demand, d)
+
+
+def test_reader_parallel_error_order(tmp_path):
+    """Several bad tokens: the error of the first one (in file order) is the
+    one reported, as a sequential reader would, wherever the chunks fall."""
+    rng = np.random.default_rng(6)
+    m, n = 600, 600
+    toks = [str(x) for x in rng.integers(1, 1000, size=m * n)]
+    s = np.full(m, 10)
+    d = np.full(n, 10)
+
+    def read(tokens, scale=0):
+        p = str(tmp_path / "e.dat")
+        _write_dat(p, s, d, tokens)
+        with pytest.raises(fg.FlockError) as ex:
+            fg.read_dat(p, scale=scale)
+        return ex.value.status
+
+    t = list(toks); t[200000] = "1.5"; t[300000] = "x7"
+    assert read(t) == fg.FLOCK_ERR_INEXACT            # inexact comes first
+    t = list(toks); t[100] = "x7"; t[300000] = "1.5"
+    assert read(t) == fg.FLOCK_ERR_PARSE               # bad text comes first
+    t = list(toks); t[250000] = str((1 << 30) + 1)
+    assert read(t) == fg.FLOCK_ERR_RANGE
+    t = list(toks[:-5]); t[1000] = "2.5"
+    assert read(t) == fg.FLOCK_ERR_INEXACT             # before the missing tokens
+    assert read(toks[:-5]) == fg.FLOCK_ERR_PARSE       # missing tokens
+
+
+def test_binary_instance_round_trip(tmp_path):
+    inst = fg.generate(0, 9, 123, 77, -1000, 1000, 1, 100)
+    p = str(tmp_path / "x.fbin")
+    fg.write_bin(inst, p)
+    assert os.path.getsize(p) == 16 + 4 * (123 + 77 + 123 * 77)
+    back = fg.read_bin(p)
+    np.testing.assert_array_equal(back.supply, inst.supply)
+    np.testing.assert_array_equal(back.demand, inst.demand)
+    np.testing.assert_array_equal(back.cost, inst.cost)
+    with open(p, "r+b") as f:
+        f.truncate(100)
+    with pytest.raises(fg.FlockError) as ex:
+        fg.read_bin(p)
+    assert ex.value.status == fg.FLOCK_ERR_PARSE
