@@ -280,9 +280,9 @@ def _result(st: CStats, flows: np.ndarray, u=None, v=None) -> Result:
 
 
 def solve(inst: Instance, bfs: str = "vogel", pivot: str = "switch", max_iterations: int = 0,
-          verify: bool = True, duals: bool = True, raise_on_error: bool = True) -> Result:
+          verify: bool = True, duals: bool = True, raise_on_error: bool = True, pricing: str = "partial") -> Result:
     ci = inst.c()
-    opt = _options(bfs, pivot, max_iterations, verify)
+    opt = _options(bfs, pivot, max_iterations, verify, pricing)
     V = inst.m + inst.n
     flows = np.zeros((V - 1, 3), np.int32)
     u = np.zeros(inst.m, np.int64) if duals else None

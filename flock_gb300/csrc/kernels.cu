@@ -68,8 +68,12 @@ __device__ __forceinline__ int4 ld_stream4(const int4* p) {
     return v;
 }
 
-__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int ntile) {
+// rows: price only the listed rows (c.sc->pp_n of them: partial pricing),
+// null for all; gate: run only when *gate == gate_val (null: always).
+__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int ntile, const int32_t* rows,
+                                                           const int32_t* gate, int gate_val) {
     if (c.sc->done) return;
+    if (gate && *gate != gate_val) return;
     __shared__ __align__(16) int32_t vt[kSweepTile];
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
@@ -78,10 +82,12 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int
     const int jn = min(tile, n - j0);
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
     const int nseg = (jn + kSegCols - 1) / kSegCols;
-    const long long units = (long long)m * nseg, stride = (long long)nrg * wpb;
+    const int nrows = rows ? min(max(c.sc->pp_n, 0), kPPRows) : m;
+    const long long units = (long long)nrows * nseg, stride = (long long)nrg * wpb;
     if (!c.sc->narrow) {
         for (long long u = (long long)rg * wpb + warp; u < units; u += stride) {
-            const int i = (int)(u / nseg), s = (int)(u % nseg);
+            const int i = rows ? rows[u / nseg] : (int)(u / nseg), s = (int)(u % nseg);
+            if (!FLOCK_IN(i, m)) { if (lane == 0) fail_check(c.sc, 19); continue; }
             const int a = j0 + s * kSegCols, b = min(j0 + jn, a + kSegCols);
             const uint64_t k = row_best_exact(I.cost + (size_t)i * I.ldc, c.pot[i], c.pot + m, a, b);
             if (lane == 0) atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)k);
@@ -92,7 +98,8 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int
     __syncthreads();
     const int4* v4 = reinterpret_cast<const int4*>(vt);
     for (long long u = (long long)rg * wpb + warp; u < units; u += stride) {
-        const int i = (int)(u / nseg), s = (int)(u % nseg);
+        const int i = rows ? rows[u / nseg] : (int)(u / nseg), s = (int)(u % nseg);
+        if (!FLOCK_IN(i, m)) { if (lane == 0) fail_check(c.sc, 19); continue; }
         const int a = s * kSegCols, b = min(jn, a + kSegCols);   // tile-local columns [a, b)
         const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc + j0);
         int32_t bv = INT32_MAX, bj = INT32_MAX;
@@ -149,6 +156,7 @@ struct GridPivot {
     uint64_t mk, ml;        // per side: minimum order-preserving flow
     uint64_t qk, ql;        // per side: leaving edge (depth << 32 | child)
     int32_t wide;           // a column dual left the int32 window
+    int32_t full;           // partial pricing: this round sweeps every row
     int32_t pend[48];       // pointer-jumping pass it left vertices pending
 };
 
@@ -385,6 +393,36 @@ __global__ void __launch_bounds__(256) k_gjump_final(Ctx c, GridPivot* gp) {
     if (wide) s_wide = 1;
     __syncthreads();
     if (threadIdx.x == 0 && s_wide) atomicOr(&gp->wide, 1);
+}
+
+// Partial pricing on the plain path (large instances): decide whether this
+// round sweeps every row, re-price the candidates otherwise (k_sweep with the
+// row list), fall back to a full sweep in the same round when they hold no
+// negative key, and after a full sweep choose the next candidates.  Rows
+// without a key this round keep kNoKey (k_gjump_final clears every key).
+__global__ void k_pdecide(Ctx c, GridPivot* gp) {
+    if (threadIdx.x != 0 || c.sc->done) return;
+    const int pn = c.sc->pp_n;
+    gp->full = (pn <= 0 || pn > kPPRows || c.sc->pp_age >= kPPRefresh) ? 1 : 0;
+}
+
+__global__ void __launch_bounds__(256) k_pcheck(Ctx c, GridPivot* gp) {
+    if (c.sc->done || gp->full) return;
+    const int m = c.I.m, pn = c.sc->pp_n;
+    int neg = 0;
+    for (int t = threadIdx.x; t < pn; t += blockDim.x) {
+        const int i = c.prow[t];
+        if (FLOCK_IN(i, m)) neg |= key_val(c.row_best[i]) < 0;
+    }
+    neg = __syncthreads_or(neg);
+    if (threadIdx.x == 0 && !neg) gp->full = 1;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pselect_rows(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    if (c.sc->done) return;
+    if (gp->full) select_candidate_rows(c, bs, false);
+    if (threadIdx.x == 0) c.sc->pp_age++;
 }
 
 // End of a grid round: the int32 dual flag and the round cap.
@@ -903,6 +941,8 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     int grid = 0, tile = 0, ntile = 0;
     sweep_shape(m, n, &grid, &tile, &ntile);
+    // partial pricing on the plain path for large instances (grid rounds)
+    const bool partial = opt.pricing == FLOCK_PRICING_PARTIAL && V >= kGridPivotV;
     // pivot loop: chunks of rounds captured once as a CUDA graph
     int chunk = 8;
     cudaGraphExec_t exec = nullptr;
@@ -915,7 +955,15 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
             cudaGraph_t g;
             FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
             for (int r = 0; r < chunk; r++) {
-                k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
+                if (partial) {
+                    k_pdecide<<<1, 32, 0, P.stream>>>(c, P.gp);
+                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, c.prow, &P.gp->full, 0);
+                    k_pcheck<<<1, 256, 0, P.stream>>>(c, P.gp);
+                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, &P.gp->full, 1);
+                    k_pselect_rows<<<1, 1024, 0, P.stream>>>(c, P.gp);
+                } else {
+                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+                }
                 if (V < kGridPivotV) {
                     k_pivot<<<1, nt, 0, P.stream>>>(c);
                     continue;
@@ -1060,7 +1108,7 @@ static int test_sweep(int m, int n, const int32_t* cost, const int64_t* pot, uin
     } else {
         int grid = 0, tile = 0, ntile = 0;
         sweep_shape(m, n, &grid, &tile, &ntile);
-        k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
+        k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
     }
     FLOCK_CK(cudaGetLastError());
     FLOCK_CK(cudaMemcpyAsync(keys, c.row_best, (size_t)m * 8, cudaMemcpyDeviceToHost, P.stream));
@@ -1092,9 +1140,9 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
     FLOCK_CK(cudaMemsetAsync(c.row_best, 0xff, (size_t)m * 8, P.stream));
     int grid = 0, tile = 0, ntile = 0;
     sweep_shape(m, n, &grid, &tile, &ntile);
-    for (int w = 0; w < 3; w++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
+    for (int w = 0; w < 3; w++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
-    for (int k = 0; k < iters; k++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile);
+    for (int k = 0; k < iters; k++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     FLOCK_CK(cudaEventSynchronize(P.ev[1]));
     float ms = 0;

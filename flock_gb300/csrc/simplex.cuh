@@ -439,6 +439,52 @@ __device__ void sweep_rows_cta(const Ctx& c, const int32_t* list, int cnt) {
 
 __device__ void sweep_cta(const Ctx& c) { sweep_rows_cta(c, nullptr, c.I.m); }
 
+// After a full sweep: keep the kPPRows rows with the most negative keys in
+// prow[] (32-bin histogram threshold, then row order: value-determined),
+// optionally clearing every other row's key; resets the partial-pricing age.
+// All threads of the block; uses cand[] as scratch.
+__device__ void select_candidate_rows(const Ctx& c, BlockScratch& bs, bool clear_others) {
+    const int m = c.I.m;
+    int32_t rmin = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
+    rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
+    const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
+    int last = -1;                                             // highest histogram bin kept
+    if (rmin < 0) {
+        if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int32_t v = key_val(c.row_best[i]);
+            if (v < 0) atomicAdd((unsigned long long*)&bs.red2[((int64_t)v - rmin) * 32 / span], 1ull);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t cum = bs.red2[0];
+            int l = 0;
+            for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)kPPRows; b++) { cum += bs.red2[b]; l = b; }
+            bs.i[1] = l;
+        }
+        __syncthreads();
+        last = bs.i[1];
+    }
+    // candidates in row order: exclusive scan of the selection flags
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int32_t v = key_val(c.row_best[i]);
+        c.cand[i] = (v < 0 && ((int64_t)v - rmin) * 32 / span <= last) ? 1 : 0;
+    }
+    __syncthreads();
+    const int32_t total = block_exclusive_scan_i32(c.cand, m, bs);   // ends with a barrier
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int32_t v = key_val(c.row_best[i]);
+        const bool sel = v < 0 && ((int64_t)v - rmin) * 32 / span <= last;
+        const int slot = c.cand[i];
+        if (sel && slot < kPPRows) c.prow[slot] = i;
+        else if (clear_others) c.row_best[i] = kNoKey;
+    }
+    if (threadIdx.x == 0) { c.sc->pp_n = min(total, kPPRows); c.sc->pp_age = 0; }
+    __syncthreads();
+}
+
 // Partial pricing (candidate rows).  A full sweep keeps the kPPRows rows
 // with the most negative best reduced costs in prow[] (chosen by a 32-bin
 // histogram threshold and then by row index, so the set depends only on the
@@ -465,44 +511,7 @@ __device__ void sweep_partial_cta(const Ctx& c, BlockScratch& bs) {
     }
     if (full) {
         sweep_rows_cta(c, nullptr, m);
-        int32_t rmin = 0;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
-        rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
-        const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
-        int last = -1;                                             // highest histogram bin kept
-        if (rmin < 0) {
-            if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
-            __syncthreads();
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
-                const int32_t v = key_val(c.row_best[i]);
-                if (v < 0) atomicAdd((unsigned long long*)&bs.red2[((int64_t)v - rmin) * 32 / span], 1ull);
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                uint64_t cum = bs.red2[0];
-                int l = 0;
-                for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)kPPRows; b++) { cum += bs.red2[b]; l = b; }
-                bs.i[1] = l;
-            }
-            __syncthreads();
-            last = bs.i[1];
-        }
-        // candidates in row order: exclusive scan of the selection flags (cand[] as scratch)
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            const int32_t v = key_val(c.row_best[i]);
-            c.cand[i] = (v < 0 && ((int64_t)v - rmin) * 32 / span <= last) ? 1 : 0;
-        }
-        __syncthreads();
-        const int32_t total = block_exclusive_scan_i32(c.cand, m, bs);   // ends with a barrier
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            const int32_t v = key_val(c.row_best[i]);
-            const bool sel = v < 0 && ((int64_t)v - rmin) * 32 / span <= last;
-            const int slot = c.cand[i];
-            if (sel && slot < kPPRows) c.prow[slot] = i;
-            else c.row_best[i] = kNoKey;
-        }
-        if (threadIdx.x == 0) { c.sc->pp_n = min(total, kPPRows); c.sc->pp_age = 0; }
-        __syncthreads();
+        select_candidate_rows(c, bs, true);
     }
     if (threadIdx.x == 0) c.sc->pp_age++;
     __syncthreads();

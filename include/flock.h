@@ -76,8 +76,9 @@ enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH 
  * a full sweep keeps the 64 rows with the most negative reduced costs as
  * candidates and the following rounds re-price only those rows, until they
  * hold no negative reduced cost or 32 rounds have passed; optimality is only
- * declared after a full sweep.  Batched and served forms; the plain solver
- * always uses FULL.  The optimum is the same; the pivot sequence differs. */
+ * declared after a full sweep.  Batched and served forms, and the plain
+ * solver's grid-wide rounds (m + n >= 4096); smaller plain instances always
+ * price fully.  The optimum is the same; the pivot sequence differs. */
 enum { FLOCK_PRICING_FULL = 0, FLOCK_PRICING_PARTIAL = 1 };
 
 typedef struct {

@@ -239,12 +239,13 @@ def test_plain_grid_round_matches_batched(kind):
         inst = fg.generate(0, 77, 2048, 2048, 1, 1000, 100, 1000)
     else:
         inst = fg.config_instance("degenerate1000", 7, m=2048, n=2048)
+    b = fg.batch_solve([inst], pricing="full")[0]
+    assert b.status == 0 and b.certified
     for pivot in ("switch", "sequential"):
-        p = fg.solve(inst, pivot=pivot)
-        assert p.status == 0 and p.certified, (pivot, p.status, p.notes)
-        b = fg.batch_solve([inst], pricing="full")[0]
-        assert b.status == 0 and b.certified
-        assert p.objective == b.objective
+        for pricing in ("full", "partial"):
+            p = fg.solve(inst, pivot=pivot, pricing=pricing)
+            assert p.status == 0 and p.certified, (pivot, pricing, p.status, p.notes)
+            assert p.objective == b.objective, (pivot, pricing)
 
 
 def test_lp_optimum_cross_check():
