@@ -162,7 +162,7 @@ def test_batch_forms_all_buckets(form, monkeypatch):
     for k, (inst, r) in enumerate(zip(insts, out)):
         assert r.status == 0 and r.certified, (k, inst.m, inst.n, r.status)
         if inst.m * inst.n <= 300 * 300 or k < len(shapes):
-            p = fg.solve(inst)
+            p = fg.solve(inst, pricing="full")
             assert r.objective == p.objective, (k, inst.m, inst.n)
             assert r.iterations == p.iterations, (k, inst.m, inst.n)
 
