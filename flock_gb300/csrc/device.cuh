@@ -70,6 +70,10 @@ struct Scalars {
     int32_t pricing;       // 0 full sweeps, 1 partial pricing (candidate rows)
     int32_t pp_n;          // partial pricing: candidate rows in prow[]
     int32_t pp_age;        // partial pricing: rounds since the last full sweep
+    int32_t ivp;           // which half of Ctx::iv holds the current preorder intervals
+    int32_t nwide;         // live column duals outside the int32 window (narrow == (nwide == 0))
+    int32_t stale;         // 1: depth, duals and intervals must be rebuilt from parent[] (tree_build_cta)
+    int32_t pad_;
 };
 
 // One instance as the kernels see it.
@@ -94,13 +98,16 @@ struct Ctx {
     int32_t* depth;    // V
     int64_t* pot;      // V  duals: u_i (rows), v_j (columns)
     int32_t* v32;      // n  column duals as int32 when sc->narrow (kDead32: zero-demand column)
-    // pointer-jumping scratch (double buffered)
+    // Preorder intervals, two buffers of V (sc->ivp selects the current one):
+    // iv[v] = (pre, size) with the subtree of tree vertex v holding exactly
+    // the vertices x with pre[v] <= pre[x] < pre[v] + size[v].  Dead vertices
+    // hold (0, 0).
+    int2* iv;
+    // pointer-jumping scratch, one block of jump_bytes(V) (set_jump): int32
+    // anc0, anc1, len0, len1 then int64 acc0, acc1; the Euler-tour ranking
+    // uses the same block as two arrays of 2 V words.  Between rebuilds the
+    // single pivot keeps its path in len1 and the path flows in acc1.
     int32_t* anc0; int32_t* anc1; int32_t* len0; int32_t* len1; int64_t* acc0; int64_t* acc1;
-    // binary-lifting table: level j (j < lift_cap) holds each vertex's
-    // 2^j-th ancestor (clamped at the root), V entries per level; the dual
-    // recompute writes it.  lift_cap == 0: no table (ping-pong anc0/anc1).
-    int32_t* lift;
-    int32_t lift_cap;
     // pricing
     uint64_t* row_best;   // m   packed (reduced cost, column) of the best cell per row
     uint64_t* claim;      // V   edge claims
@@ -123,13 +130,20 @@ struct Ctx {
     int32_t* uf;          // V  union-find
 };
 
-// Levels of the binary-lifting table for V vertices: every depth is < V, so
-// ceil(log2 V) doubling passes reach the root; levels 0..ceil(log2 V).
-__host__ __device__ __forceinline__ int lift_levels(int V) {
-    int l = 0;
-    while ((1 << l) < V) l++;
-    return l + 1;
+// Size of the pointer-jumping scratch block of V vertices.
+__host__ __device__ __forceinline__ size_t jump_bytes(int V) { return 32 * (size_t)V; }
+
+// Point the six pointer-jumping arrays into one block of jump_bytes(V)
+// (16-byte aligned).
+__host__ __device__ __forceinline__ void set_jump(Ctx& c, void* base, int V) {
+    int32_t* b = (int32_t*)base;
+    c.anc0 = b; c.anc1 = b + V; c.len0 = b + 2 * (size_t)V; c.len1 = b + 3 * (size_t)V;
+    c.acc0 = (int64_t*)(b + 4 * (size_t)V);
+    c.acc1 = c.acc0 + V;
 }
+
+// x lies in the subtree whose interval is w (x's preorder number px).
+__device__ __forceinline__ bool iv_in(int2 w, int px) { return (unsigned)(px - w.x) < (unsigned)w.y; }
 
 // --------------------------------------------------------------- helpers ---
 // A column dual as the int32 sweep sees it; sets `wide` when it does not fit.
@@ -186,6 +200,8 @@ __device__ __forceinline__ int64_t warp_sum_i64(int64_t v) {
 struct BlockScratch {
     uint64_t red[32];
     uint64_t red2[32];
+    uint64_t red3[32];
+    uint64_t red4[32];
     int32_t i[8];
 };
 
@@ -230,6 +246,36 @@ __device__ __forceinline__ int64_t block_sum_i64(int64_t v, BlockScratch& bs) {
     }
     __syncthreads();
     return (int64_t)bs.red[0];
+}
+
+// Two independent lexicographic minima of (a, b) and (c, d) pairs over the
+// block, in one pass of barriers; every thread gets both results.
+__device__ __forceinline__ void pair_min_into(uint64_t& a, uint64_t& b, uint64_t c, uint64_t d) {
+    if (c < a || (c == a && d < b)) { a = c; b = d; }
+}
+__device__ __forceinline__ void warp_min_pairs(uint64_t& a, uint64_t& b, uint64_t& c, uint64_t& d) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t a2 = __shfl_xor_sync(0xffffffffu, a, o), b2 = __shfl_xor_sync(0xffffffffu, b, o);
+        const uint64_t c2 = __shfl_xor_sync(0xffffffffu, c, o), d2 = __shfl_xor_sync(0xffffffffu, d, o);
+        pair_min_into(a, b, a2, b2);
+        pair_min_into(c, d, c2, d2);
+    }
+}
+__device__ __forceinline__ void block_min_pairs(uint64_t& a, uint64_t& b, uint64_t& c, uint64_t& d, BlockScratch& bs) {
+    warp_min_pairs(a, b, c, d);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) { bs.red[w] = a; bs.red2[w] = b; bs.red3[w] = c; bs.red4[w] = d; }
+    __syncthreads();
+    if (w == 0) {
+        uint64_t x = kNoKey, y = kNoKey, z = kNoKey, u = kNoKey;
+        if (l < nw) { x = bs.red[l]; y = bs.red2[l]; z = bs.red3[l]; u = bs.red4[l]; }
+        warp_min_pairs(x, y, z, u);
+        if (l == 0) { bs.red[0] = x; bs.red2[0] = y; bs.red3[0] = z; bs.red4[0] = u; }
+    }
+    __syncthreads();
+    a = bs.red[0]; b = bs.red2[0]; c = bs.red3[0]; d = bs.red4[0];
 }
 
 // Two smallest keys: insert / merge.

@@ -1,10 +1,10 @@
 // cuda_emu.h -- runs the CTA-level device code of this library on the host:
-// one CTA = 32 fibers (one warp) on one OS thread, __syncthreads and warp
-// shuffles are real barriers that also check that all threads reached the
-// same call site, atomics are std::atomic_ref.  Used by the host test harness
-// (emu_check.cpp) to execute the unmodified device functions under
-// AddressSanitizer / UndefinedBehaviorSanitizer, so that out-of-bounds
-// accesses in the device logic show up on the CPU.
+// one CTA = 32 to 256 fibers (whole warps) on one OS thread; __syncthreads is
+// a CTA barrier and a warp shuffle a barrier of its warp, both checking that
+// every thread arrived from the same call site; atomics are std::atomic_ref.
+// Used by the host test harness (emu_check.cpp) to execute the unmodified
+// device functions under AddressSanitizer / UndefinedBehaviorSanitizer, so
+// that out-of-bounds accesses in the device logic show up on the CPU.
 #pragma once
 #include <ucontext.h>
 #include <atomic>
@@ -26,22 +26,25 @@
 
 struct int4 { int x, y, z, w; };
 inline int4 make_int4(int x, int y, int z, int w) { return int4{x, y, z, w}; }
+struct int2 { int x, y; };
+inline int2 make_int2(int x, int y) { return int2{x, y}; }
 struct EmuDim { unsigned x = 0, y = 0, z = 0; };
 
 namespace emu {
-constexpr int kLanes = 32;
-// One CTA = 32 fibers on the calling OS thread; a barrier switches back to
-// the scheduler, which resumes the fibers once all of them have arrived.
+constexpr int kMaxThreads = 256;
+// One CTA = blockDim.x fibers on the calling OS thread; a barrier switches
+// back to the scheduler, which resumes a warp once all its threads reached a
+// warp barrier, and the CTA once every thread reached a CTA barrier.
 struct Cta {
     ucontext_t sched;
-    ucontext_t fib[kLanes];
-    std::vector<char> stack[kLanes];
-    bool arrived[kLanes];
-    bool finished[kLanes];
+    ucontext_t fib[kMaxThreads];
+    std::vector<char> stack[kMaxThreads];
+    int wait[kMaxThreads];     // 0 running, 1 at a CTA barrier, 2 at a warp barrier
+    bool finished[kMaxThreads];
     int cur = 0;
-    uint64_t xchg[kLanes];
+    uint64_t xchg[kMaxThreads];
     std::atomic<int> any{0};
-    int site[kLanes];          // call site of each thread's current barrier
+    int site[kMaxThreads];     // call site of each thread's current barrier
     int mismatches = 0;
     long long barriers = 0;
 };
@@ -49,7 +52,7 @@ inline Cta*& cta() { static Cta* c = nullptr; return c; }
 inline EmuDim tid;
 }  // namespace emu
 
-static const EmuDim blockDim{32, 1, 1};
+inline EmuDim blockDim{32, 1, 1};   // set before run_cta: a multiple of 32, at most kMaxThreads
 static const EmuDim blockIdx{0, 0, 0};
 static const EmuDim gridDim{1, 1, 1};
 #define threadIdx (emu::tid)
@@ -58,14 +61,16 @@ namespace emu {
 // Every barrier (including the ones inside emulated shuffles) records its call
 // site; threads meeting at one barrier phase from different sites means a
 // __syncthreads() was reached divergently.
-inline void sync_at(int line) {
+inline void wait_at(int line, int kind) {
     Cta* c = cta();
     const int me = c->cur;
     c->site[me] = line;
-    c->arrived[me] = true;
+    c->wait[me] = kind;
     swapcontext(&c->fib[me], &c->sched);
     tid.x = (unsigned)me;
 }
+inline void sync_at(int line) { wait_at(line, 1); }
+inline void warp_sync_at(int line) { wait_at(line, 2); }
 }  // namespace emu
 #define __syncthreads() emu::sync_at(__LINE__)
 #define __syncthreads_or(p) emu::sync_or(p, __LINE__)
@@ -83,25 +88,25 @@ inline int sync_or(int p, int line) {
 }
 }  // namespace emu
 
+// src: the source thread (in the caller's warp)
 template <class T>
-inline T emu_shfl(T v, int src_lane) {
+inline T emu_shfl(T v, int src) {
     emu::Cta* c = emu::cta();
     uint64_t bits = 0;
     memcpy(&bits, &v, sizeof(T));
-    emu::sync_at(-1);
+    emu::warp_sync_at(-1);
     c->xchg[threadIdx.x] = bits;
-    emu::sync_at(-2);
-    uint64_t got = c->xchg[src_lane];
-    emu::sync_at(-3);
+    emu::warp_sync_at(-2);
+    uint64_t got = c->xchg[src];
+    emu::warp_sync_at(-3);
     T out;
     memcpy(&out, &got, sizeof(T));
     return out;
 }
-template <class T> inline T __shfl_xor_sync(unsigned, T v, int o) { return emu_shfl(v, (int)(threadIdx.x ^ o)); }
+template <class T> inline T __shfl_xor_sync(unsigned, T v, int o) { return emu_shfl(v, (int)(threadIdx.x ^ (o & 31))); }
 template <class T> inline T __shfl_up_sync(unsigned, T v, int o) {
-    const int src = (int)threadIdx.x - o;
-    T got = emu_shfl(v, src < 0 ? (int)threadIdx.x : src);
-    return got;
+    const int lane = (int)(threadIdx.x & 31);
+    return emu_shfl(v, lane >= o ? (int)threadIdx.x - o : (int)threadIdx.x);
 }
 
 template <class T, class U> inline T atomicAdd(T* p, U v) { return std::atomic_ref<T>(*p).fetch_add((T)v); }
@@ -135,42 +140,61 @@ inline void fiber_main() {
     c->finished[me] = true;
     swapcontext(&c->fib[me], &c->sched);
 }
-// Run f() on one emulated CTA of 32 threads.  Returns the number of barrier
-// phases whose threads arrived from different call sites (0 when every
-// __syncthreads() is reached uniformly), or -1 on a deadlock.
+// Run f() on one emulated CTA of blockDim.x threads.  Returns the number of
+// barrier phases whose threads arrived from different call sites (0 when
+// every barrier is reached uniformly), or -1 on a deadlock.
 inline int run_cta(const std::function<void()>& f) {
+    const int nt = (int)blockDim.x;
+    if (nt < 32 || nt > kMaxThreads || nt % 32) { fprintf(stderr, "emu: bad block size %d\n", nt); return -1; }
     Cta* c = new Cta();
     cta() = c;
     entry() = &f;
-    for (int t = 0; t < kLanes; t++) {
+    for (int t = 0; t < nt; t++) {
         c->stack[t].resize(1 << 17);
         getcontext(&c->fib[t]);
         c->fib[t].uc_stack.ss_sp = c->stack[t].data();
         c->fib[t].uc_stack.ss_size = c->stack[t].size();
         c->fib[t].uc_link = nullptr;
         makecontext(&c->fib[t], (void (*)())fiber_main, 0);
-        c->arrived[t] = false;
+        c->wait[t] = 0;
         c->finished[t] = false;
     }
+    auto mismatch = [&](int t0, int t) {
+        if (c->mismatches++ < 5)
+            fprintf(stderr, "barrier mismatch: thread %d at line %d, thread %d at line %d\n", t0, c->site[t0], t,
+                    c->site[t]);
+    };
     int result = 0;
     for (;;) {
-        for (int t = 0; t < kLanes; t++) {
-            if (c->finished[t] || c->arrived[t]) continue;
+        for (int t = 0; t < nt; t++) {
+            if (c->finished[t] || c->wait[t]) continue;
             c->cur = t;
             swapcontext(&c->sched, &c->fib[t]);
         }
-        int nfin = 0, narr = 0;
-        for (int t = 0; t < kLanes; t++) { nfin += c->finished[t]; narr += c->arrived[t]; }
-        if (nfin == kLanes) break;
-        if (nfin > 0) { result = -1; fprintf(stderr, "deadlock: %d threads finished, %d at a barrier\n", nfin, narr); break; }
+        int nfin = 0, ncta = 0;
+        for (int t = 0; t < nt; t++) { nfin += c->finished[t]; ncta += c->wait[t] == 1; }
+        if (nfin == nt) break;
+        // warps whose every thread waits at a warp barrier go on first
+        bool released = false;
+        for (int w = 0; w < nt / 32; w++) {
+            bool all = true;
+            for (int t = 32 * w; t < 32 * w + 32; t++) all = all && !c->finished[t] && c->wait[t] == 2;
+            if (!all) continue;
+            for (int t = 32 * w + 1; t < 32 * w + 32; t++)
+                if (c->site[t] != c->site[32 * w]) { mismatch(32 * w, t); break; }
+            for (int t = 32 * w; t < 32 * w + 32; t++) c->wait[t] = 0;
+            released = true;
+        }
+        if (released) continue;
+        if (nfin > 0 || ncta != nt) {
+            result = -1;
+            fprintf(stderr, "deadlock: %d threads finished, %d at a CTA barrier\n", nfin, ncta);
+            break;
+        }
         c->barriers++;
-        for (int t = 1; t < kLanes; t++)
-            if (c->site[t] != c->site[0]) {
-                if (c->mismatches++ < 5)
-                    fprintf(stderr, "barrier mismatch: thread 0 at line %d, thread %d at line %d\n", c->site[0], t, c->site[t]);
-                break;
-            }
-        for (int t = 0; t < kLanes; t++) c->arrived[t] = false;
+        for (int t = 1; t < nt; t++)
+            if (c->site[t] != c->site[0]) { mismatch(0, t); break; }
+        for (int t = 0; t < nt; t++) c->wait[t] = 0;
     }
     if (result == 0) result = c->mismatches;
     cta() = nullptr;

@@ -4,6 +4,11 @@
 // device logic.  Instances come from the library's generator.
 //   emu_check <seed> <count> <lo> <hi> <first> <last> [mode] [pricing: 0 full, 1 partial, 2 partial + row keys
 //   scrambled between rounds]
+// Environment: EMU_THREADS (block size, a multiple of 32, default 32),
+// EMU_VERIFY (1, default: after every single pivot the incrementally updated
+// depths, duals, int32 duals and preorder intervals are checked against a full
+// rebuild), EMU_COST_HI / EMU_QTY_LO / EMU_QTY_HI (generator ranges; small
+// ranges give ties and degenerate bases).
 #define FLOCK_EMU
 #include <cstdio>
 #include <cstdlib>
@@ -19,6 +24,62 @@ using namespace flock;
 template <class T> static T* arr(std::vector<std::unique_ptr<char[]>>& keep, size_t n) {
     keep.emplace_back(new char[n * sizeof(T) + 1]);
     return (T*)keep.back().get();
+}
+
+static int verify = 1;
+
+// The tree's derived state as the single pivot leaves it.
+struct TreeState {
+    std::vector<int32_t> depth, v32;
+    std::vector<int64_t> pot;
+    std::vector<int2> iv;
+    int32_t ivp = 0, nwide = 0, narrow = 0;
+};
+
+static void save_tree(const Ctx& c, int V, TreeState& t) {
+    t.depth.assign(c.depth, c.depth + V);
+    t.pot.assign(c.pot, c.pot + V);
+    t.v32.assign(c.v32, c.v32 + c.I.n);
+    t.iv.assign(c.iv, c.iv + 2 * (size_t)V);
+    t.ivp = c.sc->ivp; t.nwide = c.sc->nwide; t.narrow = c.sc->narrow;
+}
+
+static void restore_tree(const Ctx& c, int V, const TreeState& t) {
+    memcpy(c.depth, t.depth.data(), 4 * (size_t)V);
+    memcpy(c.pot, t.pot.data(), 8 * (size_t)V);
+    memcpy(c.v32, t.v32.data(), 4 * (size_t)c.I.n);
+    memcpy(c.iv, t.iv.data(), sizeof(int2) * 2 * (size_t)V);
+    c.sc->ivp = t.ivp; c.sc->nwide = t.nwide; c.sc->narrow = t.narrow;
+}
+
+// Compare the incremental state `t` with the rebuilt one in `c`: depths,
+// duals, int32 duals and the wide count exactly; intervals by their meaning
+// (any preorder is valid): sizes equal, preorder numbers a permutation of
+// 0..alive-1, every vertex's number inside its parent's interval.
+static void check_incremental(const Ctx& c, int V, const TreeState& t, int* errors) {
+    auto bad = [&](const char* what, int v, long long a, long long b) {
+        if ((*errors)++ < 8) fprintf(stderr, "  %s at vertex %d: incremental %lld, rebuilt %lld\n", what, v, a, b);
+    };
+    const int m = c.I.m;
+    const int2* inc = t.iv.data() + (t.ivp ? V : 0);
+    const int2* reb = c.iv + (c.sc->ivp ? V : 0);
+    std::vector<int> seen(V, 0);
+    int alive = 0;
+    for (int v = 0; v < V; v++) {
+        if (c.parent[v] == -2) continue;
+        alive++;
+        if (t.depth[v] != c.depth[v]) bad("depth", v, t.depth[v], c.depth[v]);
+        if (t.pot[v] != c.pot[v]) bad("dual", v, t.pot[v], c.pot[v]);
+        if (v >= m && t.v32[v - m] != c.v32[v - m]) bad("int32 dual", v, t.v32[v - m], c.v32[v - m]);
+        if (inc[v].y != reb[v].y) bad("subtree size", v, inc[v].y, reb[v].y);
+        if (inc[v].x < 0 || inc[v].x >= V || seen[inc[v].x]++) bad("preorder number", v, inc[v].x, reb[v].x);
+        const int p = c.parent[v];
+        if (p >= 0 && (inc[v].x == inc[p].x || !iv_in(inc[p], inc[v].x))) bad("interval nesting", v, inc[v].x, inc[p].x);
+    }
+    for (int v = 0; v < V; v++)
+        if (c.parent[v] != -2 && inc[v].x >= alive) bad("preorder range", v, inc[v].x, alive);
+    if (t.nwide != c.sc->nwide) bad("wide count", -1, t.nwide, c.sc->nwide);
+    if (t.narrow != c.sc->narrow) bad("narrow flag", -1, t.narrow, c.sc->narrow);
 }
 
 static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int32_t* cost, int mode, int pricing,
@@ -44,11 +105,8 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.pot = arr<int64_t>(keep, V);
     c.v32 = arr<int32_t>(keep, V);
     c.prow = arr<int32_t>(keep, kPPRows);
-    c.lift_cap = lift_levels(V);
-    c.lift = arr<int32_t>(keep, (size_t)V * c.lift_cap);
-    c.anc0 = arr<int32_t>(keep, V); c.anc1 = arr<int32_t>(keep, V);
-    c.len0 = arr<int32_t>(keep, V); c.len1 = arr<int32_t>(keep, V);
-    c.acc0 = arr<int64_t>(keep, V); c.acc1 = arr<int64_t>(keep, V);
+    c.iv = arr<int2>(keep, 2 * (size_t)V);
+    set_jump(c, arr<int64_t>(keep, jump_bytes(V) / 8), V);
     c.row_best = arr<uint64_t>(keep, m); c.claim = arr<uint64_t>(keep, V);
     c.cand = arr<int32_t>(keep, m); c.cand_theta = arr<int64_t>(keep, m);
     c.cand_q = arr<int32_t>(keep, m); c.cand_info = arr<int32_t>(keep, m);
@@ -57,14 +115,18 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.bsum = arr<int64_t>(keep, V); c.csr_start = arr<int32_t>(keep, V + 1);
     c.csr_adj = arr<int32_t>(keep, 2 * V); c.order = arr<int32_t>(keep, V); c.uf = arr<int32_t>(keep, V);
     BlockScratch bs;
+    TreeState saved;
+    int inc_errors = 0;
     const int mism = emu::run_cta([&] {
         vogel_cta(c, bs);
         if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
         __syncthreads();
         sf_init_cta(c, bs);
-        if (!c.sc->done) tree_recompute_cta(c, bs);
+        if (!c.sc->done) tree_build_cta(c, bs);
         uint64_t junk = 0x9E3779B97F4A7C15ull;
         for (;;) {
+            if (c.sc->done) break;
+            if (c.sc->stale) tree_build_cta(c, bs);
             if (c.sc->done) break;
             // pricing 2: row keys do not survive between rounds (as in the
             // round form, which stages them afresh): fill them with garbage
@@ -77,7 +139,17 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
             if (threadIdx.x == 0) c.sc->rounds++;
             __syncthreads();
             if (c.sc->done) break;
-            tree_recompute_cta(c, bs);
+            if (verify && !c.sc->stale) {
+                if (threadIdx.x == 0) save_tree(c, V, saved);
+                __syncthreads();
+                tree_build_cta(c, bs);
+                if (threadIdx.x == 0) {
+                    check_incremental(c, V, saved, &inc_errors);
+                    restore_tree(c, V, saved);
+                }
+                __syncthreads();
+                if (inc_errors) break;
+            }
         }
         if (!(c.sc->status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE))) {
             finalize_cta(c, bs);
@@ -86,6 +158,10 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
         }
     });
     *out = *sc;
+    if (inc_errors) {
+        fprintf(stderr, "incremental tree state differs from the rebuild (%d errors)\n", inc_errors);
+        return mism ? mism : 1;
+    }
     return mism;
 }
 
@@ -98,11 +174,15 @@ int main(int argc, char** argv) {
     const int pricing = argc > 8 ? atoi(argv[8]) : 0;
     std::vector<int32_t> ms(count), ns(count);
     flock_generate_sizes(seed, count, lo, hi, ms.data(), ns.data());
+    auto env = [](const char* k, int dflt) { const char* v = getenv(k); return v ? atoi(v) : dflt; };
+    blockDim.x = (unsigned)env("EMU_THREADS", 32);
+    verify = env("EMU_VERIFY", 1);
+    const int cost_hi = env("EMU_COST_HI", 1000), qlo = env("EMU_QTY_LO", 100), qhi = env("EMU_QTY_HI", 1000);
     int bad = 0;
     for (int k = first; k <= last && k < count; k++) {
         const int m = ms[k], n = ns[k];
         std::vector<int32_t> s(m), d(n), c((size_t)m * n);
-        flock_generate(0, seed * 1000003ull + k + 1, m, n, 1, 1000, 100, 1000, s.data(), d.data(), c.data());
+        flock_generate(0, seed * 1000003ull + k + 1, m, n, 1, cost_hi, qlo, qhi, s.data(), d.data(), c.data());
         Scalars r;
         const int mism = solve_one(m, n, s.data(), d.data(), c.data(), mode, pricing, &r);
         const bool ok = r.status == 0 && r.cert == 0 && mism == 0;

@@ -28,8 +28,7 @@ struct BatchArgs {
     int32_t* active;            // round kernel: instances still running after the round
     int32_t maxV, maxM;         // largest instance of the launch (shared-memory staging size)
     int32_t bfs_method, mode, max_rounds;
-    int32_t light;              // 1: stage only the per-step tree arrays (largest bucket)
-    int32_t lift;               // 1: stage the binary-lifting table (parallel single pivots)
+    int32_t light;              // 1: stage only the per-step tree arrays (largest buckets)
     int32_t pricing;            // Scalars::pricing of every instance
 };
 
@@ -66,12 +65,8 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.depth = (int32_t*)k.S(4 * v);
     c.flow = (int64_t*)k.S(8 * v);
     c.claim = (uint64_t*)k.S(8 * v);
-    c.anc0 = (int32_t*)k.S(4 * v);
-    c.anc1 = (int32_t*)k.S(4 * v);
-    c.len0 = (int32_t*)k.S(4 * v);
-    c.len1 = (int32_t*)k.S(4 * v);
-    c.acc0 = (int64_t*)k.S(8 * v);
-    c.acc1 = (int64_t*)k.S(8 * v);
+    set_jump(c, k.S(jump_bytes(V)), V);
+    c.iv = (int2*)k.S(16 * v);
     c.row_best = (uint64_t*)k.S(8 * mm);
     c.pot = smem ? (int64_t*)k.S(8 * v) : (pot_global ? pot_global : (int64_t*)k.G(8 * v));
     c.v32 = (int32_t*)k.S(4 * v);
@@ -93,8 +88,6 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.csr_adj = (int32_t*)k.G(8 * v);
     c.order = (int32_t*)k.G(4 * v);
     c.uf = (int32_t*)k.G(4 * v);
-    c.lift_cap = lift_levels(V);
-    c.lift = (int32_t*)k.G(4 * v * (size_t)c.lift_cap);
     if (smem_bytes) *smem_bytes = k.so;
     if (global_bytes) *global_bytes = (k.go + 255) & ~size_t(255);
 }

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method) {
     }
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
     sf_init_cta(c, bs);
-    if (!c.sc->done) tree_recompute_cta<kJumpPlain>(c, bs);
+    if (!c.sc->done) tree_build_cta<kJumpPlain>(c, bs);
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
         if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
     }
     __syncthreads();
-    if (!c.sc->done) tree_recompute_cta<kJumpPlain>(c, bs);
+    if (!c.sc->done && c.sc->stale) tree_build_cta<kJumpPlain>(c, bs);
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
@@ -147,20 +147,27 @@ __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
 // The plain solver's pivot round for large instances, spread over the whole
 // GPU: one pivot per round (Dantzig's rule: the most negative row key, first
 // row among ties), every step a grid-wide kernel, the kernel boundaries the
-// only synchronisation.  The steps follow single_pivot_lift and
-// tree_recompute_cta exactly (same cycle membership test, tie rules, re-hang
-// and pointer-jumping passes); a pass kernel whose predecessor left no vertex
-// pending returns at once, so a round costs the passes its tree needs.
+// only synchronisation.  The steps follow single_pivot_iv exactly (same
+// interval membership test, tie rules, path reversal and in-place update of
+// depths, duals and intervals), so a round costs six short kernels whatever
+// the tree's depth.
 struct GridPivot {
     uint64_t best;          // entering candidate: (reduced cost, row)
     uint64_t mk, ml;        // per side: minimum order-preserving flow
     uint64_t qk, ql;        // per side: leaving edge (depth << 32 | child)
-    int32_t wide;           // a column dual left the int32 window
     int32_t full;           // partial pricing: this round sweeps every row
-    int32_t pend[48];       // pointer-jumping pass it left vertices pending
+    int32_t npath;          // path vertices recorded by k_gapply
+    int32_t dwide;          // change of the count of int32-window misses
+    int32_t pad_;
+    // the pivot, fixed by k_gapply before k_gupdate changes depths and duals
+    int64_t th, r;
+    int32_t ok, e, other, q, de, dq, t, dother, eside, pad2_;
+    int2 Q, O;
 };
 
 constexpr int kGridPivotV = 4096;     // plain instances with m + n >= this use the grid round
+
+__device__ __forceinline__ const int2* iv_now(const Ctx& c, int V) { return c.iv + (c.sc->ivp ? V : 0); }
 
 __global__ void __launch_bounds__(1024, 1) k_gselect(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
@@ -182,7 +189,9 @@ __global__ void __launch_bounds__(1024, 1) k_gselect(Ctx c, GridPivot* gp) {
         gp->mk = gp->ml = kNoKey;
         gp->qk = 0;
         gp->ql = kNoKey;
-        gp->wide = 0;
+        gp->npath = 0;
+        gp->dwide = 0;
+        gp->ok = 0;
         c.sc->rounds++;
         c.sc->ncand = best == kNoKey ? 0 : 1;
         if (best == kNoKey) c.sc->done = 1;
@@ -195,17 +204,14 @@ __global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
     const int m = c.I.m, V = m + c.I.n;
     const int k = (int)key_idx(gp->best);
     const int l = m + (int)key_idx(c.row_best[k]);
-    const int dk = c.depth[k], dl = c.depth[l];
+    const int2* iv = iv_now(c, V);
+    const int pk = iv[k].x, pl = iv[l].x;
     uint64_t mk = kNoKey, ml = kNoKey;
-    int lbad = 0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         int side = 0;
         if (c.parent[v] >= 0) {
-            const int dv = c.depth[v];
-            int xk = dv <= dk ? kth_anc(c, V, k, dk - dv) : -1;
-            int xl = dv <= dl ? kth_anc(c, V, l, dl - dv) : -1;
-            if ((dv <= dk && xk < 0) || (dv <= dl && xl < 0)) lbad = 1;
-            const bool on_k = xk == v, on_l = xl == v;
+            const int2 w = iv[v];
+            const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
             if (on_k != on_l) side = on_k ? 1 : 2;
         }
         c.claim[v] = (uint64_t)side;
@@ -214,11 +220,9 @@ __global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
     }
     mk = block_min_u64(mk, bs);
     ml = block_min_u64(ml, bs);
-    lbad = __syncthreads_or(lbad);
     if (threadIdx.x == 0) {
         if (mk != kNoKey) atomicMin((unsigned long long*)&gp->mk, (unsigned long long)mk);
         if (ml != kNoKey) atomicMin((unsigned long long*)&gp->ml, (unsigned long long)ml);
-        if (lbad) fail_check(c.sc, 16);
     }
 }
 
@@ -248,158 +252,153 @@ __global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
     }
 }
 
-// The pivot's parameters, read by every thread of the apply and commit steps.
-struct GridPivotArgs {
-    bool ok, lside;
-    int q, e, other, de, dq;
-    uint64_t eside;
-    int64_t th;
-};
-
-__device__ __forceinline__ GridPivotArgs grid_pivot_args(const Ctx& c, const GridPivot* gp) {
-    GridPivotArgs p;
-    const int m = c.I.m, V = m + c.I.n;
-    p.lside = gp->ml <= gp->mk;
-    const uint64_t fmin = p.lside ? gp->ml : gp->mk;
-    const uint64_t pick = p.lside ? gp->ql : gp->qk;
-    p.ok = fmin != kNoKey && (p.lside ? pick != kNoKey : pick != 0);
-    p.q = (int)(uint32_t)pick;
-    p.ok = p.ok && FLOCK_IN(p.q, V);
-    p.th = (int64_t)(fmin ^ 0x8000000000000000ull);
-    const int k = (int)key_idx(gp->best);
-    const int l = m + (int)key_idx(c.row_best[k]);
-    p.e = p.lside ? l : k;
-    p.other = p.lside ? k : l;
-    p.de = c.depth[p.e];
-    p.dq = p.ok ? c.depth[p.q] : 0;
-    p.eside = p.lside ? 2 : 1;
-    return p;
-}
-
-// Flows along the cycle change by -/+theta; the segment from the leaving edge
-// down to the entering endpoint gets its new parents and flows in len1/acc1
-// (its own flows are read here and replaced in k_gcommit, so no vertex reads
-// a flow that this kernel writes).
+// Flows along the cycle change by -/+theta except on the path from the
+// entering endpoint e up to the leaving edge, whose vertices are recorded by
+// index (len1) with their updated flows (acc1) for k_gupdate.  Block 0 also
+// fixes the pivot's parameters in gp (nothing here changes depths, duals or
+// intervals, so every block computes the same ones).
 __global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
+    __shared__ int s_n;
     if (c.sc->done) return;
     const int m = c.I.m, V = m + c.I.n;
-    const GridPivotArgs p = grid_pivot_args(c, gp);
-    if (!p.ok) {
+    const bool lside = gp->ml <= gp->mk;
+    const uint64_t fmin = lside ? gp->ml : gp->mk;
+    const uint64_t pick = lside ? gp->ql : gp->qk;
+    const int q = (int)(uint32_t)pick;
+    if (fmin == kNoKey || (lside ? pick == kNoKey : pick == 0) || !FLOCK_IN(q, V) || c.parent[q] < 0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
         return;
     }
+    const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
+    const int k = (int)key_idx(gp->best);
+    const int l = m + (int)key_idx(c.row_best[k]);
+    const int e = lside ? l : k, other = lside ? k : l;
+    const int de = c.depth[e], dq = c.depth[q], t = de - dq;
+    if (!FLOCK_IN(t, V)) {                         // the path indexes len1/acc1 (V entries)
+        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
+        return;
+    }
+    const uint64_t eside = lside ? 2 : 1;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    int n = 0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const uint64_t sd = c.claim[v];
         if (!sd) continue;
-        const int64_t delta = (sd == 1) == (v < m) ? -p.th : p.th;
-        if (sd == p.eside && c.depth[v] >= p.dq) {
-            const int prev = v == p.e ? p.other : kth_anc(c, V, p.e, p.de - c.depth[v] - 1);
-            if (!FLOCK_IN(prev, V)) { fail_check(c.sc, 17); continue; }
-            c.len1[v] = prev;
-            c.acc1[v] = v == p.e ? p.th : c.flow[prev] + ((p.eside == 1) == (prev < m) ? -p.th : p.th);
+        const int64_t delta = (sd == 1) == (v < m) ? -th : th;
+        const int dv = c.depth[v];
+        if (sd == eside && dv >= dq) {
+            const int i = de - dv;
+            if (!FLOCK_IN(i, t + 1)) { fail_check(c.sc, 17); continue; }
+            c.len1[i] = v;
+            c.acc1[i] = c.flow[v] + delta;
+            n++;
         } else {
             c.flow[v] += delta;
         }
     }
-}
-
-__global__ void __launch_bounds__(256) k_gcommit(Ctx c, GridPivot* gp) {
-    if (c.sc->done) return;
-    const int m = c.I.m, V = m + c.I.n;
-    const GridPivotArgs p = grid_pivot_args(c, gp);
-    if (!p.ok) return;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        if (c.claim[v] != p.eside || c.depth[v] < p.dq) continue;
-        c.parent[v] = c.len1[v];
-        c.flow[v] = c.acc1[v];
-    }
+    if (n) atomicAdd(&s_n, n);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_n) atomicAdd(&gp->npath, s_n);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        c.sc->pivots++;
-        c.sc->last_winners = 1;
+        const int2* iv = iv_now(c, V);
+        gp->th = th;
+        gp->r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
+        gp->e = e; gp->other = other; gp->q = q;
+        gp->de = de; gp->dq = dq; gp->t = t;
+        gp->dother = c.depth[other];
+        gp->eside = (int32_t)eside;
+        gp->Q = iv[q]; gp->O = iv[other];
+        gp->ok = 1;
     }
 }
 
-// Dual recompute over the grid: level 0 of the lifting table, then one kernel
-// per doubling pass, then the depths, duals and int32 duals.
-__global__ void __launch_bounds__(256) k_gjump_init(Ctx c, GridPivot* gp) {
-    if (c.sc->done) return;
-    const InstDev& I = c.I;
-    const int V = I.m + I.n, root = c.sc->root;
-    if (blockIdx.x == 0 && threadIdx.x < 48) gp->pend[threadIdx.x] = 0;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const int p = c.parent[v];
-        if (p == -2) { c.lift[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
-        else if (v == root) { c.lift[v] = v; c.len0[v] = 0; c.acc0[v] = 0; }
-        else if (!FLOCK_IN(p, V) || (p < I.m) == (v < I.m)) { fail_check(c.sc, 20); c.lift[v] = root; c.len0[v] = 0; c.acc0[v] = 0; }
-        else { c.lift[v] = p; c.len0[v] = 1; c.acc0[v] = edge_cost(I, v, p); }
-    }
-}
-
-__global__ void __launch_bounds__(256) k_gjump(Ctx c, GridPivot* gp, int it) {
-    __shared__ int s_any;
-    if (c.sc->done) return;
-    if (it > 0 && gp->pend[it - 1] == 0) return;        // the tree was done a pass ago
-    const int V = c.I.m + c.I.n, root = c.sc->root;
-    const int32_t* aA = c.lift + (size_t)it * V;
-    int32_t* aB = c.lift + (size_t)(it + 1) * V;
-    const int32_t* lA = (it & 1) ? c.len1 : c.len0;
-    int32_t* lB = (it & 1) ? c.len0 : c.len1;
-    const int64_t* xA = (it & 1) ? c.acc1 : c.acc0;
-    int64_t* xB = (it & 1) ? c.acc0 : c.acc1;
-    if (threadIdx.x == 0) s_any = 0;
-    __syncthreads();
-    int mine = 0;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const int a = aA[v];
-        if (a < 0 || a == root) { aB[v] = a; lB[v] = lA[v]; xB[v] = xA[v]; continue; }
-        if (!FLOCK_IN(a, V)) { fail_check(c.sc, 21); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
-        const int aa = aA[a];
-        if (!FLOCK_IN(aa, V)) { fail_check(c.sc, 22); aB[v] = root; lB[v] = 0; xB[v] = 0; continue; }
-        const int la = lA[v];
-        aB[v] = aa;
-        lB[v] = la + lA[a];
-        xB[v] = xA[v] + ((la & 1) ? -xA[a] : xA[a]);
-        mine |= (aa != root);
-    }
-    if (mine) s_any = 1;
-    __syncthreads();
-    if (threadIdx.x == 0 && s_any) atomicOr(&gp->pend[it], 1);
-}
-
-__global__ void __launch_bounds__(256) k_gjump_final(Ctx c, GridPivot* gp) {
-    __shared__ int s_wide;
+// The tree update of single_pivot_iv over the grid: new intervals into the
+// other half of iv, depths and duals of the re-hung subtree, the reversed
+// path's parents and flows; every row key cleared for the next sweep.
+__global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
+    __shared__ int s_w;
     if (c.sc->done) return;
     const int m = c.I.m, V = m + c.I.n;
-    const int passes = c.lift_cap - 1;
-    int p = -1;                                           // final level
-    for (int it = 0; it < passes; it++)
-        if (gp->pend[it] == 0) { p = it + 1; break; }
-    if (p < 0) {                                          // still pending: not a tree
-        if (blockIdx.x == 0 && threadIdx.x == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+    const int t = gp->t, q = gp->q;
+    if (!gp->ok || !FLOCK_IN(t, V) || gp->npath != t + 1 || c.len1[t] != q) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
         return;
     }
-    const int32_t* lF = (p & 1) ? c.len1 : c.len0;
-    const int64_t* xF = (p & 1) ? c.acc1 : c.acc0;
-    if (threadIdx.x == 0) s_wide = 0;
+    const int par = c.sc->ivp;
+    const int2* ivA = c.iv + (par ? V : 0);
+    int2* ivB = c.iv + (par ? 0 : V);
+    const int2 Q = gp->Q, O = gp->O;
+    const int P = Q.x, s = Q.y;
+    const int ins = O.x - (O.x >= P + s ? s : 0) + 1;
+    const int dnew = gp->dother + 1 - gp->de;
+    const int other = gp->other;
+    const bool erow = gp->e < m;
+    const int64_t r = gp->r, th = gp->th;
+    const int32_t* path = c.len1;
+    const int64_t* pflow = c.acc1;
+    if (threadIdx.x == 0) s_w = 0;
     __syncthreads();
-    int wide = 0;
+    int dwide = 0, bad = 0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const int64_t pv = xF[v];
-        c.depth[v] = lF[v];
-        c.pot[v] = pv;
-        if (v >= m) c.v32[v - m] = narrow_dual(pv, wide);
+        if (c.parent[v] == -2) continue;
+        const int2 w = ivA[v];
+        int2 nw;
+        if (iv_in(Q, w.x)) {
+            int lo = 0, hi = t;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const int pv = path[mid];
+                if (!FLOCK_IN(pv, V)) { bad = 1; break; }
+                if (iv_in(ivA[pv], w.x)) hi = mid; else lo = mid + 1;
+            }
+            const int i = lo;
+            const int pi = path[i];
+            if (!FLOCK_IN(pi, V)) { bad = 1; continue; }
+            const int2 Pi = ivA[pi];
+            int off = 0, rank = w.x - Pi.x;
+            if (i > 0) {
+                const int pc = path[i - 1];
+                if (!FLOCK_IN(pc, V)) { bad = 1; continue; }
+                const int2 Pc = ivA[pc];
+                off = Pc.y;
+                if (w.x >= Pc.x) rank -= Pc.y;
+            }
+            nw.x = ins + off + rank;
+            nw.y = v == pi ? s - off : w.y;
+            c.depth[v] = dnew + 2 * i + c.depth[v];
+            const int64_t p0 = c.pot[v];
+            const int64_t p1 = p0 + ((v < m) == erow ? r : -r);
+            c.pot[v] = p1;
+            if (v >= m) {
+                int w0 = 0, w1 = 0;
+                narrow_dual(p0, w0);
+                c.v32[v - m] = narrow_dual(p1, w1);
+                dwide += w1 - w0;
+            }
+            if (v == pi) {
+                c.parent[v] = i == 0 ? other : path[i - 1];
+                c.flow[v] = i == 0 ? th : pflow[i - 1];
+            }
+        } else {
+            const int y = w.x - (w.x >= P + s ? s : 0);
+            nw.x = y + (y >= ins ? s : 0);
+            nw.y = w.y - (iv_in(w, P) ? s : 0) + (iv_in(w, O.x) ? s : 0);
+        }
+        ivB[v] = nw;
     }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) c.row_best[i] = kNoKey;
-    if (wide) s_wide = 1;
+    if (bad) fail_check(c.sc, 24);
+    if (dwide) atomicAdd(&s_w, dwide);
     __syncthreads();
-    if (threadIdx.x == 0 && s_wide) atomicOr(&gp->wide, 1);
+    if (threadIdx.x == 0 && s_w) atomicAdd(&gp->dwide, s_w);
 }
 
 // Partial pricing on the plain path (large instances): decide whether this
 // round sweeps every row, re-price the candidates otherwise (k_sweep with the
 // row list), fall back to a full sweep in the same round when they hold no
 // negative key, and after a full sweep choose the next candidates.  Rows
-// without a key this round keep kNoKey (k_gjump_final clears every key).
+// without a key this round keep kNoKey (k_gupdate clears every key).
 __global__ void k_pdecide(Ctx c, GridPivot* gp) {
     if (threadIdx.x != 0 || c.sc->done) return;
     const int pn = c.sc->pp_n;
@@ -425,10 +424,15 @@ __global__ void __launch_bounds__(1024, 1) k_pselect_rows(Ctx c, GridPivot* gp) 
     if (threadIdx.x == 0) c.sc->pp_age++;
 }
 
-// End of a grid round: the int32 dual flag and the round cap.
+// End of a grid round: the current interval buffer, the int32 dual flag,
+// the pivot count and the round cap.
 __global__ void k_gend(Ctx c, GridPivot* gp) {
     if (threadIdx.x != 0 || c.sc->done) return;
-    c.sc->narrow = gp->wide ? 0 : 1;
+    c.sc->ivp ^= 1;
+    c.sc->nwide += gp->dwide;
+    c.sc->narrow = c.sc->nwide == 0;
+    c.sc->pivots++;
+    c.sc->last_winners = 1;
     if (c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
 }
 
@@ -564,16 +568,16 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
     }
 }
 
-// Shared-memory staging of the arrays every pivot step touches.  Light
-// staging (the largest bucket) keeps the pointer-jumping buffers and the
-// edge claims in the instance's global working set.  The binary-lifting
-// table (which replaces the two pointer-jumping ancestor buffers and makes
-// single-candidate pivots fully parallel) is staged when it fits (kLift),
-// else it stays in the global working set.  Every pointer is carved
-// from the extern shared base and the flags are compile-time constants, so
-// the compiler knows they address shared memory (shared loads and atomics
-// rather than generic ones).  staged_bytes() below follows the same order.
-template <bool kLight, bool kLift>
+// Shared-memory staging of the arrays every pivot step touches: the tree,
+// the duals, the row keys and the preorder intervals.  Full staging adds the
+// edge claims and the pointer-jumping block (used by the rebuilds, i.e. the
+// first round and the rounds after multi-pivot rounds); light staging (the
+// largest instances) keeps those two in the instance's global working set.
+// Every pointer is carved from the extern shared base and the flag is a
+// compile-time constant, so the compiler knows they address shared memory
+// (shared loads and atomics rather than generic ones).  staged_bytes() below
+// follows the same order.
+template <bool kLight>
 __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
     Carver k{nullptr, 0, smem, 0};
     c.parent = (int32_t*)k.S(4 * (size_t)V);
@@ -582,56 +586,44 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     c.row_best = (uint64_t*)k.S(8 * (size_t)M);
     c.pot = (int64_t*)k.S(8 * (size_t)V);
     c.v32 = (int32_t*)k.S(4 * (size_t)V);
-    // Without kLift the lifting table stays in the instance's global working
-    // set (carved there by batch_ctx, stride and level count of the instance).
+    c.iv = (int2*)k.S(16 * (size_t)V);
     if (kLight) return;
     c.claim = (uint64_t*)k.S(8 * (size_t)V);
-    c.len0 = (int32_t*)k.S(4 * (size_t)V);
-    c.len1 = (int32_t*)k.S(4 * (size_t)V);
-    c.acc0 = (int64_t*)k.S(8 * (size_t)V);
-    c.acc1 = (int64_t*)k.S(8 * (size_t)V);
-    if (kLift) {
-        c.lift_cap = lift_levels(V);
-        c.lift = (int32_t*)k.S(4 * (size_t)V * c.lift_cap);
-    }
-    c.anc0 = c.lift;
-    c.anc1 = c.lift;
+    set_jump(c, k.S(jump_bytes(V)), V);
 }
 
-inline size_t staged_bytes(int V, int M, bool light, bool lift) {
+inline size_t staged_bytes(int V, int M, bool light) {
     Carver k{nullptr, 0, (unsigned char*)16, 0};
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
-    k.S(4 * (size_t)V);
-    if (!light) {
-        k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)V);
-        if (lift) k.S(4 * (size_t)V * lift_levels(V));
-    }
+    k.S(4 * (size_t)V); k.S(16 * (size_t)V);
+    if (!light) { k.S(8 * (size_t)V); k.S(jump_bytes(V)); }
     return (k.so + 15) & ~size_t(15);
 }
 
 // Largest dynamic shared memory a staged launch may use.
 constexpr size_t kStageSmemMax = 226 * 1024;
 
-// Staging of a launch whose largest instance is maxV x (rows maxM): light
-// for the largest bucket, the lifting table whenever it fits.
-inline bool stage_lift(int maxV, int maxM, bool light) {
-    return !light && staged_bytes(maxV, maxM, false, true) <= kStageSmemMax;
-}
+// Staging of a launch whose largest instance is maxV x (rows maxM): full
+// whenever it fits.
+inline bool stage_light(int maxV, int maxM) { return staged_bytes(maxV, maxM, false) > kStageSmemMax; }
 
 // Pricing rounds of one instance with its tree staged in shared memory:
 // `max_here` rounds at most (1 for the round-kernel form), or until done.
-template <bool kLight, bool kLift>
+// The staged state starts from parent[] and flow[] (a rebuild in the first
+// round); single pivots keep it current, multi-pivot rounds mark it stale.
+template <bool kLight>
 __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs, unsigned char* smem,
                             int max_here) {
     Ctx g;
     batch_ctx(a, d, g);
     Ctx c = g;
-    stage_hot<kLight, kLift>(c, smem, a.maxV, a.maxM);
+    stage_hot<kLight>(c, smem, a.maxV, a.maxM);
     const int V = d.m + d.n;
     for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = g.parent[v]; c.flow[v] = g.flow[v]; }
+    if (threadIdx.x == 0) c.sc->stale = 1;
     __syncthreads();
     for (int r = 0; r < max_here; r++) {
-        tree_recompute_cta(c, bs);
+        if (c.sc->stale) tree_build_cta(c, bs);
         if (!c.sc->done) {
             if (c.sc->pricing) sweep_partial_cta(c, bs);
             else sweep_cta(c);
@@ -669,9 +661,8 @@ __global__ void __launch_bounds__(256) k_bround(BatchArgs a) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) continue;
         if (d.sc->done) continue;          // every thread reads the same value
-        if (a.light) brounds_one<true, false>(a, d, bs, smem, 1);
-        else if (a.lift) brounds_one<false, true>(a, d, bs, smem, 1);
-        else brounds_one<false, false>(a, d, bs, smem, 1);
+        if (a.light) brounds_one<true>(a, d, bs, smem, 1);
+        else brounds_one<false>(a, d, bs, smem, 1);
     }
 }
 
@@ -708,9 +699,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
         if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); publish_done(d); continue; }
         bsetup_one(a, d, bs);
         if (!d.sc->done) {
-            if (a.light) brounds_one<true, false>(a, d, bs, smem, 1 << 30);
-            else if (a.lift) brounds_one<false, true>(a, d, bs, smem, 1 << 30);
-            else brounds_one<false, false>(a, d, bs, smem, 1 << 30);
+            if (a.light) brounds_one<true>(a, d, bs, smem, 1 << 30);
+            else brounds_one<false>(a, d, bs, smem, 1 << 30);
         }
         bfinal_one(a, d, bs);
         publish_done(d);
@@ -974,10 +964,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                 k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
                 k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
                 k_gapply<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                k_gcommit<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                k_gjump_init<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                for (int it = 0; it < c.lift_cap - 1; it++) k_gjump<<<gg, 256, 0, P.stream>>>(c, P.gp, it);
-                k_gjump_final<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
                 k_gend<<<1, 32, 0, P.stream>>>(c, P.gp);
             }
             FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
@@ -1155,12 +1142,12 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 // -------------------------------------------------------- batched solver ---
 // Size buckets by V = m + n.  Instances above the last edge run on the plain
 // path (their staged tree would not fit in shared memory).
-// The last bucket stages lightly (staged_bytes(4096, 4095, true) = 144 KB);
-// the others stage fully (staged_bytes(2944, 2943, false) fits 226 KB).
+// A bucket stages fully when its largest instance fits (up to V = 2048 with
+// M = V - 1); the others stage lightly (staged_bytes(4096, 4095, true) =
+// 208 KB).
 static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944, 4096};
 static const int kNumBuckets = 8;
 static const int kMaxStagedV = 4096;
-static bool bucket_light(int b) { return b == kNumBuckets - 1; }
 static const int kMaxChunk = 64;
 
 static int bucket_of(int V) {
@@ -1398,8 +1385,7 @@ struct BatchRunner {
         a.count = bstart[b + 1] - bstart[b];
         a.next = nullptr; a.active = nullptr;
         a.maxV = bmaxV[b]; a.maxM = bmaxM[b];
-        a.light = bucket_light(b) ? 1 : 0;
-        a.lift = stage_lift(bmaxV[b], bmaxM[b], a.light != 0) ? 1 : 0;
+        a.light = stage_light(bmaxV[b], bmaxM[b]) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = pivot_mode(opt);
         a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
@@ -1408,6 +1394,8 @@ struct BatchRunner {
     }
 
     int32_t* ctr(int b) { return d_ctr.as<int32_t>() + (size_t)b * 2 * kMaxChunk; }
+
+    size_t bucket_smem(int b) { return staged_bytes(bmaxV[b], bmaxM[b], stage_light(bmaxV[b], bmaxM[b])); }
 
     int grid_for(int b, const TuneCfg& t, size_t smem, const void* fn) {
         int per_sm = 0;
@@ -1420,7 +1408,7 @@ struct BatchRunner {
     // Pricing rounds of bucket b as a CUDA graph: `chunk` x (zero the
     // counters, one k_bround launch).
     int capture_rounds(int b, const TuneCfg& t, cudaGraphExec_t* exec) {
-        const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
+        const size_t smem = bucket_smem(b);
         const int grid = grid_for(b, t, smem, (const void*)k_bround);
         cudaStream_t s = st[b];
         cudaGraph_t g;
@@ -1459,7 +1447,7 @@ struct BatchRunner {
             a.next = ctr(b);
             if (stage && (rc = stage_bucket(b, st[b]))) return rc;
             if (cfg[b].persistent) {
-                const size_t smem = staged_bytes(bmaxV[b], bmaxM[b], bucket_light(b), stage_lift(bmaxV[b], bmaxM[b], bucket_light(b)));
+                const size_t smem = bucket_smem(b);
                 FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
                 const void* fn = bsolve_fn(cfg[b].threads);
                 void* kargs[] = {&a};
@@ -1751,9 +1739,8 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.mode = pivot_mode(opt);
     a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
-    a.light = maxV > kBucketEdges[kNumBuckets - 2] ? 1 : 0;
-    a.lift = stage_lift(maxV, maxM, a.light != 0) ? 1 : 0;
-    const size_t smem = staged_bytes(maxV, maxM, a.light != 0, a.lift != 0);
+    a.light = stage_light(maxV, maxM) ? 1 : 0;
+    const size_t smem = staged_bytes(maxV, maxM, a.light != 0);
     const int threads = serve_threads(maxV);
     const void* fn = bsolve_fn(threads);
     int per_sm = 0;

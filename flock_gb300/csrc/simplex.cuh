@@ -252,17 +252,14 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
 
 // --------------------------------------------------------------- duals ------
 // depth[] and pot[] from parent[] by pointer jumping: pot[v] = acc + (-1)^len pot[anc].
+// Also the int32 column duals and the count of those outside the window.
 template <int J = kJump>
 __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int V = I.m + I.n;
     const int root = c.sc->root;
-    // With a lifting table every doubling level is kept (level it+1 from
-    // level it); otherwise two buffers alternate.
-    const bool lifting = c.lift_cap > 0;
-    int32_t* aA = lifting ? c.lift : c.anc0;
-    int32_t* aB = lifting ? c.lift + V : c.anc1;
-    const int max_it = lifting ? c.lift_cap - 1 : 40;
+    int32_t* aA = c.anc0;
+    int32_t* aB = c.anc1;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
         const int p = c.parent[v];
         if (p == -2) { aA[v] = -2; c.len0[v] = 0; c.acc0[v] = kDeadPot; }
@@ -274,7 +271,7 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
     int64_t* xA = c.acc0; int64_t* xB = c.acc1;
     int pending = 1;
     __syncthreads();
-    for (int it = 0; it < max_it && pending; it++) {
+    for (int it = 0; it < 40 && pending; it++) {
         int mine = 0;
         // J vertices per thread per step with their loads interleaved
         // (a thread's vertices are independent chains): when V exceeds the
@@ -314,23 +311,124 @@ __device__ void tree_recompute_cta(const Ctx& c, BlockScratch& bs) {
             }
         }
         pending = __syncthreads_or(mine);
-        if (lifting) { aA = aB; aB = c.lift + (size_t)(it + 2) * V; }
-        else { int32_t* t1 = aA; aA = aB; aB = t1; }
+        int32_t* t1 = aA; aA = aB; aB = t1;
         int32_t* t2 = lA; lA = lB; lB = t2;
         int64_t* t3 = xA; xA = xB; xB = t3;
     }
-    int wide = 0;
+    int64_t wide = 0;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
         const int64_t p = xA[v];
         c.depth[v] = lA[v];
         c.pot[v] = p;
-        if (v >= I.m) c.v32[v - I.m] = narrow_dual(p, wide);
+        if (v >= I.m) { int w = 0; c.v32[v - I.m] = narrow_dual(p, w); wide += w; }
     }
-    wide = __syncthreads_or(wide);
+    wide = block_sum_i64(wide, bs);
     if (threadIdx.x == 0) {
-        c.sc->narrow = !wide;
+        c.sc->nwide = (int32_t)wide;
+        c.sc->narrow = wide == 0;
         if (pending) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
     }
+    __syncthreads();
+}
+
+// Preorder intervals of the tree from parent[] (into the first half of iv,
+// sc->ivp = 0).  Euler tour: for each non-root tree vertex v the arc 2v
+// enters v from its parent and the arc 2v+1 leaves it; after entering v the
+// tour takes v's first child (or leaves v), after leaving v it enters v's
+// next sibling (or leaves the parent; the root's last child ends the tour).
+// Pointer jumping gives each arc the number of entering arcs from it to the
+// end of the tour, S(a); with T = S(first arc) = tree vertices - 1:
+//   pre(v) = T - S(2v) + 1,   size(v) = S(2v) - S(2v+1),   root: (0, T + 1).
+// Children lists (first child / next sibling) live in claim[]; the two arc
+// buffers in the pointer-jumping scratch.  Sibling order does not matter:
+// any preorder gives the same ancestor relation.
+template <int J = kJump>
+__device__ void euler_intervals_cta(const Ctx& c, BlockScratch& bs) {
+    const int V = c.I.m + c.I.n;
+    const int root = c.sc->root;
+    int32_t* fc = (int32_t*)c.claim;          // first child
+    int32_t* ns = fc + V;                      // next sibling
+    for (int v = threadIdx.x; v < V; v += blockDim.x) fc[v] = -1;
+    __syncthreads();
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int p = c.parent[v];
+        if (FLOCK_IN(p, V)) ns[v] = atomicExch(&fc[p], v);
+    }
+    __syncthreads();
+    // arc word: (successor arc + 1) << 32 | entering arcs counted so far (0: end)
+    uint64_t* X = (uint64_t*)c.anc0;
+    uint64_t* Y = (uint64_t*)c.acc0;
+    const int A = 2 * V;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int p = c.parent[v];
+        uint64_t d = 0, u = 0;
+        if (FLOCK_IN(p, V)) {
+            const int f = fc[v], sb = ns[v];
+            const int sd = f >= 0 ? 2 * f : 2 * v + 1;
+            const int su = sb >= 0 ? 2 * sb : (p == root ? -1 : 2 * p + 1);
+            d = ((uint64_t)(uint32_t)(sd + 1) << 32) | 1u;
+            u = (uint64_t)(uint32_t)(su + 1) << 32;
+        }
+        X[2 * v] = d;
+        X[2 * v + 1] = u;
+    }
+    int pending = 1;
+    __syncthreads();
+    for (int it = 0; it < 40 && pending; it++) {
+        int mine = 0, bad = 0;
+        for (int base = threadIdx.x; base < A; base += J * blockDim.x) {
+            uint64_t x[J], y[J];
+            int sa[J];
+            #pragma unroll
+            for (int u = 0; u < J; u++) {
+                const int a = base + u * blockDim.x;
+                x[u] = a < A ? X[a] : 0;
+                sa[u] = (int)(x[u] >> 32) - 1;
+                if (sa[u] >= A) { bad = 1; sa[u] = -1; }
+            }
+            #pragma unroll
+            for (int u = 0; u < J; u++) y[u] = sa[u] >= 0 ? X[sa[u]] : 0;
+            #pragma unroll
+            for (int u = 0; u < J; u++) {
+                const int a = base + u * blockDim.x;
+                if (a >= A) continue;
+                if (sa[u] < 0) { Y[a] = x[u] & 0xffffffffull; continue; }
+                Y[a] = (y[u] & 0xffffffff00000000ull) | (uint32_t)((uint32_t)x[u] + (uint32_t)y[u]);
+                mine |= (y[u] >> 32) != 0;
+            }
+        }
+        if (bad) fail_check(c.sc, 23);
+        pending = __syncthreads_or(mine);
+        uint64_t* t = X; X = Y; Y = t;
+    }
+    const int f0 = fc[root];
+    const int T = FLOCK_IN(f0, V) ? (int)(uint32_t)X[2 * f0] : 0;
+    int2* iv = c.iv;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const int p = c.parent[v];
+        int2 w = make_int2(0, 0);
+        if (v == root) w = make_int2(0, T + 1);
+        else if (FLOCK_IN(p, V)) {
+            const int sd = (int)(uint32_t)X[2 * v], su = (int)(uint32_t)X[2 * v + 1];
+            w = make_int2(T - sd + 1, sd - su);
+        }
+        iv[v] = w;
+    }
+    if (threadIdx.x == 0) {
+        c.sc->ivp = 0;
+        if (pending || T + 1 != c.sc->v_alive) fail_check(c.sc, 23);
+    }
+    __syncthreads();
+}
+
+// Full rebuild of the tree's derived state from parent[] and flow[]:
+// depths, duals, int32 duals, preorder intervals.
+template <int J = kJump>
+__device__ void tree_build_cta(const Ctx& c, BlockScratch& bs) {
+    tree_recompute_cta<J>(c, bs);
+    if (c.sc->done) return;
+    euler_intervals_cta<J>(c, bs);
+    if (threadIdx.x == 0) c.sc->stale = 0;
     __syncthreads();
 }
 
@@ -614,139 +712,171 @@ __device__ __forceinline__ void cycle_apply(const Ctx& c, int k, int l, const Cy
     }
 }
 
-// k-th ancestor of x from the lifting table (k below 2^(lift_cap-1));
-// -1 if the table leads outside the tree.
-__device__ __forceinline__ int kth_anc(const Ctx& c, int V, int x, int k) {
-    for (int j = 0; k; j++, k >>= 1) {
-        if (k & 1) {
-            x = c.lift[(size_t)j * V + x];
-            if (!FLOCK_IN(x, V)) return -1;
-        }
-    }
-    return x;
-}
-
 // int64 -> uint64 preserving order (for unsigned block reductions).
 __device__ __forceinline__ uint64_t oflow(int64_t f) { return (uint64_t)f ^ 0x8000000000000000ull; }
 
-// One pivot of entering cell (row k, column vertex l) with every step over
-// the cycle done by the whole CTA in parallel, using the lifting table.  A
-// tree edge (child v) is on the cycle iff v is an ancestor-or-self of
-// exactly one of k and l (the k-th ancestor test).  The leaving edge and
-// θ follow cycle_walk's rule exactly: on the k side the decreasing edges
-// are row children and ties go to the one nearest k (the deepest); on the
-// l side column children, ties to the one nearest the apex (the
-// shallowest); the l side wins ties between the sides.  The flows change by
-// ∓θ along the cycle and the segment from the leaving edge down to the
-// entering cell's endpoint is re-hung, as cycle_apply does.  Uses claim[]
-// (side marks) and len1/acc1 (new parents and flows) as scratch.  Returns
-// 1 if the pivot was applied (block-uniform).
+// One pivot of entering cell (row k, column vertex l), every step done by the
+// whole CTA in parallel on the preorder intervals, and the tree's derived
+// state updated in place of a rebuild.
+//
+// Cycle: a tree edge (child v) is on the cycle iff v's subtree holds exactly
+// one of k and l.  The leaving edge and theta follow cycle_walk's rule
+// exactly: on the k side the decreasing edges are row children and ties go
+// to the deepest, on the l side column children, ties to the shallowest; the
+// l side wins ties between the sides.  One reduction of two (flow, tie key)
+// pairs gives both sides' candidates.
+//
+// Update: let q be the leaving edge's child, e the entering endpoint below
+// it (S = subtree of q holds e) and other the endpoint outside S.  The path
+// e = p_0, ..., p_t = q is reversed (p_i's new parent is p_(i-1), e's is
+// other) and S is re-hung below other.  For x in S whose deepest path
+// ancestor is p_i: depth' = depth(other) + 1 + i + (depth(x) - depth(p_i)),
+// and every dual in S shifts by the entering cell's reduced cost r (rows on
+// e's side of the bipartition by +r, the others by -r), so that the new tree
+// edge has zero reduced cost.  Intervals: S's block is cut out and re-inserted
+// right after other; inside it the branches of p_0, p_1, ... follow one
+// another (branch i = subtree(p_i) minus subtree(p_(i-1)), old order kept),
+// so that each subtree' is contiguous; sizes change on the path and on the
+// old and new ancestors of S.  Old intervals are read from one buffer of iv
+// and the new ones written to the other.
+// Scratch: claim[] (side marks), len1 (the path by index i), acc1 (the path
+// edges' flows after the cycle update).  Returns 1 if the pivot was applied
+// (block-uniform).
 template <int J = kJump>
-__device__ int single_pivot_lift(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
+__device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
     const int m = c.I.m;
-    const int dk = c.depth[k], dl = c.depth[l];
-    uint64_t mk = kNoKey, ml = kNoKey;
-    int lbad = 0;
-    // J vertices per thread at a time; their k-th ancestor lookups go
-    // level by level together (independent chains, one latency per level).
-    for (int base = threadIdx.x; base < V; base += J * blockDim.x) {
-        int vv[J], rk[J], rl[J], xk[J], xl[J];
-        #pragma unroll
-        for (int u = 0; u < J; u++) {
-            const int v = base + u * blockDim.x;
-            vv[u] = v;
-            rk[u] = rl[u] = -1;                     // -1: no test; else steps still to climb
-            xk[u] = k; xl[u] = l;
-            if (v < V && c.parent[v] >= 0) {
-                const int dv = c.depth[v];
-                if (dv <= dk) rk[u] = dk - dv;
-                if (dv <= dl) rl[u] = dl - dv;
-            }
-        }
-        for (int j = 0; j < c.lift_cap; j++) {
-            int more = 0;
-            #pragma unroll
-            for (int u = 0; u < J; u++) {
-                if (rk[u] > 0) {
-                    if (rk[u] & 1) { xk[u] = c.lift[(size_t)j * V + xk[u]]; if (!FLOCK_IN(xk[u], V)) { lbad = 1; rk[u] = -1; } }
-                    if (rk[u] > 0) { rk[u] >>= 1; more |= rk[u] > 0; }
-                }
-                if (rl[u] > 0) {
-                    if (rl[u] & 1) { xl[u] = c.lift[(size_t)j * V + xl[u]]; if (!FLOCK_IN(xl[u], V)) { lbad = 1; rl[u] = -1; } }
-                    if (rl[u] > 0) { rl[u] >>= 1; more |= rl[u] > 0; }
-                }
-            }
-            if (!more) break;
-        }
-        #pragma unroll
-        for (int u = 0; u < J; u++) {
-            const int v = vv[u];
-            if (v >= V) continue;
-            const bool on_k = rk[u] == 0 && xk[u] == v;
-            const bool on_l = rl[u] == 0 && xl[u] == v;
-            const int side = on_k != on_l ? (on_k ? 1 : 2) : 0;   // 1: k side, 2: l side
-            c.claim[v] = (uint64_t)side;
-            if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
-            if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
-        }
-    }
-    if (lbad) fail_check(c.sc, 16);
-    mk = block_min_u64(mk, bs);
-    ml = block_min_u64(ml, bs);
-    const bool lside = ml <= mk;                   // uniform
-    const uint64_t fmin = lside ? ml : mk;
-    // leaving edge: k side the deepest, l side the shallowest among the minima
-    uint64_t pick = lside ? kNoKey : 0ull;
+    const int par = c.sc->ivp;
+    const int2* ivA = c.iv + (par ? V : 0);
+    int2* ivB = c.iv + (par ? 0 : V);
+    const int pk = ivA[k].x, pl = ivA[l].x;
+    // (order-preserving flow, tie key): k side ties to the largest (depth, v),
+    // so its key is complemented; l side to the smallest
+    uint64_t kf = kNoKey, kt = kNoKey, lf = kNoKey, lt = kNoKey;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        const uint64_t sd = c.claim[v];
-        if (lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) {
-            if (oflow(c.flow[v]) == fmin) {
-                const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
-                if (lside) pick = key < pick ? key : pick;
-                else pick = key > pick ? key : pick;
-            }
+        int side = 0;
+        if (c.parent[v] >= 0) {
+            const int2 w = ivA[v];
+            const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
+            side = on_k != on_l ? (on_k ? 1 : 2) : 0;
         }
+        c.claim[v] = (uint64_t)side;
+        if (side == 1 && v < m)
+            pair_min_into(kf, kt, oflow(c.flow[v]), ~(((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v));
+        if (side == 2 && v >= m)
+            pair_min_into(lf, lt, oflow(c.flow[v]), ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v);
     }
-    pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
-    if (fmin == kNoKey || pick == kNoKey || (!lside && pick == 0)) {
+    block_min_pairs(kf, kt, lf, lt, bs);
+    const bool lside = lf <= kf;                   // uniform
+    const uint64_t fmin = lside ? lf : kf;
+    const int q = (int)(uint32_t)(lside ? lt : ~kt);
+    if (fmin == kNoKey || !FLOCK_IN(q, V) || c.parent[q] < 0) {
         if (threadIdx.x == 0) fail_check(c.sc, 16);
         __syncthreads();
         return 0;
     }
-    const int q = (int)(uint32_t)pick;
     const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
     const int e = lside ? l : k, other = lside ? k : l;
-    const int de = lside ? dl : dk, dq = c.depth[q];
-    const uint64_t eside = lside ? 2 : 1;
-    // flows along the cycle; the re-hung segment's new parents and flows
-    for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        const uint64_t sd = c.claim[v];
-        if (sd) c.flow[v] += (sd == 1) == (v < m) ? -th : th;
-    }
-    __syncthreads();
-    int bad = 0;
-    for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        if (c.claim[v] != eside) continue;
-        const int dv = c.depth[v];
-        if (dv < dq) continue;                     // above the leaving edge
-        const int prev = v == e ? other : kth_anc(c, V, e, de - dv - 1);
-        if (!FLOCK_IN(prev, V)) { bad = 1; continue; }
-        c.len1[v] = prev;
-        c.acc1[v] = v == e ? th : c.flow[prev];
-    }
-    bad = __syncthreads_or(bad);
-    if (bad) {
+    const int de = c.depth[e], dq = c.depth[q], t = de - dq;
+    if (!FLOCK_IN(t, V)) {                         // the path indexes len1/acc1 (V entries)
         if (threadIdx.x == 0) fail_check(c.sc, 17);
         __syncthreads();
         return 0;
     }
-    for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        if (c.claim[v] != eside || c.depth[v] < dq) continue;
-        c.parent[v] = c.len1[v];
-        c.flow[v] = c.acc1[v];
-    }
+    const uint64_t eside = lside ? 2 : 1;
+    int32_t* path = c.len1;
+    int64_t* pflow = c.acc1;
+    // flows along the cycle; the path from e up to q recorded by index
+    if (threadIdx.x == 0) { bs.i[4] = 0; bs.i[5] = 0; }
     __syncthreads();
-    return 1;
+    // the entering cell's reduced cost (exact), read before any dual changes
+    const int64_t r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
+    const int dother = c.depth[other];
+    int npath = 0, bad = 0;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const uint64_t sd = c.claim[v];
+        if (!sd) continue;
+        const int64_t delta = (sd == 1) == (v < m) ? -th : th;
+        const int dv = c.depth[v];
+        if (sd == eside && dv >= dq) {
+            const int i = de - dv;
+            if (!FLOCK_IN(i, t + 1)) { bad = 1; continue; }
+            path[i] = v;
+            pflow[i] = c.flow[v] + delta;
+            npath++;
+        } else {
+            c.flow[v] += delta;
+        }
+    }
+    if (npath) atomicAdd(&bs.i[5], npath);
+    bad = __syncthreads_or(bad);
+    if (bad || bs.i[5] != t + 1 || path[t] != q) {
+        if (threadIdx.x == 0) fail_check(c.sc, 17);
+        __syncthreads();
+        return 0;
+    }
+    const int2 Q = ivA[q], O = ivA[other];
+    const int P = Q.x, s = Q.y;
+    const int ins = O.x - (O.x >= P + s ? s : 0) + 1;   // S's new first position
+    const int dnew = dother + 1 - de;                  // depth' = dnew + 2 i + depth
+    const bool erow = e < m;
+    int dwide = 0;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        if (c.parent[v] == -2) continue;               // not in the tree
+        const int2 w = ivA[v];
+        int2 nw;
+        if (iv_in(Q, w.x)) {
+            // deepest path vertex above v: smallest i whose subtree holds v
+            int lo = 0, hi = t;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const int pv = path[mid];
+                if (!FLOCK_IN(pv, V)) { bad = 1; break; }
+                if (iv_in(ivA[pv], w.x)) hi = mid; else lo = mid + 1;
+            }
+            const int i = lo;
+            const int pi = path[i];
+            if (!FLOCK_IN(pi, V)) { bad = 1; continue; }
+            const int2 Pi = ivA[pi];
+            int off = 0, rank = w.x - Pi.x;
+            if (i > 0) {
+                const int pc = path[i - 1];
+                if (!FLOCK_IN(pc, V)) { bad = 1; continue; }
+                const int2 Pc = ivA[pc];
+                off = Pc.y;
+                if (w.x >= Pc.x) rank -= Pc.y;
+            }
+            nw.x = ins + off + rank;
+            nw.y = v == pi ? s - off : w.y;
+            c.depth[v] = dnew + 2 * i + c.depth[v];
+            const int64_t p0 = c.pot[v];
+            const int64_t p1 = p0 + ((v < m) == erow ? r : -r);
+            c.pot[v] = p1;
+            if (v >= m) {
+                int w0 = 0, w1 = 0;
+                narrow_dual(p0, w0);
+                c.v32[v - m] = narrow_dual(p1, w1);
+                dwide += w1 - w0;
+            }
+            if (v == pi) {
+                c.parent[v] = i == 0 ? other : path[i - 1];
+                c.flow[v] = i == 0 ? th : pflow[i - 1];
+            }
+        } else {
+            const int y = w.x - (w.x >= P + s ? s : 0);
+            nw.x = y + (y >= ins ? s : 0);
+            nw.y = w.y - (iv_in(w, P) ? s : 0) + (iv_in(w, O.x) ? s : 0);
+        }
+        ivB[v] = nw;
+    }
+    if (dwide) atomicAdd(&bs.i[4], dwide);
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        if (bad) fail_check(c.sc, 24);
+        c.sc->ivp = par ^ 1;
+        c.sc->nwide += bs.i[4];
+        c.sc->narrow = c.sc->nwide == 0;
+    }
+    return bad ? 0 : 1;
 }
 
 // Parallel mode: candidates walked per round (the rest wait for later rounds).
@@ -826,9 +956,9 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         __syncthreads();
         return;
     }
-    if (ncand == 1 && c.lift_cap > 0) {
+    if (ncand == 1) {
         const int i = c.cand[0];
-        const int ok = single_pivot_lift<J>(c, bs, i, m + (int)key_idx(c.row_best[i]), V);
+        const int ok = single_pivot_iv<J>(c, bs, i, m + (int)key_idx(c.row_best[i]), V);
         if (threadIdx.x == 0) {
             c.sc->pivots += ok;
             c.sc->ncand = 1;
@@ -839,18 +969,16 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         __syncthreads();
         return;
     }
-    // A single candidate always wins: no claims, no ownership pass.
-    const bool single = ncand == 1;
-    if (!single) {
-        for (int v = threadIdx.x; v < V; v += blockDim.x) c.claim[v] = kNoKey;
-        __syncthreads();
-    }
+    // Several candidates: claims, ownership, then the owners applied; the
+    // tree's derived state is rebuilt before the next sweep.
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.claim[v] = kNoKey;
+    __syncthreads();
     int bad = 0;
     for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
         const int i = c.cand[t];
         const uint64_t key = c.row_best[i];
         const int l = m + (int)key_idx(key);
-        const uint64_t P = single ? kNoKey : pack_i32(key_val(key), (uint32_t)i);
+        const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
         const CycleResult cr = cycle_walk(c, i, l, P, V);
         c.cand_theta[t] = cr.theta;
         c.cand_q[t] = cr.q;
@@ -861,7 +989,6 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
     int wins = 0;
     for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
         if (c.cand_info[t] & 4) continue;
-        if (single) { c.cand_info[t] |= 2; wins++; continue; }
         const int i = c.cand[t];
         const uint64_t key = c.row_best[i];
         const int l = m + (int)key_idx(key);
@@ -883,6 +1010,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         c.sc->pivots += (int32_t)w;
         c.sc->ncand = ncand;
         c.sc->last_winners = (int32_t)w;
+        c.sc->stale = 1;
         if (any_bad || w == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
         if (mode == 2 && w < kSwitchPivots) c.sc->mode = 0;
     }
