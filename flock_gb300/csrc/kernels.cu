@@ -600,8 +600,9 @@ inline size_t staged_bytes(int V, int M, bool light) {
     return (k.so + 15) & ~size_t(15);
 }
 
-// Largest dynamic shared memory a staged launch may use.
-constexpr size_t kStageSmemMax = 226 * 1024;
+// Largest dynamic shared memory a staged launch may use (the 227 KB of a
+// block less the kernels' static BlockScratch and work-stealing slot).
+constexpr size_t kStageSmemMax = 225 * 1024;
 
 // Staging of a launch whose largest instance is maxV x (rows maxM): full
 // whenever it fits.
@@ -1212,9 +1213,9 @@ struct BatchRunner {
         FLOCK_CK(cudaEventCreate(&ev_start));
         FLOCK_CK(cudaEventCreate(&ev_done));
         FLOCK_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-        FLOCK_CK(cudaFuncSetAttribute(k_bround, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
+        FLOCK_CK(cudaFuncSetAttribute(k_bround, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageSmemMax));
         for (int t : {256, 512, 1024})
-            FLOCK_CK(cudaFuncSetAttribute(bsolve_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
+            FLOCK_CK(cudaFuncSetAttribute(bsolve_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageSmemMax));
         FLOCK_CK(d_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         FLOCK_CK(h_ctr.ensure((size_t)kNumBuckets * 2 * kMaxChunk * sizeof(int32_t)));
         init = true;
@@ -1716,7 +1717,7 @@ ServeLayout serve_layout(int m, int n) {
 
 int serve_init() {
     for (int t : {256, 512, 1024})
-        FLOCK_CK(cudaFuncSetAttribute(bsolve_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024));
+        FLOCK_CK(cudaFuncSetAttribute(bsolve_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageSmemMax));
     return FLOCK_OK;
 }
 
