@@ -202,7 +202,7 @@ struct BlockScratch {
     uint64_t red2[32];
     uint64_t red3[32];
     uint64_t red4[32];
-    int32_t i[8];
+    int32_t i[12];
 };
 
 __device__ __forceinline__ uint64_t block_min_u64(uint64_t v, BlockScratch& bs) {

@@ -522,11 +522,62 @@ __device__ __forceinline__ int batch_next(const BatchArgs& a, int* s_idx) {
     return idx < a.count ? idx : -1;
 }
 
-// Initial solution and strongly feasible start tree of one instance, in the
-// instance's global working set.
-__device__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs) {
+// Shared-memory staging of the setup: the initial allocation list (kept from
+// Vogel to the start tree), then Vogel's per-line arrays or, in the same
+// space once Vogel is done, the start tree's scratch, parents and depths.
+// setup_stage_bytes() below follows the same carving.
+struct SetupStage {
+    template <class K> __host__ __device__ static void list(Ctx& c, K& k, int V) {
+        c.bfs_src = (int32_t*)k.S(4 * (size_t)V);
+        c.bfs_dst = (int32_t*)k.S(4 * (size_t)V);
+        c.bfs_qty = (int32_t*)k.S(4 * (size_t)V);
+    }
+    template <class K> __host__ __device__ static void vogel(Ctx& c, K& k, int V) {
+        c.top2 = (int4*)k.S(16 * (size_t)V);
+        c.diff = (int32_t*)k.S(4 * (size_t)V);
+        c.res = (int32_t*)k.S(4 * (size_t)V);
+        c.rescan = (int32_t*)k.S(4 * (size_t)V);
+        c.covered = (uint8_t*)k.S((size_t)V);
+    }
+    template <class K> __host__ __device__ static void tree(Ctx& c, K& k, int V) {
+        c.bsum = (int64_t*)k.S(8 * (size_t)V);
+        c.csr_adj = (int32_t*)k.S(8 * (size_t)V);
+        c.csr_start = (int32_t*)k.S(4 * ((size_t)V + 1));
+        c.order = (int32_t*)k.S(4 * (size_t)V);
+        c.uf = (int32_t*)k.S(4 * (size_t)V);
+        c.parent = (int32_t*)k.S(4 * (size_t)V);
+        c.depth = (int32_t*)k.S(4 * (size_t)V);
+    }
+};
+
+inline size_t setup_stage_bytes(int V) {
+    Ctx c;
+    Carver k{nullptr, 0, (unsigned char*)16, 0};
+    SetupStage::list(c, k, V);
+    Carver kv = k, kt = k;
+    SetupStage::vogel(c, kv, V);
+    SetupStage::tree(c, kt, V);
+    return (std::max(kv.so, kt.so) + 15) & ~size_t(15);
+}
+
+// Initial solution and strongly feasible start tree of one instance.  With
+// kStage the working arrays live in shared memory (the persistent kernel's
+// dynamic block, free until the rounds stage the tree) and the parents are
+// copied to the instance's working set at the end; else everything is in
+// the working set.
+template <bool kStage>
+__device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs,
+                                           unsigned char* smem) {
     Ctx c;
     batch_ctx(a, d, c);
+    const Ctx g = c;
+    const int V = d.m + d.n;
+    Carver k{nullptr, 0, smem, 0};
+    if (kStage) {
+        SetupStage::list(c, k, V);
+        Carver kv = k;
+        SetupStage::vogel(c, kv, V);
+    }
     if (threadIdx.x == 0) {
         Scalars z;
         memset(&z, 0, sizeof(z));
@@ -543,14 +594,20 @@ __device__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch&
         __syncthreads();
     }
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
-    const int V = d.m + d.n;
-    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
-        d.bfs[3 * k + 0] = c.bfs_src[k];
-        d.bfs[3 * k + 1] = c.bfs_dst[k];
-        d.bfs[3 * k + 2] = c.bfs_qty[k];
+    for (int q = threadIdx.x; q < V - 1; q += blockDim.x) {
+        d.bfs[3 * q + 0] = c.bfs_src[q];
+        d.bfs[3 * q + 1] = c.bfs_dst[q];
+        d.bfs[3 * q + 2] = c.bfs_qty[q];
     }
     __syncthreads();
+    if (kStage) {
+        Carver kt = k;
+        SetupStage::tree(c, kt, V);
+    }
     sf_init_cta(c, bs);
+    if (kStage) {
+        for (int v = threadIdx.x; v < V; v += blockDim.x) g.parent[v] = c.parent[v];
+    }
     __syncthreads();
 }
 
@@ -564,7 +621,7 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
     for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); continue; }
-        bsetup_one(a, d, bs);
+        bsetup_one<false>(a, d, bs, nullptr);
     }
 }
 
@@ -592,12 +649,18 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     set_jump(c, k.S(jump_bytes(V)), V);
 }
 
+// Rounds staging; the launch's dynamic block also holds the staged setup
+// (launch_smem_bytes).
 inline size_t staged_bytes(int V, int M, bool light) {
     Carver k{nullptr, 0, (unsigned char*)16, 0};
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
     k.S(4 * (size_t)V); k.S(16 * (size_t)V);
     if (!light) { k.S(8 * (size_t)V); k.S(jump_bytes(V)); }
     return (k.so + 15) & ~size_t(15);
+}
+
+inline size_t launch_smem_bytes(int V, int M, bool light) {
+    return std::max(staged_bytes(V, M, light), setup_stage_bytes(V));
 }
 
 // Largest dynamic shared memory a staged launch may use (the 227 KB of a
@@ -698,7 +761,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
     for (int idx; (idx = batch_next(a, &s_idx)) >= 0;) {
         const BatchDesc d = a.desc[idx];
         if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); publish_done(d); continue; }
-        bsetup_one(a, d, bs);
+        bsetup_one<true>(a, d, bs, smem);
         if (!d.sc->done) {
             if (a.light) brounds_one<true>(a, d, bs, smem, 1 << 30);
             else brounds_one<false>(a, d, bs, smem, 1 << 30);
@@ -1396,7 +1459,7 @@ struct BatchRunner {
 
     int32_t* ctr(int b) { return d_ctr.as<int32_t>() + (size_t)b * 2 * kMaxChunk; }
 
-    size_t bucket_smem(int b) { return staged_bytes(bmaxV[b], bmaxM[b], stage_light(bmaxV[b], bmaxM[b])); }
+    size_t bucket_smem(int b) { return launch_smem_bytes(bmaxV[b], bmaxM[b], stage_light(bmaxV[b], bmaxM[b])); }
 
     int grid_for(int b, const TuneCfg& t, size_t smem, const void* fn) {
         int per_sm = 0;
@@ -1741,7 +1804,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
     a.light = stage_light(maxV, maxM) ? 1 : 0;
-    const size_t smem = staged_bytes(maxV, maxM, a.light != 0);
+    const size_t smem = launch_smem_bytes(maxV, maxM, a.light != 0);
     const int threads = serve_threads(maxV);
     const void* fn = bsolve_fn(threads);
     int per_sm = 0;

@@ -99,33 +99,89 @@ __device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs) {
     __syncthreads();
 }
 
-// Refresh the stored penalties of lines [lo, hi) (all rows or all columns).
-__device__ void vogel_refresh(const Ctx& c, int lo, int hi, BlockScratch& bs) {
-    if (threadIdx.x == 0) bs.i[6] = 0;
-    __syncthreads();
+// Refresh the stored penalties of lines [lo, hi) (all rows or all columns)
+// and return the largest (penalty, line) key among them.  A line whose cache
+// lost a crossing is rescanned first (one warp per line when there are
+// enough of them, else the whole block per line).  The block reduction also
+// settles the step's choice: `best` = the larger of that key and `other`
+// (the other half's largest key), and `stale` = whether the chosen line's
+// cache must be rebuilt, decided by one thread before the reduction's last
+// barrier (afterwards thread 0's allocation may change covered[]).  The
+// rescan count bs.i[ctr] must be 0 on entry and is 0 again on return (rows
+// and columns use different counters).
+__device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uint64_t other, uint64_t& best,
+                                      int& stale, BlockScratch& bs) {
+    uint64_t mx = 0;
     for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
-        if (!c.covered[v] && !top2_valid(c, v, c.top2[v])) {
-            int k = atomicAdd(&bs.i[6], 1);
-            c.rescan[k] = v;
+        if (c.covered[v]) {
+            c.diff[v] = -1;
+            const uint64_t k = pack_i32(-1, (uint32_t)v);
+            mx = k > mx ? k : mx;
+            continue;
+        }
+        const int4 t = c.top2[v];
+        if (!top2_valid(c, v, t)) { c.rescan[atomicAdd(&bs.i[ctr], 1)] = v; continue; }
+        const int32_t p = vogel_penalty(t);
+        c.diff[v] = p;
+        const uint64_t k = pack_i32(p, (uint32_t)v);
+        mx = k > mx ? k : mx;
+    }
+    __syncthreads();
+    const int k = bs.i[ctr];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (k >= nw) {
+        for (int q = w; q < k; q += nw) {
+            const int L = c.rescan[q];
+            vogel_rescan_warp(c, L);
+            if (l == 0) {
+                const int32_t p = vogel_penalty(c.top2[L]);
+                c.diff[L] = p;
+                const uint64_t key = pack_i32(p, (uint32_t)L);
+                mx = key > mx ? key : mx;
+            }
+        }
+    } else {
+        for (int q = 0; q < k; q++) {
+            const int L = c.rescan[q];
+            vogel_rescan_block(c, L, bs);
+            if (threadIdx.x == 0) {
+                const int32_t p = vogel_penalty(c.top2[L]);
+                c.diff[L] = p;
+                const uint64_t key = pack_i32(p, (uint32_t)L);
+                mx = key > mx ? key : mx;
+            }
+        }
+    }
+    mx = warp_max_u64(mx);
+    __syncthreads();
+    if (l == 0) bs.red[w] = mx;
+    __syncthreads();
+    if (w == 0) {
+        uint64_t x = l < nw ? bs.red[l] : 0ull;
+        x = warp_max_u64(x);
+        if (l == 0) {
+            const uint64_t all = x > other ? x : other;
+            const int L = (int)key_idx(all);
+            bs.red[0] = x;
+            bs.red2[0] = all;
+            bs.i[9] = top2_valid(c, L, c.top2[L]) ? 0 : 1;
+            bs.i[ctr] = 0;                   // every thread read it before the first barrier above
         }
     }
     __syncthreads();
-    const int k = bs.i[6];
-    const int nw = blockDim.x >> 5;
-    if (k >= nw) {
-        for (int q = threadIdx.x >> 5; q < k; q += nw) vogel_rescan_warp(c, c.rescan[q]);
-    } else {
-        for (int q = 0; q < k; q++) vogel_rescan_block(c, c.rescan[q], bs);
-    }
-    __syncthreads();
-    for (int v = lo + threadIdx.x; v < hi; v += blockDim.x)
-        c.diff[v] = c.covered[v] ? -1 : vogel_penalty(c.top2[v]);
-    __syncthreads();
+    best = bs.red2[0];
+    stale = bs.i[9];
+    return bs.red[0];
 }
 
 // Vogel's approximation.  Writes the V-1 allocations to c.bfs_* in allocation
 // order and the event count to c.sc->events (-1: the reference's behaviour is
 // undefined from the step written as (-1,-1,0) on).
+//
+// A step covers exactly one line, so only that line's half (rows or
+// columns) has its penalties refreshed in the next step; the other half's
+// penalties stay as stored (the reference's staleness rule), and so does
+// its largest key, kept in bs.red4[0] (rows) / bs.red4[1] (columns).
 __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n, V = m + n;
@@ -150,10 +206,12 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
         c.top2[m + j] = top2_from_keys(a1, a2);
     }
     if (threadIdx.x == 0) {
-        bs.i[0] = 1; bs.i[1] = 1;   // prev_row, prev_col
+        bs.i[0] = 1; bs.i[1] = 1;   // refresh rows / columns in the next step
         bs.i[2] = 0; bs.i[3] = 0;   // covered rows / columns (counters)
         bs.i[4] = 0;                // stale min-cost index
         bs.i[5] = 0;                // events
+        bs.i[6] = 0; bs.i[8] = 0;   // rescan list lengths (rows, columns)
+        bs.red4[0] = 0; bs.red4[1] = 0;
         bs.i[7] = 0;                // stop
     }
     __syncthreads();
@@ -161,25 +219,17 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
         const int cr = bs.i[2], cc = bs.i[3];
         if (cr + cc >= V - 1 || bs.i[7]) break;
         const int pr = bs.i[0], pc = bs.i[1];
-        __syncthreads();
-        if (pr) vogel_refresh(c, 0, m, bs);
-        if (pc) vogel_refresh(c, m, V, bs);
-        uint64_t best = 0;
-        for (int v = threadIdx.x; v < V; v += blockDim.x) {
-            uint64_t k = pack_i32(c.diff[v], (uint32_t)v);
-            best = k > best ? k : best;
-        }
-        best = block_max_u64(best, bs);
+        uint64_t mrow = bs.red4[0], mcol = bs.red4[1], best = 0;
+        int stale = 0;
+        if (pr) mrow = vogel_refresh_max(c, 0, m, 6, pc ? 0ull : mcol, best, stale, bs);
+        if (pc) mcol = vogel_refresh_max(c, m, V, 8, mrow, best, stale, bs);
         const int L = (int)key_idx(best);
-        // One thread decides whether the chosen line's cache is stale; the
-        // decision is broadcast and a barrier separates every read of
-        // covered[] here from thread 0's allocation below, which writes it.
-        if (threadIdx.x == 0) bs.i[6] = top2_valid(c, L, c.top2[L]) ? 0 : 1;
-        __syncthreads();
-        if (bs.i[6]) vogel_rescan_block(c, L, bs);
+        if (stale) vogel_rescan_block(c, L, bs);
         if (threadIdx.x == 0) {
-            if (pr) bs.i[0] = 0;
-            if (pc) bs.i[1] = 0;
+            bs.red4[0] = mrow;
+            bs.red4[1] = mcol;
+            bs.i[0] = 0;
+            bs.i[1] = 0;
             const int4 t = c.top2[L];
             const bool found = t.z >= 0;
             const int cross = found ? t.z : bs.i[4];
