@@ -105,9 +105,14 @@ struct Ctx {
     int2* iv;
     // pointer-jumping scratch, one block of jump_bytes(V) (set_jump): int32
     // anc0, anc1, len0, len1 then int64 acc0, acc1; the Euler-tour ranking
-    // uses the same block as two arrays of 2 V words.  Between rebuilds the
-    // single pivot keeps its path in len1 and the path flows in acc1.
+    // uses the same block as two arrays of 2 V words.
     int32_t* anc0; int32_t* anc1; int32_t* len0; int32_t* len1; int64_t* acc0; int64_t* acc1;
+    // single pivot scratch: cycle side of each vertex, the re-hung path by
+    // index and its updated flows (V each; may alias len1 / acc1, which only
+    // the rebuilds use)
+    uint8_t* side;
+    int32_t* path;
+    int64_t* pflow;
     // pricing
     uint64_t* row_best;   // m   packed (reduced cost, column) of the best cell per row
     uint64_t* claim;      // V   edge claims

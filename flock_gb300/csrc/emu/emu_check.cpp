@@ -107,6 +107,8 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.prow = arr<int32_t>(keep, kPPRows);
     c.iv = arr<int2>(keep, 2 * (size_t)V);
     set_jump(c, arr<int64_t>(keep, jump_bytes(V) / 8), V);
+    c.path = c.len1; c.pflow = c.acc1;
+    c.side = arr<uint8_t>(keep, V);
     c.row_best = arr<uint64_t>(keep, m); c.claim = arr<uint64_t>(keep, V);
     c.cand = arr<int32_t>(keep, m); c.cand_theta = arr<int64_t>(keep, m);
     c.cand_q = arr<int32_t>(keep, m); c.cand_info = arr<int32_t>(keep, m);
@@ -133,9 +135,11 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
             if (pricing == 2 && threadIdx.x == 0)
                 for (int i = 0; i < m; i++) { junk = junk * 6364136223846793005ull + 1442695040888963407ull; c.row_best[i] = junk; }
             __syncthreads();
-            if (c.sc->pricing) sweep_partial_cta(c, bs);
+            uint64_t entering = kNoKey;
+            const bool partial = c.sc->pricing != 0;
+            if (partial) entering = sweep_partial_cta(c, bs);
             else sweep_cta(c);
-            pivot_round_cta(c, bs);
+            pivot_round_cta(c, bs, partial, entering);
             if (threadIdx.x == 0) c.sc->rounds++;
             __syncthreads();
             if (c.sc->done) break;

@@ -66,6 +66,9 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.flow = (int64_t*)k.S(8 * v);
     c.claim = (uint64_t*)k.S(8 * v);
     set_jump(c, k.S(jump_bytes(V)), V);
+    c.path = c.len1;
+    c.pflow = c.acc1;
+    c.side = (uint8_t*)k.S(v);
     c.iv = (int2*)k.S(16 * v);
     c.row_best = (uint64_t*)k.S(8 * mm);
     c.pot = smem ? (int64_t*)k.S(8 * v) : (pot_global ? pot_global : (int64_t*)k.G(8 * v));

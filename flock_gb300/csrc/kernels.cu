@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
             const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
             if (on_k != on_l) side = on_k ? 1 : 2;
         }
-        c.claim[v] = (uint64_t)side;
+        c.side[v] = (uint8_t)side;
         if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
         if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
     }
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
     }
     uint64_t pick = lside ? kNoKey : 0ull;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const uint64_t sd = c.claim[v];
+        const uint64_t sd = c.side[v];
         if ((lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) && oflow(c.flow[v]) == fmin) {
             const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
             if (lside) pick = key < pick ? key : pick;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
 
 // Flows along the cycle change by -/+theta except on the path from the
 // entering endpoint e up to the leaving edge, whose vertices are recorded by
-// index (len1) with their updated flows (acc1) for k_gupdate.  Block 0 also
+// index (path) with their updated flows (pflow) for k_gupdate.  Block 0 also
 // fixes the pivot's parameters in gp (nothing here changes depths, duals or
 // intervals, so every block computes the same ones).
 __global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
@@ -283,15 +283,15 @@ __global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
     __syncthreads();
     int n = 0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        const uint64_t sd = c.claim[v];
+        const uint64_t sd = c.side[v];
         if (!sd) continue;
         const int64_t delta = (sd == 1) == (v < m) ? -th : th;
         const int dv = c.depth[v];
         if (sd == eside && dv >= dq) {
             const int i = de - dv;
             if (!FLOCK_IN(i, t + 1)) { fail_check(c.sc, 17); continue; }
-            c.len1[i] = v;
-            c.acc1[i] = c.flow[v] + delta;
+            c.path[i] = v;
+            c.pflow[i] = c.flow[v] + delta;
             n++;
         } else {
             c.flow[v] += delta;
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
     if (c.sc->done) return;
     const int m = c.I.m, V = m + c.I.n;
     const int t = gp->t, q = gp->q;
-    if (!gp->ok || !FLOCK_IN(t, V) || gp->npath != t + 1 || c.len1[t] != q) {
+    if (!gp->ok || !FLOCK_IN(t, V) || gp->npath != t + 1 || c.path[t] != q) {
         if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
         return;
     }
@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
     const int other = gp->other;
     const bool erow = gp->e < m;
     const int64_t r = gp->r, th = gp->th;
-    const int32_t* path = c.len1;
-    const int64_t* pflow = c.acc1;
+    const int32_t* path = c.path;
+    const int64_t* pflow = c.pflow;
     if (threadIdx.x == 0) s_w = 0;
     __syncthreads();
     int dwide = 0, bad = 0;
@@ -626,14 +626,15 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
 }
 
 // Shared-memory staging of the arrays every pivot step touches: the tree,
-// the duals, the row keys and the preorder intervals.  Full staging adds the
-// edge claims and the pointer-jumping block (used by the rebuilds, i.e. the
-// first round and the rounds after multi-pivot rounds); light staging (the
-// largest instances) keeps those two in the instance's global working set.
-// Every pointer is carved from the extern shared base and the flag is a
-// compile-time constant, so the compiler knows they address shared memory
-// (shared loads and atomics rather than generic ones).  staged_bytes() below
-// follows the same order.
+// the duals, the row keys and the preorder intervals; unless kLight (the
+// largest instances), also the single pivot's side marks, path and path
+// flows.  The edge claims of multi-pivot rounds and the pointer-jumping
+// block of the rebuilds (the first round and the rounds after multi-pivot
+// rounds) stay in the instance's global working set, which keeps the staged
+// block small enough for several instances per SM.  Every pointer is carved
+// from the extern shared base and the flag is a compile-time constant, so
+// the compiler knows they address shared memory (shared loads and atomics
+// rather than generic ones).  staged_bytes() below follows the same order.
 template <bool kLight>
 __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, int M) {
     Carver k{nullptr, 0, smem, 0};
@@ -645,8 +646,9 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     c.v32 = (int32_t*)k.S(4 * (size_t)V);
     c.iv = (int2*)k.S(16 * (size_t)V);
     if (kLight) return;
-    c.claim = (uint64_t*)k.S(8 * (size_t)V);
-    set_jump(c, k.S(jump_bytes(V)), V);
+    c.pflow = (int64_t*)k.S(8 * (size_t)V);
+    c.path = (int32_t*)k.S(4 * (size_t)V);
+    c.side = (uint8_t*)k.S((size_t)V);
 }
 
 // Rounds staging; the launch's dynamic block also holds the staged setup
@@ -655,7 +657,7 @@ inline size_t staged_bytes(int V, int M, bool light) {
     Carver k{nullptr, 0, (unsigned char*)16, 0};
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
     k.S(4 * (size_t)V); k.S(16 * (size_t)V);
-    if (!light) { k.S(8 * (size_t)V); k.S(jump_bytes(V)); }
+    if (!light) { k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S((size_t)V); }
     return (k.so + 15) & ~size_t(15);
 }
 
@@ -689,9 +691,11 @@ __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch
     for (int r = 0; r < max_here; r++) {
         if (c.sc->stale) tree_build_cta(c, bs);
         if (!c.sc->done) {
-            if (c.sc->pricing) sweep_partial_cta(c, bs);
+            uint64_t entering = kNoKey;
+            const bool partial = c.sc->pricing != 0;
+            if (partial) entering = sweep_partial_cta(c, bs);
             else sweep_cta(c);
-            pivot_round_cta(c, bs);
+            pivot_round_cta(c, bs, partial, entering);
         }
         if (threadIdx.x == 0) {
             c.sc->rounds++;
@@ -1206,9 +1210,9 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 // -------------------------------------------------------- batched solver ---
 // Size buckets by V = m + n.  Instances above the last edge run on the plain
 // path (their staged tree would not fit in shared memory).
-// A bucket stages fully when its largest instance fits (up to V = 2048 with
-// M = V - 1); the others stage lightly (staged_bytes(4096, 4095, true) =
-// 208 KB).
+// A bucket stages fully when its largest instance fits (57 V + 8 M bytes: up
+// to V = 3500 or so); the others stage lightly (staged_bytes(4096, 4095,
+// true) = 208 KB).
 static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944, 4096};
 static const int kNumBuckets = 8;
 static const int kMaxStagedV = 4096;

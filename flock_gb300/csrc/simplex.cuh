@@ -540,12 +540,18 @@ __device__ void sweep_cta(const Ctx& c) { sweep_rows_cta(c, nullptr, c.I.m); }
 // After a full sweep: keep the kPPRows rows with the most negative keys in
 // prow[] (32-bin histogram threshold, then row order: value-determined),
 // optionally clearing every other row's key; resets the partial-pricing age.
-// All threads of the block; uses cand[] as scratch.
-__device__ void select_candidate_rows(const Ctx& c, BlockScratch& bs, bool clear_others) {
+// Returns the smallest (reduced cost, row) pair among the negative keys
+// (kNoKey: none), i.e. the sequential rule's entering row.  All threads of
+// the block; uses cand[] as scratch.
+__device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool clear_others) {
     const int m = c.I.m;
-    int32_t rmin = 0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
-    rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
+    uint64_t bestp = kNoKey;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int32_t v = key_val(c.row_best[i]);
+        if (v < 0) { const uint64_t P = pack_i32(v, (uint32_t)i); bestp = P < bestp ? P : bestp; }
+    }
+    bestp = block_min_u64(bestp, bs);                          // ends with a barrier
+    const int32_t rmin = bestp == kNoKey ? 0 : key_val(bestp);
     const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
     int last = -1;                                             // highest histogram bin kept
     if (rmin < 0) {
@@ -581,38 +587,42 @@ __device__ void select_candidate_rows(const Ctx& c, BlockScratch& bs, bool clear
     }
     if (threadIdx.x == 0) { c.sc->pp_n = min(total, kPPRows); c.sc->pp_age = 0; }
     __syncthreads();
+    return bestp;
 }
 
 // Partial pricing (candidate rows).  A full sweep keeps the kPPRows rows
 // with the most negative best reduced costs in prow[] (chosen by a 32-bin
 // histogram threshold and then by row index, so the set depends only on the
 // values) and clears every other row's key; the next rounds re-price only
-// those rows, every other row's key cleared first (row_best need not survive
-// between rounds: the round form stages it afresh in every launch).  A full
-// sweep runs again when the candidates hold no negative reduced cost any more
-// or after kPPRefresh rounds, so a round without a negative key
-// (optimality) is always a full sweep.
-__device__ void sweep_partial_cta(const Ctx& c, BlockScratch& bs) {
+// those rows.  Every reader of the keys in a partial-pricing round looks at
+// the listed rows only (row_best need not survive between rounds: the round
+// form stages it afresh in every launch).  A full sweep runs again when the
+// candidates hold no negative reduced cost any more or after kPPRefresh
+// rounds, so a round without a negative key (optimality) is always a full
+// sweep.  Returns the smallest (reduced cost, row) pair among the negative
+// keys (kNoKey: none): the sequential rule's entering row, already reduced
+// over the block.  The caller's end-of-round barrier orders pp_age.
+__device__ uint64_t sweep_partial_cta(const Ctx& c, BlockScratch& bs) {
     const int m = c.I.m;
     const int pn = c.sc->pp_n, age = c.sc->pp_age;
-    int full = pn <= 0 || pn > kPPRows || age >= kPPRefresh;
+    const bool full = pn <= 0 || pn > kPPRows || age >= kPPRefresh;
+    uint64_t best = kNoKey;
     if (!full) {
-        for (int i = threadIdx.x; i < m; i += blockDim.x) c.row_best[i] = kNoKey;
-        __syncthreads();
         sweep_rows_cta(c, c.prow, pn);
-        int neg = 0;
         for (int t = threadIdx.x; t < pn; t += blockDim.x) {
             const int i = c.prow[t];
-            if (FLOCK_IN(i, m)) neg |= key_val(c.row_best[i]) < 0;
+            if (!FLOCK_IN(i, m)) continue;                     // recorded by the sweep
+            const int32_t v = key_val(c.row_best[i]);
+            if (v < 0) { const uint64_t P = pack_i32(v, (uint32_t)i); best = P < best ? P : best; }
         }
-        full = !__syncthreads_or(neg);
+        best = block_min_u64(best, bs);
     }
-    if (full) {
+    if (full || best == kNoKey) {
         sweep_rows_cta(c, nullptr, m);
-        select_candidate_rows(c, bs, true);
+        best = select_candidate_rows(c, bs, true);
     }
     if (threadIdx.x == 0) c.sc->pp_age++;
-    __syncthreads();
+    return best;
 }
 
 // ---------------------------------------------------------------- pivots ----
@@ -739,8 +749,8 @@ __device__ __forceinline__ uint64_t oflow(int64_t f) { return (uint64_t)f ^ 0x80
 // so that each subtree' is contiguous; sizes change on the path and on the
 // old and new ancestors of S.  Old intervals are read from one buffer of iv
 // and the new ones written to the other.
-// Scratch: claim[] (side marks), len1 (the path by index i), acc1 (the path
-// edges' flows after the cycle update).  Returns 1 if the pivot was applied
+// Scratch: side[] (cycle side marks), path[] (the path by index i),
+// pflow[] (the path edges' flows after the cycle update).  Returns 1 if the pivot was applied
 // (block-uniform).
 template <int J = kJump>
 __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
@@ -759,12 +769,13 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
             const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
             side = on_k != on_l ? (on_k ? 1 : 2) : 0;
         }
-        c.claim[v] = (uint64_t)side;
+        c.side[v] = (uint8_t)side;
         if (side == 1 && v < m)
             pair_min_into(kf, kt, oflow(c.flow[v]), ~(((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v));
         if (side == 2 && v >= m)
             pair_min_into(lf, lt, oflow(c.flow[v]), ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v);
     }
+    if (threadIdx.x == 0) { bs.i[4] = 0; bs.i[5] = 0; }   // ordered by the reduction's barriers
     block_min_pairs(kf, kt, lf, lt, bs);
     const bool lside = lf <= kf;                   // uniform
     const uint64_t fmin = lside ? lf : kf;
@@ -783,17 +794,15 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
         return 0;
     }
     const uint64_t eside = lside ? 2 : 1;
-    int32_t* path = c.len1;
-    int64_t* pflow = c.acc1;
+    int32_t* path = c.path;
+    int64_t* pflow = c.pflow;
     // flows along the cycle; the path from e up to q recorded by index
-    if (threadIdx.x == 0) { bs.i[4] = 0; bs.i[5] = 0; }
-    __syncthreads();
     // the entering cell's reduced cost (exact), read before any dual changes
     const int64_t r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
     const int dother = c.depth[other];
     int npath = 0, bad = 0;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        const uint64_t sd = c.claim[v];
+        const uint64_t sd = c.side[v];
         if (!sd) continue;
         const int64_t delta = (sd == 1) == (v < m) ? -th : th;
         const int dv = c.depth[v];
@@ -886,19 +895,35 @@ constexpr int kMaxCand = 32;
 constexpr int kSwitchPivots = 10;
 
 // One pricing round after sweep: choose candidates, claim, apply.
+// have_best: the sweep already reduced the sequential rule's entering row
+// (pre_best, kNoKey: none).  With partial pricing only the listed candidate
+// rows hold keys this round, and only they are read.
 template <int J = kJump>
-__device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
+__device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best = false, uint64_t pre_best = kNoKey) {
     const InstDev& I = c.I;
     const int m = I.m, V = m + I.n;
     const int mode = c.sc->mode;
-    if (threadIdx.x == 0) bs.i[0] = 0;
-    __syncthreads();
     // a candidate key whose column is outside the instance is an internal
     // error: recorded, never used as an index
     const uint32_t ncols = (uint32_t)I.n;
+    const bool plist = c.sc->pricing != 0;
+    const int nrows = plist ? min(max(c.sc->pp_n, 0), kPPRows) : m;
+    int ncand = 0, first = 0;
+    if (mode == 0 && have_best) {
+        ncand = pre_best != kNoKey ? 1 : 0;
+        first = (int)key_idx(pre_best);
+        if (ncand && (!FLOCK_IN(first, m) || key_idx(c.row_best[first]) >= ncols)) {   // block-uniform
+            if (threadIdx.x == 0) fail_check(c.sc, 18);
+            return;
+        }
+    } else {
+    if (threadIdx.x == 0) bs.i[0] = 0;
+    __syncthreads();
     if (mode == 0) {
         uint64_t best = kNoKey;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        for (int t = threadIdx.x; t < nrows; t += blockDim.x) {
+            const int i = plist ? c.prow[t] : t;
+            if (!FLOCK_IN(i, m)) continue;
             const uint64_t k = c.row_best[i];
             if (k != kNoKey && key_val(k) < 0 && key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
             if (k != kNoKey && key_val(k) < 0) {
@@ -917,7 +942,9 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         // so leaving out weaker rows changes no decision among the rest; the
         // cap bounds the cycle walks of a round.
         int32_t rmin = 0;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        for (int t = threadIdx.x; t < nrows; t += blockDim.x) {
+            const int i = plist ? c.prow[t] : t;
+            if (!FLOCK_IN(i, m)) continue;
             const uint64_t k = c.row_best[i];
             if (k != kNoKey && key_val(k) < 0 && key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
             if (k != kNoKey) rmin = min(rmin, key_val(k));
@@ -927,7 +954,9 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
             const int64_t span = -(int64_t)rmin;
             if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
             __syncthreads();
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            for (int t = threadIdx.x; t < nrows; t += blockDim.x) {
+                const int i = plist ? c.prow[t] : t;
+                if (!FLOCK_IN(i, m)) continue;
                 const uint64_t k = c.row_best[i];
                 if (k != kNoKey && key_val(k) < 0 && key_idx(k) < ncols)
                     atomicAdd((unsigned long long*)&bs.red2[((int64_t)key_val(k) - rmin) * 32 / span], 1ull);
@@ -941,7 +970,9 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
             }
             __syncthreads();
             const int last = bs.i[1];
-            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            for (int t = threadIdx.x; t < nrows; t += blockDim.x) {
+                const int i = plist ? c.prow[t] : t;
+                if (!FLOCK_IN(i, m)) continue;
                 const uint64_t k = c.row_best[i];
                 if (k != kNoKey && key_val(k) < 0 && key_idx(k) < ncols &&
                     ((int64_t)key_val(k) - rmin) * 32 / span <= last)
@@ -950,15 +981,18 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
         }
     }
     __syncthreads();
-    const int ncand = bs.i[0];
+    ncand = bs.i[0];
+    first = c.cand[0];
+    }
+    // The two outcomes below end with thread 0 writing the scalars; every
+    // caller follows with its own thread-0 update and a barrier before the
+    // scalars are read again.
     if (ncand == 0) {
         if (threadIdx.x == 0) { c.sc->done = 1; c.sc->ncand = 0; }
-        __syncthreads();
         return;
     }
     if (ncand == 1) {
-        const int i = c.cand[0];
-        const int ok = single_pivot_iv<J>(c, bs, i, m + (int)key_idx(c.row_best[i]), V);
+        const int ok = single_pivot_iv<J>(c, bs, first, m + (int)key_idx(c.row_best[first]), V);
         if (threadIdx.x == 0) {
             c.sc->pivots += ok;
             c.sc->ncand = 1;
@@ -966,7 +1000,6 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs) {
             if (!ok) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
             if (mode == 2) c.sc->mode = 0;
         }
-        __syncthreads();
         return;
     }
     // Several candidates: claims, ownership, then the owners applied; the
