@@ -183,6 +183,19 @@ int main(int argc, char** argv) {
     verify = env("EMU_VERIFY", 1);
     const int cost_hi = env("EMU_COST_HI", 1000), qlo = env("EMU_QTY_LO", 100), qhi = env("EMU_QTY_HI", 1000);
     int bad = 0;
+    // EMU_FILE: solve the instance of that binary instance file instead
+    if (const char* f = getenv("EMU_FILE")) {
+        int32_t m = 0, n = 0;
+        if (flock_bin_shape(f, &m, &n)) { fprintf(stderr, "cannot read %s\n", f); return 2; }
+        std::vector<int32_t> s(m), d(n), c((size_t)m * n);
+        if (flock_read_bin(f, m, n, s.data(), d.data(), c.data())) { fprintf(stderr, "cannot read %s\n", f); return 2; }
+        Scalars r;
+        const int mism = solve_one(m, n, s.data(), d.data(), c.data(), mode, pricing, &r);
+        const bool ok = r.status == 0 && r.cert == 0 && mism == 0;
+        printf("%s m=%d n=%d obj=%lld rounds=%d pivots=%d status=%d cert=%d fail_site=%d barrier_mismatch=%d %s\n", f, m,
+               n, (long long)r.objective, r.rounds, r.pivots, r.status, r.cert, r.fail_site, mism, ok ? "ok" : "BAD");
+        return ok ? 0 : 1;
+    }
     for (int k = first; k <= last && k < count; k++) {
         const int m = ms[k], n = ns[k];
         std::vector<int32_t> s(m), d(n), c((size_t)m * n);

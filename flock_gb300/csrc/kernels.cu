@@ -1171,6 +1171,47 @@ static int test_sweep(int m, int n, const int32_t* cost, const int64_t* pot, uin
     return FLOCK_OK;
 }
 
+// Test hook: candidate-row selection (select_candidate_rows, clearing the
+// other rows) over host row keys of an m-row instance.
+__global__ void __launch_bounds__(1024) k_test_select(Ctx c, uint64_t* best) {
+    __shared__ BlockScratch bs;
+    const uint64_t b = select_candidate_rows(c, bs, true);
+    if (threadIdx.x == 0) *best = b;
+}
+
+static int test_select_rows(int m, const uint64_t* keys, uint64_t* keys_out, int32_t* prow, int32_t* pn,
+                            int32_t* pp_rows, uint64_t* best, int threads) {
+    if (m < 1 || !keys || !keys_out || !prow || !pn || !pp_rows || !best) return FLOCK_ERR_ARG;
+    if (threads < 32 || threads > 1024 || threads % 32) return FLOCK_ERR_ARG;
+    PlainSolver& P = plain();
+    std::lock_guard<std::mutex> lk(P.mu);
+    int rc = P.setup();
+    if (rc) return rc;
+    const int n = 1, V = m + n;
+    size_t gbytes = 0;
+    Ctx probe;
+    carve_ctx(probe, nullptr, V, m, nullptr, nullptr, nullptr, &gbytes);
+    FLOCK_CK(P.ws.ensure(al256(gbytes) + al256(sizeof(Scalars)) + 256));
+    Ctx c;
+    carve_ctx(c, P.ws.as<uint8_t>(), V, m, nullptr, nullptr);
+    c.sc = P.ws.as<Scalars>(al256(gbytes));
+    uint64_t* d_best = P.ws.as<uint64_t>(al256(gbytes) + al256(sizeof(Scalars)));
+    c.I.m = m; c.I.n = n; c.I.ldc = 4;
+    if ((rc = P.reset_scalars(c.sc, 0, 1))) return rc;
+    FLOCK_CK(cudaMemcpyAsync(c.row_best, keys, (size_t)m * 8, cudaMemcpyHostToDevice, P.stream));
+    k_test_select<<<1, threads, 0, P.stream>>>(c, d_best);
+    FLOCK_CK(cudaGetLastError());
+    FLOCK_CK(cudaMemcpyAsync(keys_out, c.row_best, (size_t)m * 8, cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaMemcpyAsync(prow, c.prow, (size_t)kPPRows * 4, cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaMemcpyAsync(best, d_best, 8, cudaMemcpyDeviceToHost, P.stream));
+    Scalars* hs = P.h_sc.as<Scalars>();
+    FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaStreamSynchronize(P.stream));
+    *pn = hs->pp_n;
+    *pp_rows = kPPRows;
+    return FLOCK_OK;
+}
+
 static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
     if (m < 1 || n < 1 || iters < 1 || !avg_ms) return FLOCK_ERR_ARG;
     PlainSolver& P = plain();
@@ -1945,6 +1986,13 @@ int flock_bench_batch_cells(int64_t* cells) { return flock::batch_cells(cells); 
  * m x n matrix (random costs and duals, inputs resident). */
 int flock_bench_sweep(int32_t m, int32_t n, int32_t iters, float* avg_ms, int32_t* tile) {
     return flock::bench_sweep(m, n, iters, avg_ms, tile);
+}
+
+/* Test hook: partial pricing's candidate-row selection over host row keys
+ * (prow needs room for the returned pp_rows entries). */
+int flock_test_select_rows(int32_t m, const uint64_t* keys, uint64_t* keys_out, int32_t* prow, int32_t* pn,
+                           int32_t* pp_rows, uint64_t* best, int32_t threads) {
+    return flock::test_select_rows(m, keys, keys_out, prow, pn, pp_rows, best, threads);
 }
 
 /* Test hook: one reduced-cost sweep over host costs and duals, row keys back. */

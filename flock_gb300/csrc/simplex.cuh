@@ -540,18 +540,16 @@ __device__ void sweep_cta(const Ctx& c) { sweep_rows_cta(c, nullptr, c.I.m); }
 // After a full sweep: keep the kPPRows rows with the most negative keys in
 // prow[] (32-bin histogram threshold, then row order: value-determined),
 // optionally clearing every other row's key; resets the partial-pricing age.
-// Returns the smallest (reduced cost, row) pair among the negative keys
-// (kNoKey: none), i.e. the sequential rule's entering row.  All threads of
-// the block; uses cand[] as scratch.
+// Returns the smallest (reduced cost, row) pair among the kept rows (kNoKey:
+// none), i.e. the sequential rule's entering row over the keys that remain:
+// when the first histogram bin alone holds more than kPPRows rows, the rows
+// past kPPRows in row order are dropped, possibly the overall best one.  All
+// threads of the block; uses cand[] as scratch.
 __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool clear_others) {
     const int m = c.I.m;
-    uint64_t bestp = kNoKey;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const int32_t v = key_val(c.row_best[i]);
-        if (v < 0) { const uint64_t P = pack_i32(v, (uint32_t)i); bestp = P < bestp ? P : bestp; }
-    }
-    bestp = block_min_u64(bestp, bs);                          // ends with a barrier
-    const int32_t rmin = bestp == kNoKey ? 0 : key_val(bestp);
+    int32_t rmin = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
+    rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
     const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
     int last = -1;                                             // highest histogram bin kept
     if (rmin < 0) {
@@ -578,16 +576,21 @@ __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool c
     }
     __syncthreads();
     const int32_t total = block_exclusive_scan_i32(c.cand, m, bs);   // ends with a barrier
+    uint64_t bestp = kNoKey;
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
         const int32_t v = key_val(c.row_best[i]);
         const bool sel = v < 0 && ((int64_t)v - rmin) * 32 / span <= last;
         const int slot = c.cand[i];
-        if (sel && slot < kPPRows) c.prow[slot] = i;
-        else if (clear_others) c.row_best[i] = kNoKey;
+        if (sel && slot < kPPRows) {
+            c.prow[slot] = i;
+            const uint64_t P = pack_i32(v, (uint32_t)i);
+            bestp = P < bestp ? P : bestp;
+        } else if (clear_others) {
+            c.row_best[i] = kNoKey;
+        }
     }
     if (threadIdx.x == 0) { c.sc->pp_n = min(total, kPPRows); c.sc->pp_age = 0; }
-    __syncthreads();
-    return bestp;
+    return block_min_u64(bestp, bs);                           // its barriers order the writes above
 }
 
 // Partial pricing (candidate rows).  A full sweep keeps the kPPRows rows

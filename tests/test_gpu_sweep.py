@@ -115,3 +115,85 @@ def test_sweep_extreme_costs():
     exp = expected_keys(cost, pot)
     np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
     np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 256), exp)
+
+
+# ---------------------------------------------------------------------------
+# Partial pricing's candidate-row selection (select_candidate_rows): rows with
+# negative keys, a 32-bin histogram over [rmin, 0) whose leading bins hold at
+# most kPPRows rows (the first bin always), then the first kPPRows such rows
+# in row order; every other key cleared.  The returned entering row is the
+# smallest (value, row) among the rows kept.
+NOKEY = (1 << 64) - 1
+
+
+def pack(v, idx):
+    return ((((v & 0xFFFFFFFF) ^ 0x80000000)) << 32) | idx
+
+
+def expect_select(vals, kpp):
+    m = len(vals)
+    neg = [v for v in vals if v is not None and v < 0]
+    rmin = min(neg) if neg else 0
+    span = -rmin if rmin < 0 else 1
+    last = -1
+    if rmin < 0:
+        hist = [0] * 32
+        for v in neg:
+            hist[((v - rmin) * 32) // span] += 1
+        cum, last = hist[0], 0
+        for b in range(1, 32):
+            if cum + hist[b] > kpp:
+                break
+            cum += hist[b]
+            last = b
+    sel = [v is not None and v < 0 and ((v - rmin) * 32) // span <= last for v in vals]
+    kept = [i for i in range(m) if sel[i]][:kpp]
+    best = min((vals[i], i) for i in kept) if kept else None
+    return kept, sum(sel), best
+
+
+def gpu_select(keys, threads=256):
+    L = fg.lib()
+    f = L.flock_test_select_rows
+    f.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
+    keys = np.ascontiguousarray(keys, np.uint64)
+    out = np.zeros_like(keys)
+    prow = np.full(1024, -1, np.int32)
+    pn, kpp = ctypes.c_int32(-1), ctypes.c_int32(-1)
+    best = np.zeros(1, np.uint64)
+    rc = f(len(keys), keys.ctypes.data, out.ctypes.data, prow.ctypes.data, ctypes.addressof(pn),
+           ctypes.addressof(kpp), best.ctypes.data, threads)
+    assert rc == 0, L.flock_last_error()
+    return out, prow[:pn.value].tolist(), kpp.value, int(best[0])
+
+
+def check_select(vals, threads=256):
+    keys = np.array([NOKEY if v is None else pack(v, i % 7) for i, v in enumerate(vals)], np.uint64)
+    out, prow, kpp, best = gpu_select(keys, threads)
+    kept, total, eb = expect_select(vals, kpp)
+    assert prow == kept
+    want = NOKEY if eb is None else pack(eb[0], eb[1])
+    assert best == want, (hex(best), eb)
+    keep = set(kept)
+    for i in range(len(vals)):
+        assert int(out[i]) == (int(keys[i]) if i in keep else NOKEY), i
+
+
+def test_select_rows_crowded_first_bin():
+    """More rows than kPPRows in the first histogram bin: the rows past
+    kPPRows in row order are dropped, among them the overall best one, and the
+    entering row returned is the best row kept."""
+    vals = [-100] * 200
+    vals[150] = -101
+    check_select(vals)
+    check_select(vals, threads=64)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_select_rows_random(seed):
+    rng = np.random.default_rng(seed)
+    m = int(rng.integers(1, 700))
+    lo = int(rng.choice([3, 50, 100000]))
+    vals = [None if rng.random() < 0.2 else int(rng.integers(-lo, lo)) for _ in range(m)]
+    check_select(vals, threads=int(rng.choice([32, 128, 256, 1024])))
