@@ -44,8 +44,15 @@ constexpr uint64_t kNoKey = ~0ull;
 // default of the batched kernels (64 registers) and the plain solver's.
 constexpr int kJump = 2;
 constexpr int kJumpPlain = 4;
-constexpr int kPPRows = 64;      // partial pricing: candidate rows kept by a full sweep
-constexpr int kPPRefresh = 32;   // partial pricing: rounds between full sweeps
+constexpr int kPPRows = 64;      // partial pricing: capacity of the candidate-row list
+// Partial pricing defaults (Scalars::pp_rows / pp_refresh): candidate rows
+// kept by a full sweep and rounds between full sweeps.  The batched and
+// served forms (instances of up to a few thousand vertices, every row's
+// matrix re-read from L2) gain from frequent full sweeps and short lists; the
+// plain solver's large instances, where a full sweep streams the whole
+// matrix from HBM, from longer intervals.
+constexpr int kPPRowsBatch = 32, kPPRefreshBatch = 8;
+constexpr int kPPRowsPlain = 64, kPPRefreshPlain = 32;
 
 struct Scalars {
     int32_t status;
@@ -70,6 +77,8 @@ struct Scalars {
     int32_t pricing;       // 0 full sweeps, 1 partial pricing (candidate rows)
     int32_t pp_n;          // partial pricing: candidate rows in prow[]
     int32_t pp_age;        // partial pricing: rounds since the last full sweep
+    int32_t pp_rows;       // partial pricing: candidate rows kept by a full sweep (1..kPPRows)
+    int32_t pp_refresh;    // partial pricing: rounds between full sweeps (>= 1)
     int32_t ivp;           // which half of Ctx::iv holds the current preorder intervals
     int32_t nwide;         // live column duals outside the int32 window (narrow == (nwide == 0))
     int32_t stale;         // 1: depth, duals and intervals must be rebuilt from parent[] (tree_build_cta)

@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
 __global__ void k_pdecide(Ctx c, GridPivot* gp) {
     if (threadIdx.x != 0 || c.sc->done) return;
     const int pn = c.sc->pp_n;
-    gp->full = (pn <= 0 || pn > kPPRows || c.sc->pp_age >= kPPRefresh) ? 1 : 0;
+    gp->full = (pn <= 0 || pn > kPPRows || c.sc->pp_age >= max(c.sc->pp_refresh, 1)) ? 1 : 0;
 }
 
 __global__ void __launch_bounds__(256) k_pcheck(Ctx c, GridPivot* gp) {
@@ -584,6 +584,8 @@ __device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& 
         z.max_rounds = a.max_rounds;
         z.mode = a.mode;
         z.pricing = a.pricing;
+        z.pp_rows = kPPRowsBatch;
+        z.pp_refresh = kPPRefreshBatch;
         *c.sc = z;
     }
     __syncthreads();
@@ -957,6 +959,8 @@ struct PlainSolver {
         memset(&z, 0, sizeof(z));
         z.mode = mode;
         z.max_rounds = max_rounds;
+        z.pp_rows = kPPRowsPlain;
+        z.pp_refresh = kPPRefreshPlain;
         memcpy(h_sc.p, &z, sizeof(z));
         FLOCK_CK(cudaMemcpyAsync(dsc, h_sc.p, sizeof(z), cudaMemcpyHostToDevice, stream));
         return FLOCK_OK;
@@ -1208,7 +1212,7 @@ static int test_select_rows(int m, const uint64_t* keys, uint64_t* keys_out, int
     FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
     FLOCK_CK(cudaStreamSynchronize(P.stream));
     *pn = hs->pp_n;
-    *pp_rows = kPPRows;
+    *pp_rows = hs->pp_rows;
     return FLOCK_OK;
 }
 

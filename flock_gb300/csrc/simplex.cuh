@@ -537,16 +537,17 @@ __device__ void sweep_rows_cta(const Ctx& c, const int32_t* list, int cnt) {
 
 __device__ void sweep_cta(const Ctx& c) { sweep_rows_cta(c, nullptr, c.I.m); }
 
-// After a full sweep: keep the kPPRows rows with the most negative keys in
+// After a full sweep: keep the sc->pp_rows rows with the most negative keys in
 // prow[] (32-bin histogram threshold, then row order: value-determined),
 // optionally clearing every other row's key; resets the partial-pricing age.
 // Returns the smallest (reduced cost, row) pair among the kept rows (kNoKey:
 // none), i.e. the sequential rule's entering row over the keys that remain:
-// when the first histogram bin alone holds more than kPPRows rows, the rows
-// past kPPRows in row order are dropped, possibly the overall best one.  All
+// when the first histogram bin alone holds more than pp_rows rows, the rows
+// past pp_rows in row order are dropped, possibly the overall best one.  All
 // threads of the block; uses cand[] as scratch.
 __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool clear_others) {
     const int m = c.I.m;
+    const int cap = min(max(c.sc->pp_rows, 1), kPPRows);
     int32_t rmin = 0;
     for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
     rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
@@ -563,7 +564,7 @@ __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool c
         if (threadIdx.x == 0) {
             uint64_t cum = bs.red2[0];
             int l = 0;
-            for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)kPPRows; b++) { cum += bs.red2[b]; l = b; }
+            for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)cap; b++) { cum += bs.red2[b]; l = b; }
             bs.i[1] = l;
         }
         __syncthreads();
@@ -581,7 +582,7 @@ __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool c
         const int32_t v = key_val(c.row_best[i]);
         const bool sel = v < 0 && ((int64_t)v - rmin) * 32 / span <= last;
         const int slot = c.cand[i];
-        if (sel && slot < kPPRows) {
+        if (sel && slot < cap) {
             c.prow[slot] = i;
             const uint64_t P = pack_i32(v, (uint32_t)i);
             bestp = P < bestp ? P : bestp;
@@ -589,18 +590,18 @@ __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool c
             c.row_best[i] = kNoKey;
         }
     }
-    if (threadIdx.x == 0) { c.sc->pp_n = min(total, kPPRows); c.sc->pp_age = 0; }
+    if (threadIdx.x == 0) { c.sc->pp_n = min(total, cap); c.sc->pp_age = 0; }
     return block_min_u64(bestp, bs);                           // its barriers order the writes above
 }
 
-// Partial pricing (candidate rows).  A full sweep keeps the kPPRows rows
+// Partial pricing (candidate rows).  A full sweep keeps the pp_rows rows
 // with the most negative best reduced costs in prow[] (chosen by a 32-bin
 // histogram threshold and then by row index, so the set depends only on the
 // values) and clears every other row's key; the next rounds re-price only
 // those rows.  Every reader of the keys in a partial-pricing round looks at
 // the listed rows only (row_best need not survive between rounds: the round
 // form stages it afresh in every launch).  A full sweep runs again when the
-// candidates hold no negative reduced cost any more or after kPPRefresh
+// candidates hold no negative reduced cost any more or after pp_refresh
 // rounds, so a round without a negative key (optimality) is always a full
 // sweep.  Returns the smallest (reduced cost, row) pair among the negative
 // keys (kNoKey: none): the sequential rule's entering row, already reduced
@@ -608,7 +609,7 @@ __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool c
 __device__ uint64_t sweep_partial_cta(const Ctx& c, BlockScratch& bs) {
     const int m = c.I.m;
     const int pn = c.sc->pp_n, age = c.sc->pp_age;
-    const bool full = pn <= 0 || pn > kPPRows || age >= kPPRefresh;
+    const bool full = pn <= 0 || pn > kPPRows || age >= max(c.sc->pp_refresh, 1);
     uint64_t best = kNoKey;
     if (!full) {
         sweep_rows_cta(c, c.prow, pn);
