@@ -45,14 +45,14 @@ constexpr uint64_t kNoKey = ~0ull;
 constexpr int kJump = 2;
 constexpr int kJumpPlain = 4;
 constexpr int kPPRows = 64;      // partial pricing: capacity of the candidate-row list
-// Partial pricing defaults (Scalars::pp_rows / pp_refresh): candidate rows
-// kept by a full sweep and rounds between full sweeps.  The batched and
-// served forms (instances of up to a few thousand vertices, every row's
-// matrix re-read from L2) gain from frequent full sweeps and short lists; the
-// plain solver's large instances, where a full sweep streams the whole
-// matrix from HBM, from longer intervals.
-constexpr int kPPRowsBatch = 32, kPPRefreshBatch = 8;
-constexpr int kPPRowsPlain = 64, kPPRefreshPlain = 32;
+// Partial pricing settings (Scalars::pp_rows / pp_refresh): candidate rows
+// kept by a full sweep and rounds between full sweeps.  Instances of up to
+// kPPSmallV vertices (a full sweep is cheap next to a round's fixed cost)
+// gain from frequent full sweeps and short lists; larger ones, where a full
+// sweep streams a matrix of millions of cells, from longer intervals.
+constexpr int kPPSmallV = 1024;
+constexpr int kPPRowsSmall = 32, kPPRefreshSmall = 8;
+constexpr int kPPRowsLarge = 64, kPPRefreshLarge = 32;
 
 struct Scalars {
     int32_t status;

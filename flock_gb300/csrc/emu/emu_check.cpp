@@ -9,7 +9,7 @@
 // depths, duals, int32 duals and preorder intervals are checked against a full
 // rebuild), EMU_COST_HI / EMU_QTY_LO / EMU_QTY_HI (generator ranges; small
 // ranges give ties and degenerate bases), EMU_PP_ROWS / EMU_PP_REFRESH
-// (partial pricing settings, default the plain solver's), EMU_FILE (solve the
+// (partial pricing settings, default 64 and 32), EMU_FILE (solve the
 // instance of that binary instance file instead).
 #define FLOCK_EMU
 #include <cstdio>
@@ -99,8 +99,8 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     memset(sc, 0, sizeof(Scalars));
     sc->mode = mode;
     sc->pricing = pricing ? 1 : 0;
-    sc->pp_rows = getenv("EMU_PP_ROWS") ? atoi(getenv("EMU_PP_ROWS")) : kPPRowsPlain;
-    sc->pp_refresh = getenv("EMU_PP_REFRESH") ? atoi(getenv("EMU_PP_REFRESH")) : kPPRefreshPlain;
+    sc->pp_rows = getenv("EMU_PP_ROWS") ? atoi(getenv("EMU_PP_ROWS")) : kPPRowsLarge;
+    sc->pp_refresh = getenv("EMU_PP_REFRESH") ? atoi(getenv("EMU_PP_REFRESH")) : kPPRefreshLarge;
     sc->max_rounds = 1 << 30;
     c.sc = sc;
     c.bfs_src = arr<int32_t>(keep, V); c.bfs_dst = arr<int32_t>(keep, V); c.bfs_qty = arr<int32_t>(keep, V);

@@ -584,8 +584,9 @@ __device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& 
         z.max_rounds = a.max_rounds;
         z.mode = a.mode;
         z.pricing = a.pricing;
-        z.pp_rows = kPPRowsBatch;
-        z.pp_refresh = kPPRefreshBatch;
+        const bool small = d.m + d.n <= kPPSmallV;
+        z.pp_rows = small ? kPPRowsSmall : kPPRowsLarge;
+        z.pp_refresh = small ? kPPRefreshSmall : kPPRefreshLarge;
         *c.sc = z;
     }
     __syncthreads();
@@ -959,8 +960,8 @@ struct PlainSolver {
         memset(&z, 0, sizeof(z));
         z.mode = mode;
         z.max_rounds = max_rounds;
-        z.pp_rows = kPPRowsPlain;
-        z.pp_refresh = kPPRefreshPlain;
+        z.pp_rows = kPPRowsLarge;             // partial pricing runs on the plain path from kGridPivotV vertices
+        z.pp_refresh = kPPRefreshLarge;
         memcpy(h_sc.p, &z, sizeof(z));
         FLOCK_CK(cudaMemcpyAsync(dsc, h_sc.p, sizeof(z), cudaMemcpyHostToDevice, stream));
         return FLOCK_OK;
