@@ -300,6 +300,7 @@ def extras(fg, insts, res, peaks) -> dict:
     gbs = sb / (ms * 1e-3) / 1e9
     out["sweep_8000"] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                          "ms": ms, "bytes": sb, "traffic": DRAM_BYTES_SWEEP_8000, "kernel": "k_sweep"}
+    out["plain_configs"] = plain_configs(fg)
     out["served"] = served(fg)
     # CPU baseline: the oracle port of the reference path on all host cores
     try:
@@ -320,7 +321,7 @@ def extras(fg, insts, res, peaks) -> dict:
 
 SERVE_POOL = 512                 # served stream: distinct instances (reused)
 SERVE_REQUESTS = 1024            # requests per offered rate
-SERVE_RATES = (0.25, 0.5, 1.0)   # offered load as fractions of batched capacity
+SERVE_RATES = (0.1, 0.25, 0.5, 1.0, 1.2)   # offered load as fractions of batched capacity
 SERVE_PLAIN_SAMPLE = 16
 
 
@@ -381,6 +382,25 @@ def served(fg) -> dict:
     out["plain_solves_s"] = plain
     out["plain_sample"] = f"first {len(smp)} instances of the pool"
     out["served_vs_plain"] = max(r["solves_s"] for r in out["rates"]) / plain
+    return out
+
+
+def plain_configs(fg) -> dict:
+    """The plain solver on the two single-instance workloads: 1000 x 1000
+    degenerate-prone (costs 1..20, quantities 1..50, seed 0) and 8000 x 8000
+    Euclidean (costs = rounded distances of uniform points in [0,1000]^2,
+    quantities 1..10000, seed 0): wall time of flock_solve, rounds, pivots,
+    pivots/s, objective and certificate."""
+    out = {}
+    fg.solve(fg.config_instance("uniform100", 0))
+    for name in ("degenerate1000", "euclid8000"):
+        inst = fg.config_instance(name, 0)
+        t0 = time.perf_counter()
+        r = fg.solve(inst)
+        dt = time.perf_counter() - t0
+        out[name] = {"m": inst.m, "n": inst.n, "seconds": dt, "rounds": r.iterations, "pivots": r.pivots,
+                     "pivots_per_s": r.pivots / dt, "objective": r.objective,
+                     "certified": bool(r.certified and r.status == 0)}
     return out
 
 

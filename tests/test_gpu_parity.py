@@ -109,6 +109,22 @@ def test_solve_degenerate_mid():
     assert_optimal(inst, fg.solve(inst))
 
 
+@pytest.mark.parametrize("pivot", ["parallel", "switch"])
+def test_degenerate_1000_full_size(pivot):
+    """The 1000 x 1000 degenerate-prone workload itself (costs 1..20,
+    quantities 1..50, seed 0) with parallel pivots and deconfliction: the
+    reference path's own result is optimal here, and the objective must be
+    identical to it (int64)."""
+    inst = fg.config_instance("degenerate1000", 0)
+    ref = oracle.solve_ref(inst.supply, inst.demand, inst.cost)
+    assert oracle.verdict(inst.supply, inst.demand, inst.cost, ref) == "optimal"
+    res = fg.solve(inst, pivot=pivot)
+    assert_optimal(inst, res, ref)
+    assert res.objective == int(round(ref["objective"]))
+    b = fg.batch_solve([inst], pivot=pivot)[0]          # batched results carry no duals
+    assert b.status == 0 and b.certified and b.objective == res.objective
+
+
 @pytest.mark.parametrize("shape", [(1, 1), (1, 7), (6, 1), (2, 2), (3, 50), (50, 3)])
 def test_edge_shapes(shape):
     m, n = shape
