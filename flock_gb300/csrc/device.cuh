@@ -216,6 +216,7 @@ struct BlockScratch {
     uint64_t red2[32];
     uint64_t red3[32];
     uint64_t red4[32];
+    uint64_t part1[32], part2[32];   // per-warp partial results (Vogel's split rescans)
     int32_t i[12];
 };
 

@@ -73,6 +73,7 @@ inline void sync_at(int line) { wait_at(line, 1); }
 inline void warp_sync_at(int line) { wait_at(line, 2); }
 }  // namespace emu
 #define __syncthreads() emu::sync_at(__LINE__)
+#define __syncwarp(...) emu::warp_sync_at(-4)
 #define __syncthreads_or(p) emu::sync_or(p, __LINE__)
 namespace emu {
 inline int sync_or(int p, int line) {

@@ -101,16 +101,19 @@ __device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs) {
 
 // Refresh the stored penalties of lines [lo, hi) (all rows or all columns)
 // and return the largest (penalty, line) key among them.  A line whose cache
-// lost a crossing is rescanned first (one warp per line when there are
-// enough of them, else the whole block per line).  The block reduction also
-// settles the step's choice: `best` = the larger of that key and `other`
-// (the other half's largest key), and `stale` = whether the chosen line's
-// cache must be rebuilt, decided by one thread before the reduction's last
+// lost a crossing is rescanned first: one warp per line when there are at
+// least as many such lines as warps, else the warps split them (warp w scans
+// every g-th 32-wide slice of line w mod k, g = warps / k) and warp 0 merges
+// the partial top-2 pairs inside the final reduction.  That reduction also
+// settles the step's choice: `best` = the larger of the half's key and
+// `other` (the other half's largest key), and `stale` = whether the chosen
+// line's cache must be rebuilt, decided by one thread before the last
 // barrier (afterwards thread 0's allocation may change covered[]).  The
 // rescan count bs.i[ctr] must be 0 on entry and is 0 again on return (rows
-// and columns use different counters).
+// and columns use different counters).  Three barriers.
 __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uint64_t other, uint64_t& best,
                                       int& stale, BlockScratch& bs) {
+    const InstDev& I = c.I;
     uint64_t mx = 0;
     for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
         if (c.covered[v]) {
@@ -140,24 +143,42 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
                 mx = key > mx ? key : mx;
             }
         }
-    } else {
-        for (int q = 0; q < k; q++) {
-            const int L = c.rescan[q];
-            vogel_rescan_block(c, L, bs);
-            if (threadIdx.x == 0) {
-                const int32_t p = vogel_penalty(c.top2[L]);
-                c.diff[L] = p;
-                const uint64_t key = pack_i32(p, (uint32_t)L);
-                mx = key > mx ? key : mx;
+    } else if (k > 0) {
+        const int g = nw / k;
+        if (w < g * k) {
+            const int L = c.rescan[w % k], s = w / k;
+            uint64_t a1 = kNoKey, a2 = kNoKey;
+            if (L < I.m) {
+                const int32_t* row = I.cost + (size_t)L * I.ldc;
+                for (int j = 32 * s + l; j < I.n; j += 32 * g)
+                    if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+            } else {
+                const int j = L - I.m;
+                for (int i = 32 * s + l; i < I.m; i += 32 * g)
+                    if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
             }
+            warp_top2(a1, a2);
+            if (l == 0) { bs.part1[w] = a1; bs.part2[w] = a2; }
         }
     }
     mx = warp_max_u64(mx);
-    __syncthreads();
-    if (l == 0) bs.red[w] = mx;
+    if (l == 0) bs.red[w] = mx;        // every read of bs.red before this refresh preceded its first barrier
     __syncthreads();
     if (w == 0) {
         uint64_t x = l < nw ? bs.red[l] : 0ull;
+        if (k > 0 && k < nw && l < k) {
+            const int g = nw / k;
+            uint64_t a1 = kNoKey, a2 = kNoKey;
+            for (int s = 0; s < g; s++) top2_merge(a1, a2, bs.part1[l + s * k], bs.part2[l + s * k]);
+            const int L = c.rescan[l];
+            const int4 t = top2_from_keys(a1, a2);
+            c.top2[L] = t;
+            const int32_t p = vogel_penalty(t);
+            c.diff[L] = p;
+            const uint64_t key = pack_i32(p, (uint32_t)L);
+            x = key > x ? key : x;
+        }
+        __syncwarp();                  // the merged caches are visible to lane 0 below
         x = warp_max_u64(x);
         if (l == 0) {
             const uint64_t all = x > other ? x : other;
@@ -165,7 +186,7 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
             bs.red[0] = x;
             bs.red2[0] = all;
             bs.i[9] = top2_valid(c, L, c.top2[L]) ? 0 : 1;
-            bs.i[ctr] = 0;                   // every thread read it before the first barrier above
+            bs.i[ctr] = 0;                   // every thread read it before the barrier above
         }
     }
     __syncthreads();
