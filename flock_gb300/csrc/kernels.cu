@@ -68,16 +68,15 @@ __device__ __forceinline__ int4 ld_stream4(const int4* p) {
     return v;
 }
 
-// rows: price only the listed rows (c.sc->pp_n of them: partial pricing),
-// null for all; gate: run only when *gate == gate_val (null: always).
-__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int ntile, const int32_t* rows,
-                                                           const int32_t* gate, int gate_val) {
-    if (c.sc->done) return;
-    if (gate && *gate != gate_val) return;
-    __shared__ __align__(16) int32_t vt[kSweepTile];
+// One grid-wide sweep's share of block `bid` of `nb` (nb a multiple of
+// ntile): its column tile's int32 duals staged in vt, then (row, segment)
+// units.  rows: price only the listed rows (c.sc->pp_n of them: partial
+// pricing), null for all.  The caller orders vt's previous readers.
+__device__ __forceinline__ void sweep_part(const Ctx& c, int tile, int ntile, const int32_t* rows, int32_t* vt,
+                                           int bid, int nb) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
-    const int t = blockIdx.x % ntile, rg = blockIdx.x / ntile, nrg = gridDim.x / ntile;
+    const int t = bid % ntile, rg = bid / ntile, nrg = nb / ntile;
     const int j0 = t * tile;
     const int jn = min(tile, n - j0);
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5, warp = threadIdx.x >> 5;
@@ -126,6 +125,16 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int
     }
 }
 
+// Grid-wide sweep kernel (blockIdx.x = tile + ntile * row_group).  gate:
+// run only when *gate == gate_val (null: always).
+__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int ntile, const int32_t* rows,
+                                                           const int32_t* gate, int gate_val) {
+    if (c.sc->done) return;
+    if (gate && *gate != gate_val) return;
+    __shared__ __align__(16) int32_t vt[kSweepTile];
+    sweep_part(c, tile, ntile, rows, vt, (int)blockIdx.x, (int)gridDim.x);
+}
+
 // Launch shape of k_sweep for an m x n instance: column tiles of at most
 // kSweepTile, two blocks per SM in total, no more blocks than work units.
 static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile);
@@ -144,22 +153,23 @@ __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
 }
 
 // ------------------------------------------------- grid pivot round -------
-// The plain solver's pivot round for large instances, spread over the whole
-// GPU: one pivot per round (Dantzig's rule: the most negative row key, first
-// row among ties), every step a grid-wide kernel, the kernel boundaries the
-// only synchronisation.  The steps follow single_pivot_iv exactly (same
-// interval membership test, tie rules, path reversal and in-place update of
-// depths, duals and intervals), so a round costs six short kernels whatever
-// the tree's depth.
+// The plain solver's rounds for large instances, spread over the whole GPU:
+// seven graph-captured kernels per round, the kernel boundaries the only
+// synchronisation (a grid-wide barrier inside one cooperative launch costs
+// as much as a boundary on this two-die part).  One pivot per round
+// (Dantzig's rule: the most negative row key, first row among ties); the
+// steps follow single_pivot_iv exactly (same interval membership test, tie
+// rules, path reversal and in-place update of depths, duals and intervals),
+// so a round costs the same seven launches whatever the tree's depth.
 struct GridPivot {
     uint64_t best;          // entering candidate: (reduced cost, row)
     uint64_t mk, ml;        // per side: minimum order-preserving flow
     uint64_t qk, ql;        // per side: leaving edge (depth << 32 | child)
-    int32_t full;           // partial pricing: this round sweeps every row
-    int32_t npath;          // path vertices recorded by k_gapply
+    int32_t npath;          // path vertices recorded by the apply step
     int32_t dwide;          // change of the count of int32-window misses
-    int32_t pad_;
-    // the pivot, fixed by k_gapply before k_gupdate changes depths and duals
+    int32_t full;           // partial pricing: this round swept every row
+    uint32_t fin_count;     // blocks done with the update step
+    // the pivot, fixed by the apply step before the update changes depths and duals
     int64_t th, r;
     int32_t ok, e, other, q, de, dq, t, dother, eside, pad2_;
     int2 Q, O;
@@ -169,13 +179,17 @@ constexpr int kGridPivotV = 4096;     // plain instances with m + n >= this use 
 
 __device__ __forceinline__ const int2* iv_now(const Ctx& c, int V) { return c.iv + (c.sc->ivp ? V : 0); }
 
-__global__ void __launch_bounds__(1024, 1) k_gselect(Ctx c, GridPivot* gp) {
-    __shared__ BlockScratch bs;
-    if (c.sc->done) return;
+// Block 0: the entering candidate (over every row after a full sweep, over
+// the candidate rows otherwise: the others hold no key), the next candidate
+// rows after a full sweep, the round's bookkeeping.
+__device__ void grid_choose(const Ctx& c, GridPivot* gp, BlockScratch& bs, bool full, bool select) {
     const int m = c.I.m;
     const uint32_t ncols = (uint32_t)c.I.n;
+    const int nrows = full ? m : min(max(c.sc->pp_n, 0), kPPRows);
     uint64_t best = kNoKey;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    for (int t = threadIdx.x; t < nrows; t += blockDim.x) {
+        const int i = full ? t : c.prow[t];
+        if (!FLOCK_IN(i, m)) continue;
         const uint64_t k = c.row_best[i];
         if (k != kNoKey && key_val(k) < 0) {
             if (key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
@@ -184,6 +198,7 @@ __global__ void __launch_bounds__(1024, 1) k_gselect(Ctx c, GridPivot* gp) {
         }
     }
     best = block_min_u64(best, bs);
+    if (select) select_candidate_rows(c, bs, false);
     if (threadIdx.x == 0) {
         gp->best = best;
         gp->mk = gp->ml = kNoKey;
@@ -192,22 +207,23 @@ __global__ void __launch_bounds__(1024, 1) k_gselect(Ctx c, GridPivot* gp) {
         gp->npath = 0;
         gp->dwide = 0;
         gp->ok = 0;
+        gp->fin_count = 0;
         c.sc->rounds++;
+        c.sc->pp_age++;
         c.sc->ncand = best == kNoKey ? 0 : 1;
         if (best == kNoKey) c.sc->done = 1;
     }
 }
 
-__global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
-    __shared__ BlockScratch bs;
-    if (c.sc->done) return;
+// Cycle membership by intervals and each side's smallest decreasing flow.
+__device__ void grid_member(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
     const int m = c.I.m, V = m + c.I.n;
     const int k = (int)key_idx(gp->best);
     const int l = m + (int)key_idx(c.row_best[k]);
     const int2* iv = iv_now(c, V);
     const int pk = iv[k].x, pl = iv[l].x;
     uint64_t mk = kNoKey, ml = kNoKey;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
         int side = 0;
         if (c.parent[v] >= 0) {
             const int2 w = iv[v];
@@ -226,18 +242,17 @@ __global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
-    __shared__ BlockScratch bs;
-    if (c.sc->done) return;
+// The leaving edge among the minima: k side the deepest, l side the shallowest.
+__device__ void grid_pick(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
     const int m = c.I.m, V = m + c.I.n;
     const bool lside = gp->ml <= gp->mk;
     const uint64_t fmin = lside ? gp->ml : gp->mk;
     if (fmin == kNoKey) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
+        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
         return;
     }
     uint64_t pick = lside ? kNoKey : 0ull;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
         const uint64_t sd = c.side[v];
         if ((lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) && oflow(c.flow[v]) == fmin) {
             const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
@@ -254,19 +269,17 @@ __global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
 
 // Flows along the cycle change by -/+theta except on the path from the
 // entering endpoint e up to the leaving edge, whose vertices are recorded by
-// index (path) with their updated flows (pflow) for k_gupdate.  Block 0 also
-// fixes the pivot's parameters in gp (nothing here changes depths, duals or
-// intervals, so every block computes the same ones).
-__global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
-    __shared__ int s_n;
-    if (c.sc->done) return;
+// index (path) with their updated flows (pflow) for the update step.  Block
+// 0 also fixes the pivot's parameters in gp (nothing here changes depths,
+// duals or intervals, so every block computes the same ones).
+__device__ void grid_apply(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
     const int m = c.I.m, V = m + c.I.n;
     const bool lside = gp->ml <= gp->mk;
     const uint64_t fmin = lside ? gp->ml : gp->mk;
     const uint64_t pick = lside ? gp->ql : gp->qk;
     const int q = (int)(uint32_t)pick;
     if (fmin == kNoKey || (lside ? pick == kNoKey : pick == 0) || !FLOCK_IN(q, V) || c.parent[q] < 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
+        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
         return;
     }
     const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
@@ -274,15 +287,15 @@ __global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
     const int l = m + (int)key_idx(c.row_best[k]);
     const int e = lside ? l : k, other = lside ? k : l;
     const int de = c.depth[e], dq = c.depth[q], t = de - dq;
-    if (!FLOCK_IN(t, V)) {                         // the path indexes len1/acc1 (V entries)
-        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
+    if (!FLOCK_IN(t, V)) {                         // the path indexes path/pflow (V entries)
+        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
         return;
     }
     const uint64_t eside = lside ? 2 : 1;
-    if (threadIdx.x == 0) s_n = 0;
+    if (threadIdx.x == 0) bs.i[6] = 0;
     __syncthreads();
     int n = 0;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
         const uint64_t sd = c.side[v];
         if (!sd) continue;
         const int64_t delta = (sd == 1) == (v < m) ? -th : th;
@@ -297,10 +310,10 @@ __global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
             c.flow[v] += delta;
         }
     }
-    if (n) atomicAdd(&s_n, n);
+    if (n) atomicAdd(&bs.i[6], n);
     __syncthreads();
-    if (threadIdx.x == 0 && s_n) atomicAdd(&gp->npath, s_n);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (threadIdx.x == 0 && bs.i[6]) atomicAdd(&gp->npath, bs.i[6]);
+    if (bid == 0 && threadIdx.x == 0) {
         const int2* iv = iv_now(c, V);
         gp->th = th;
         gp->r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
@@ -315,14 +328,14 @@ __global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
 
 // The tree update of single_pivot_iv over the grid: new intervals into the
 // other half of iv, depths and duals of the re-hung subtree, the reversed
-// path's parents and flows; every row key cleared for the next sweep.
-__global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
-    __shared__ int s_w;
-    if (c.sc->done) return;
+// path's parents and flows; every row key cleared for the next sweep.  The
+// last block to finish ends the round: the current interval buffer, the
+// int32 dual flag, the pivot count and the round cap.
+__device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
     const int m = c.I.m, V = m + c.I.n;
     const int t = gp->t, q = gp->q;
     if (!gp->ok || !FLOCK_IN(t, V) || gp->npath != t + 1 || c.path[t] != q) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
+        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
         return;
     }
     const int par = c.sc->ivp;
@@ -337,10 +350,10 @@ __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
     const int64_t r = gp->r, th = gp->th;
     const int32_t* path = c.path;
     const int64_t* pflow = c.pflow;
-    if (threadIdx.x == 0) s_w = 0;
+    if (threadIdx.x == 0) bs.i[7] = 0;
     __syncthreads();
     int dwide = 0, bad = 0;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
         if (c.parent[v] == -2) continue;
         const int2 w = ivA[v];
         int2 nw;
@@ -387,53 +400,92 @@ __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
         }
         ivB[v] = nw;
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) c.row_best[i] = kNoKey;
+    for (int i = bid * blockDim.x + threadIdx.x; i < m; i += nb * blockDim.x) c.row_best[i] = kNoKey;
     if (bad) fail_check(c.sc, 24);
-    if (dwide) atomicAdd(&s_w, dwide);
+    if (dwide) atomicAdd(&bs.i[7], dwide);
     __syncthreads();
-    if (threadIdx.x == 0 && s_w) atomicAdd(&gp->dwide, s_w);
+    if (threadIdx.x == 0) {
+        if (bs.i[7]) atomicAdd(&gp->dwide, bs.i[7]);
+        __threadfence();
+        if (atomicAdd(&gp->fin_count, 1u) == (unsigned)nb - 1) {     // every block's share is in
+            __threadfence();
+            c.sc->ivp ^= 1;
+            c.sc->nwide += *(volatile int32_t*)&gp->dwide;
+            c.sc->narrow = c.sc->nwide == 0;
+            c.sc->pivots++;
+            c.sc->last_winners = 1;
+            if (c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
+        }
+    }
 }
 
-// Partial pricing on the plain path (large instances): decide whether this
-// round sweeps every row, re-price the candidates otherwise (k_sweep with the
-// row list), fall back to a full sweep in the same round when they hold no
-// negative key, and after a full sweep choose the next candidates.  Rows
-// without a key this round keep kNoKey (k_gupdate clears every key).
-__global__ void k_pdecide(Ctx c, GridPivot* gp) {
-    if (threadIdx.x != 0 || c.sc->done) return;
+// Step kernels of a grid round.  Each returns at once when the solve is
+// done (one thread reads the flag, so the whole block agrees).
+#define FLOCK_GRID_STEP_PROLOGUE() \
+    if (__syncthreads_or(threadIdx.x == 0 && c.sc->done)) return
+
+// Partial pricing decision of the round (every block computes it from the
+// same scalars): sweep every row, else the candidate rows.
+__device__ __forceinline__ bool grid_full_round(const Ctx& c) {
     const int pn = c.sc->pp_n;
-    gp->full = (pn <= 0 || pn > kPPRows || c.sc->pp_age >= max(c.sc->pp_refresh, 1)) ? 1 : 0;
+    return !c.sc->pricing || pn <= 0 || pn > kPPRows || c.sc->pp_age >= max(c.sc->pp_refresh, 1);
 }
 
-__global__ void __launch_bounds__(256) k_pcheck(Ctx c, GridPivot* gp) {
-    if (c.sc->done || gp->full) return;
+// Round start: the sweep this round's pricing asks for.
+__global__ void __launch_bounds__(kSweepThreads, 2) k_gsweep(Ctx c, GridPivot* gp, int tile, int ntile) {
+    __shared__ __align__(16) int32_t vt[kSweepTile];
+    FLOCK_GRID_STEP_PROLOGUE();
+    const bool full = grid_full_round(c);
+    if (blockIdx.x == 0 && threadIdx.x == 0) gp->full = full ? 1 : 0;
+    sweep_part(c, tile, ntile, full ? nullptr : c.prow, vt, (int)blockIdx.x, (int)gridDim.x);
+}
+
+// After a candidate sweep: every row when the candidates hold no negative
+// key (every block checks the same keys).
+__global__ void __launch_bounds__(kSweepThreads, 2) k_gsweep_rest(Ctx c, GridPivot* gp, int tile, int ntile) {
+    __shared__ __align__(16) int32_t vt[kSweepTile];
+    FLOCK_GRID_STEP_PROLOGUE();
+    if (grid_full_round(c)) return;
     const int m = c.I.m, pn = c.sc->pp_n;
     int neg = 0;
     for (int t = threadIdx.x; t < pn; t += blockDim.x) {
         const int i = c.prow[t];
         if (FLOCK_IN(i, m)) neg |= key_val(c.row_best[i]) < 0;
     }
-    neg = __syncthreads_or(neg);
-    if (threadIdx.x == 0 && !neg) gp->full = 1;
+    if (__syncthreads_or(neg)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) gp->full = 1;
+    sweep_part(c, tile, ntile, nullptr, vt, (int)blockIdx.x, (int)gridDim.x);
 }
 
-__global__ void __launch_bounds__(1024, 1) k_pselect_rows(Ctx c, GridPivot* gp) {
+__global__ void __launch_bounds__(1024, 1) k_gchoose(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
-    if (c.sc->done) return;
-    if (gp->full) select_candidate_rows(c, bs, false);
-    if (threadIdx.x == 0) c.sc->pp_age++;
+    FLOCK_GRID_STEP_PROLOGUE();
+    const bool full = gp->full != 0;
+    grid_choose(c, gp, bs, full, full && c.sc->pricing);
 }
 
-// End of a grid round: the current interval buffer, the int32 dual flag,
-// the pivot count and the round cap.
-__global__ void k_gend(Ctx c, GridPivot* gp) {
-    if (threadIdx.x != 0 || c.sc->done) return;
-    c.sc->ivp ^= 1;
-    c.sc->nwide += gp->dwide;
-    c.sc->narrow = c.sc->nwide == 0;
-    c.sc->pivots++;
-    c.sc->last_winners = 1;
-    if (c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
+__global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    FLOCK_GRID_STEP_PROLOGUE();
+    grid_member(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    FLOCK_GRID_STEP_PROLOGUE();
+    grid_pick(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    FLOCK_GRID_STEP_PROLOGUE();
+    grid_apply(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    FLOCK_GRID_STEP_PROLOGUE();
+    grid_update(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_finalize(Ctx c) {
@@ -955,11 +1007,12 @@ struct PlainSolver {
         return FLOCK_OK;
     }
 
-    int reset_scalars(Scalars* dsc, int mode, int max_rounds) {
+    int reset_scalars(Scalars* dsc, int mode, int max_rounds, bool partial = false) {
         Scalars z;
         memset(&z, 0, sizeof(z));
         z.mode = mode;
         z.max_rounds = max_rounds;
+        z.pricing = partial ? 1 : 0;
         z.pp_rows = kPPRowsLarge;             // partial pricing runs on the plain path from kGridPivotV vertices
         z.pp_refresh = kPPRefreshLarge;
         memcpy(h_sc.p, &z, sizeof(z));
@@ -996,7 +1049,9 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     Ctx c;
     int32_t* out3 = nullptr;
     if ((rc = P.prepare(I, c, &out3))) return rc;
-    if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds))) return rc;
+    // partial pricing runs on the plain path from kGridPivotV vertices (grid rounds)
+    const bool partial = opt.pricing == FLOCK_PRICING_PARTIAL && V >= kGridPivotV;
+    if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds, partial))) return rc;
     const int nt = threads_for(V);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     k_setup<<<1, nt, 0, P.stream>>>(c, opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL);
@@ -1004,54 +1059,71 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     int grid = 0, tile = 0, ntile = 0;
     sweep_shape(m, n, &grid, &tile, &ntile);
-    // partial pricing on the plain path for large instances (grid rounds)
-    const bool partial = opt.pricing == FLOCK_PRICING_PARTIAL && V >= kGridPivotV;
-    // pivot loop: chunks of rounds captured once as a CUDA graph
-    int chunk = 8;
-    cudaGraphExec_t exec = nullptr;
-    int exec_chunk = 0;
     Scalars* hs = P.h_sc.as<Scalars>();
-    for (;;) {
-        if (exec_chunk != chunk) {
-            if (exec) cudaGraphExecDestroy(exec);
-            exec = nullptr;
-            cudaGraph_t g;
-            FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
-            for (int r = 0; r < chunk; r++) {
-                if (partial) {
-                    k_pdecide<<<1, 32, 0, P.stream>>>(c, P.gp);
-                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, c.prow, &P.gp->full, 0);
-                    k_pcheck<<<1, 256, 0, P.stream>>>(c, P.gp);
-                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, &P.gp->full, 1);
-                    k_pselect_rows<<<1, 1024, 0, P.stream>>>(c, P.gp);
-                } else {
-                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+    if (V >= kGridPivotV) {
+        // large instance: the pivot round over the whole GPU, chunks of
+        // rounds captured once as a CUDA graph
+        FLOCK_CK(cudaMemsetAsync(P.gp, 0, sizeof(GridPivot), P.stream));
+        const int gg = std::max(1, std::min((V + 255) / 256, 2 * num_sms()));
+        int chunk = 8;
+        cudaGraphExec_t exec = nullptr;
+        int exec_chunk = 0;
+        for (;;) {
+            if (exec_chunk != chunk) {
+                if (exec) cudaGraphExecDestroy(exec);
+                exec = nullptr;
+                cudaGraph_t g;
+                FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+                for (int r = 0; r < chunk; r++) {
+                    k_gsweep<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
+                    if (partial) k_gsweep_rest<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
+                    k_gchoose<<<1, 1024, 0, P.stream>>>(c, P.gp);
+                    k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                    k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                    k_gapply<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                    k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
                 }
-                if (V < kGridPivotV) {
-                    k_pivot<<<1, nt, 0, P.stream>>>(c);
-                    continue;
-                }
-                // large instance: the pivot round over the whole GPU
-                const int gg = std::max(1, std::min((V + 255) / 256, 2 * num_sms()));
-                k_gselect<<<1, 1024, 0, P.stream>>>(c, P.gp);
-                k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                k_gapply<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                k_gend<<<1, 32, 0, P.stream>>>(c, P.gp);
+                FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
+                FLOCK_CK(cudaGraphInstantiate(&exec, g, 0));
+                cudaGraphDestroy(g);
+                exec_chunk = chunk;
             }
-            FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
-            FLOCK_CK(cudaGraphInstantiate(&exec, g, 0));
-            cudaGraphDestroy(g);
-            exec_chunk = chunk;
+            FLOCK_CK(cudaGraphLaunch(exec, P.stream));
+            FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
+            FLOCK_CK(cudaStreamSynchronize(P.stream));
+            if (hs->done) break;
+            if (chunk < 256) chunk *= 2;
         }
-        FLOCK_CK(cudaGraphLaunch(exec, P.stream));
-        FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
-        FLOCK_CK(cudaStreamSynchronize(P.stream));
-        if (hs->done) break;
-        if (chunk < 256) chunk *= 2;
+        if (exec) cudaGraphExecDestroy(exec);
+    } else {
+        // pivot loop: chunks of rounds (grid sweep, one-CTA pivot round)
+        // captured once as a CUDA graph
+        int chunk = 8;
+        cudaGraphExec_t exec = nullptr;
+        int exec_chunk = 0;
+        for (;;) {
+            if (exec_chunk != chunk) {
+                if (exec) cudaGraphExecDestroy(exec);
+                exec = nullptr;
+                cudaGraph_t g;
+                FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
+                for (int r = 0; r < chunk; r++) {
+                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+                    k_pivot<<<1, nt, 0, P.stream>>>(c);
+                }
+                FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
+                FLOCK_CK(cudaGraphInstantiate(&exec, g, 0));
+                cudaGraphDestroy(g);
+                exec_chunk = chunk;
+            }
+            FLOCK_CK(cudaGraphLaunch(exec, P.stream));
+            FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
+            FLOCK_CK(cudaStreamSynchronize(P.stream));
+            if (hs->done) break;
+            if (chunk < 256) chunk *= 2;
+        }
+        if (exec) cudaGraphExecDestroy(exec);
     }
-    if (exec) cudaGraphExecDestroy(exec);
     FLOCK_CK(cudaEventRecord(P.ev[2], P.stream));
     k_finalize<<<1, nt, 0, P.stream>>>(c);
     FLOCK_CK(cudaGetLastError());
