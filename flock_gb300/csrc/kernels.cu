@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(256) k_bsetup(BatchArgs a) {
 
 // Shared-memory staging of the arrays every pivot step touches: the tree,
 // the duals, the row keys and the preorder intervals; unless kLight (the
-// largest instances), also the single pivot's side marks, path and path
+// largest instances), also the single pivot's cycle chains and their
 // flows.  The edge claims of multi-pivot rounds and the pointer-jumping
 // block of the rebuilds (the first round and the rounds after multi-pivot
 // rounds) stay in the instance's global working set, which keeps the staged
@@ -703,7 +703,6 @@ __device__ __forceinline__ void stage_hot(Ctx& c, unsigned char* smem, int V, in
     if (kLight) return;
     c.pflow = (int64_t*)k.S(8 * (size_t)V);
     c.path = (int32_t*)k.S(4 * (size_t)V);
-    c.side = (uint8_t*)k.S((size_t)V);
 }
 
 // Rounds staging; the launch's dynamic block also holds the staged setup
@@ -712,7 +711,7 @@ inline size_t staged_bytes(int V, int M, bool light) {
     Carver k{nullptr, 0, (unsigned char*)16, 0};
     k.S(4 * (size_t)V); k.S(4 * (size_t)V); k.S(8 * (size_t)V); k.S(8 * (size_t)M); k.S(8 * (size_t)V);
     k.S(4 * (size_t)V); k.S(16 * (size_t)V);
-    if (!light) { k.S(8 * (size_t)V); k.S(4 * (size_t)V); k.S((size_t)V); }
+    if (!light) { k.S(8 * (size_t)V); k.S(4 * (size_t)V); }
     return (k.so + 15) & ~size_t(15);
 }
 
@@ -1328,7 +1327,7 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
 // -------------------------------------------------------- batched solver ---
 // Size buckets by V = m + n.  Instances above the last edge run on the plain
 // path (their staged tree would not fit in shared memory).
-// A bucket stages fully when its largest instance fits (57 V + 8 M bytes: up
+// A bucket stages fully when its largest instance fits (56 V + 8 M bytes: up
 // to V = 3500 or so); the others stage lightly (staged_bytes(4096, 4095,
 // true) = 208 KB).
 static const int kBucketEdges[] = {64, 128, 256, 512, 1024, 2048, 2944, 4096};

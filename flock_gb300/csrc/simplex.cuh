@@ -734,28 +734,32 @@ __device__ __forceinline__ uint64_t oflow(int64_t f) { return (uint64_t)f ^ 0x80
 // state updated in place of a rebuild.
 //
 // Cycle: a tree edge (child v) is on the cycle iff v's subtree holds exactly
-// one of k and l.  The leaving edge and theta follow cycle_walk's rule
+// one of k and l; the k side is the chain from k up to the apex, the l side
+// the chain from l.  The leaving edge and theta follow cycle_walk's rule
 // exactly: on the k side the decreasing edges are row children and ties go
 // to the deepest, on the l side column children, ties to the shallowest; the
 // l side wins ties between the sides.  One reduction of two (flow, tie key)
-// pairs gives both sides' candidates.
+// pairs gives both sides' candidates.  The same pass records both chains by
+// distance from their endpoint, with their flows (path[i] / pflow[i] for the
+// k side, path[V-1-i] / pflow[V-1-i] for the l side: the cycle has fewer
+// than V edges, so they never meet).
 //
 // Update: let q be the leaving edge's child, e the entering endpoint below
 // it (S = subtree of q holds e) and other the endpoint outside S.  The path
-// e = p_0, ..., p_t = q is reversed (p_i's new parent is p_(i-1), e's is
-// other) and S is re-hung below other.  For x in S whose deepest path
-// ancestor is p_i: depth' = depth(other) + 1 + i + (depth(x) - depth(p_i)),
-// and every dual in S shifts by the entering cell's reduced cost r (rows on
-// e's side of the bipartition by +r, the others by -r), so that the new tree
-// edge has zero reduced cost.  Intervals: S's block is cut out and re-inserted
-// right after other; inside it the branches of p_0, p_1, ... follow one
-// another (branch i = subtree(p_i) minus subtree(p_(i-1)), old order kept),
-// so that each subtree' is contiguous; sizes change on the path and on the
-// old and new ancestors of S.  Old intervals are read from one buffer of iv
-// and the new ones written to the other.
-// Scratch: side[] (cycle side marks), path[] (the path by index i),
-// pflow[] (the path edges' flows after the cycle update).  Returns 1 if the pivot was applied
-// (block-uniform).
+// e = p_0, ..., p_t = q (the start of e's chain) is reversed (p_i's new
+// parent is p_(i-1), e's is other, with the flow of the edge it replaces
+// after the cycle update) and S is re-hung below other; the other cycle
+// edges change by -/+theta.  For x in S whose deepest path ancestor is p_i:
+// depth' = depth(other) + 1 + i + (depth(x) - depth(p_i)), and every dual in
+// S shifts by the entering cell's reduced cost r (rows on e's side of the
+// bipartition by +r, the others by -r), so that the new tree edge has zero
+// reduced cost.  Intervals: S's block is cut out and re-inserted right after
+// other; inside it the branches of p_0, p_1, ... follow one another (branch
+// i = subtree(p_i) minus subtree(p_(i-1)), old order kept), so that each
+// subtree' is contiguous; sizes change on the path and on the old and new
+// ancestors of S.  Old intervals are read from one buffer of iv and the new
+// ones written to the other.  Two passes over the vertices, four barriers.
+// Returns 1 if the pivot was applied (block-uniform).
 template <int J = kJump>
 __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
     const int m = c.I.m;
@@ -763,70 +767,57 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
     const int2* ivA = c.iv + (par ? V : 0);
     int2* ivB = c.iv + (par ? 0 : V);
     const int pk = ivA[k].x, pl = ivA[l].x;
+    const int dk = c.depth[k], dl = c.depth[l];
+    // the entering cell's reduced cost (exact): read here, before any dual
+    // changes, like everything the update reads of other vertices (after the
+    // reduction other warps may already be rewriting depths, parents, duals)
+    const int64_t r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
+    int32_t* path = c.path;
+    int64_t* pflow = c.pflow;
     // (order-preserving flow, tie key): k side ties to the largest (depth, v),
     // so its key is complemented; l side to the smallest
     uint64_t kf = kNoKey, kt = kNoKey, lf = kNoKey, lt = kNoKey;
+    int bad = 0;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        int side = 0;
-        if (c.parent[v] >= 0) {
-            const int2 w = ivA[v];
-            const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
-            side = on_k != on_l ? (on_k ? 1 : 2) : 0;
-        }
-        c.side[v] = (uint8_t)side;
-        if (side == 1 && v < m)
-            pair_min_into(kf, kt, oflow(c.flow[v]), ~(((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v));
-        if (side == 2 && v >= m)
-            pair_min_into(lf, lt, oflow(c.flow[v]), ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v);
+        if (c.parent[v] < 0) continue;
+        const int2 w = ivA[v];
+        const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
+        if (on_k == on_l) continue;
+        const int dv = c.depth[v];
+        const int64_t f = c.flow[v];
+        const int i = on_k ? dk - dv : dl - dv;
+        if (!FLOCK_IN(i, V)) { bad = 1; continue; }
+        const int slot = on_k ? i : V - 1 - i;
+        path[slot] = v;
+        pflow[slot] = f;
+        const uint64_t tie = ((uint64_t)(uint32_t)dv << 32) | (uint32_t)v;
+        if (on_k && v < m) pair_min_into(kf, kt, oflow(f), ~tie);
+        if (on_l && v >= m) pair_min_into(lf, lt, oflow(f), tie);
     }
-    if (threadIdx.x == 0) { bs.i[4] = 0; bs.i[5] = 0; }   // ordered by the reduction's barriers
+    if (bad) { kf = 0; kt = 0; }                           // no real pair is (0, 0): it carries the failure
+    if (threadIdx.x == 0) bs.i[4] = 0;                     // ordered by the reduction's barriers
     block_min_pairs(kf, kt, lf, lt, bs);
-    const bool lside = lf <= kf;                   // uniform
+    if (kf == 0 && kt == 0) {                              // block-uniform
+        if (threadIdx.x == 0) fail_check(c.sc, 17);
+        __syncthreads();
+        return 0;
+    }
+    const bool lside = lf <= kf;                           // uniform
     const uint64_t fmin = lside ? lf : kf;
-    const int q = (int)(uint32_t)(lside ? lt : ~kt);
-    if (fmin == kNoKey || !FLOCK_IN(q, V) || c.parent[q] < 0) {
+    const uint64_t qkey = lside ? lt : ~kt;                // (depth << 32) | child of the leaving edge
+    const int q = (int)(uint32_t)qkey;
+    const int e = lside ? l : k, other = lside ? k : l;
+    const int de = lside ? dl : dk;
+    const int t = de - (int)(uint32_t)(qkey >> 32);
+    const int base = lside ? V - 1 : 0, dir = lside ? -1 : 1;   // e's chain entry i at path[base + dir * i]
+    if (fmin == kNoKey || !FLOCK_IN(q, V) || !FLOCK_IN(t, V) || path[base + dir * t] != q) {   // uniform
         if (threadIdx.x == 0) fail_check(c.sc, 16);
         __syncthreads();
         return 0;
     }
     const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
-    const int e = lside ? l : k, other = lside ? k : l;
-    const int de = c.depth[e], dq = c.depth[q], t = de - dq;
-    if (!FLOCK_IN(t, V)) {                         // the path indexes len1/acc1 (V entries)
-        if (threadIdx.x == 0) fail_check(c.sc, 17);
-        __syncthreads();
-        return 0;
-    }
-    const uint64_t eside = lside ? 2 : 1;
-    int32_t* path = c.path;
-    int64_t* pflow = c.pflow;
-    // flows along the cycle; the path from e up to q recorded by index
-    // the entering cell's reduced cost (exact), read before any dual changes
-    const int64_t r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
-    const int dother = c.depth[other];
-    int npath = 0, bad = 0;
-    for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        const uint64_t sd = c.side[v];
-        if (!sd) continue;
-        const int64_t delta = (sd == 1) == (v < m) ? -th : th;
-        const int dv = c.depth[v];
-        if (sd == eside && dv >= dq) {
-            const int i = de - dv;
-            if (!FLOCK_IN(i, t + 1)) { bad = 1; continue; }
-            path[i] = v;
-            pflow[i] = c.flow[v] + delta;
-            npath++;
-        } else {
-            c.flow[v] += delta;
-        }
-    }
-    if (npath) atomicAdd(&bs.i[5], npath);
-    bad = __syncthreads_or(bad);
-    if (bad || bs.i[5] != t + 1 || path[t] != q) {
-        if (threadIdx.x == 0) fail_check(c.sc, 17);
-        __syncthreads();
-        return 0;
-    }
+    const int eside = lside ? 2 : 1;
+    const int dother = lside ? dk : dl;
     const int2 Q = ivA[q], O = ivA[other];
     const int P = Q.x, s = Q.y;
     const int ins = O.x - (O.x >= P + s ? s : 0) + 1;   // S's new first position
@@ -834,25 +825,32 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
     const bool erow = e < m;
     int dwide = 0;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
-        if (c.parent[v] == -2) continue;               // not in the tree
+        const int pv0 = c.parent[v];
+        if (pv0 == -2) continue;                       // not in the tree
         const int2 w = ivA[v];
+        int side = 0;
+        if (pv0 >= 0) {
+            const bool on_k = iv_in(w, pk), on_l = iv_in(w, pl);
+            side = on_k != on_l ? (on_k ? 1 : 2) : 0;
+        }
         int2 nw;
         if (iv_in(Q, w.x)) {
             // deepest path vertex above v: smallest i whose subtree holds v
             int lo = 0, hi = t;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                const int pv = path[mid];
+                const int pv = path[base + dir * mid];
                 if (!FLOCK_IN(pv, V)) { bad = 1; break; }
                 if (iv_in(ivA[pv], w.x)) hi = mid; else lo = mid + 1;
             }
             const int i = lo;
-            const int pi = path[i];
+            const int pi = path[base + dir * i];
             if (!FLOCK_IN(pi, V)) { bad = 1; continue; }
             const int2 Pi = ivA[pi];
             int off = 0, rank = w.x - Pi.x;
+            int pc = -1;
             if (i > 0) {
-                const int pc = path[i - 1];
+                pc = path[base + dir * (i - 1)];
                 if (!FLOCK_IN(pc, V)) { bad = 1; continue; }
                 const int2 Pc = ivA[pc];
                 off = Pc.y;
@@ -870,11 +868,13 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
                 c.v32[v - m] = narrow_dual(p1, w1);
                 dwide += w1 - w0;
             }
-            if (v == pi) {
-                c.parent[v] = i == 0 ? other : path[i - 1];
-                c.flow[v] = i == 0 ? th : pflow[i - 1];
+            if (v == pi) {                             // the reversed path (every cycle edge in S is on it)
+                c.parent[v] = i == 0 ? other : pc;
+                c.flow[v] = i == 0 ? th
+                                   : pflow[base + dir * (i - 1)] + ((eside == 1) == (pc < m) ? -th : th);
             }
         } else {
+            if (side) c.flow[v] += (side == 1) == (v < m) ? -th : th;
             const int y = w.x - (w.x >= P + s ? s : 0);
             nw.x = y + (y >= ins ? s : 0);
             nw.y = w.y - (iv_in(w, P) ? s : 0) + (iv_in(w, O.x) ? s : 0);
