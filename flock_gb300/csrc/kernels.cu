@@ -154,22 +154,22 @@ __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
 
 // ------------------------------------------------- grid pivot round -------
 // The plain solver's rounds for large instances, spread over the whole GPU:
-// seven graph-captured kernels per round, the kernel boundaries the only
+// six graph-captured kernels per round, the kernel boundaries the only
 // synchronisation (a grid-wide barrier inside one cooperative launch costs
 // as much as a boundary on this two-die part).  One pivot per round
 // (Dantzig's rule: the most negative row key, first row among ties); the
 // steps follow single_pivot_iv exactly (same interval membership test, tie
 // rules, path reversal and in-place update of depths, duals and intervals),
-// so a round costs the same seven launches whatever the tree's depth.
+// so a round costs the same six launches whatever the tree's depth.
 struct GridPivot {
     uint64_t best;          // entering candidate: (reduced cost, row)
     uint64_t mk, ml;        // per side: minimum order-preserving flow
     uint64_t qk, ql;        // per side: leaving edge (depth << 32 | child)
-    int32_t npath;          // path vertices recorded by the apply step
+    int32_t pad0_;
     int32_t dwide;          // change of the count of int32-window misses
     int32_t full;           // partial pricing: this round swept every row
     uint32_t fin_count;     // blocks done with the update step
-    // the pivot, fixed by the apply step before the update changes depths and duals
+    // the pivot, fixed by the pick step's last block before the update changes depths and duals
     int64_t th, r;
     int32_t ok, e, other, q, de, dq, t, dother, eside, pad2_;
     int2 Q, O;
@@ -204,7 +204,6 @@ __device__ void grid_choose(const Ctx& c, GridPivot* gp, BlockScratch& bs, bool 
         gp->mk = gp->ml = kNoKey;
         gp->qk = 0;
         gp->ql = kNoKey;
-        gp->npath = 0;
         gp->dwide = 0;
         gp->ok = 0;
         gp->fin_count = 0;
@@ -215,13 +214,17 @@ __device__ void grid_choose(const Ctx& c, GridPivot* gp, BlockScratch& bs, bool 
     }
 }
 
-// Cycle membership by intervals and each side's smallest decreasing flow.
+// Cycle membership by intervals, each side's smallest decreasing flow, and
+// both cycle chains by distance from their endpoint with their flows
+// (path[i] / pflow[i] for the k side, path[V-1-i] / pflow[V-1-i] for the l
+// side, as single_pivot_iv records them).
 __device__ void grid_member(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
     const int m = c.I.m, V = m + c.I.n;
     const int k = (int)key_idx(gp->best);
     const int l = m + (int)key_idx(c.row_best[k]);
     const int2* iv = iv_now(c, V);
     const int pk = iv[k].x, pl = iv[l].x;
+    const int dk = c.depth[k], dl = c.depth[l];
     uint64_t mk = kNoKey, ml = kNoKey;
     for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
         int side = 0;
@@ -231,8 +234,15 @@ __device__ void grid_member(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
             if (on_k != on_l) side = on_k ? 1 : 2;
         }
         c.side[v] = (uint8_t)side;
-        if (side == 1 && v < m) { const uint64_t f = oflow(c.flow[v]); mk = f < mk ? f : mk; }
-        if (side == 2 && v >= m) { const uint64_t f = oflow(c.flow[v]); ml = f < ml ? f : ml; }
+        if (!side) continue;
+        const int64_t f = c.flow[v];
+        const int i = (side == 1 ? dk : dl) - c.depth[v];
+        if (!FLOCK_IN(i, V)) { fail_check(c.sc, 17); continue; }
+        const int slot = side == 1 ? i : V - 1 - i;
+        c.path[slot] = v;
+        c.pflow[slot] = f;
+        if (side == 1 && v < m) { const uint64_t o = oflow(f); mk = o < mk ? o : mk; }
+        if (side == 2 && v >= m) { const uint64_t o = oflow(f); ml = o < ml ? o : ml; }
     }
     mk = block_min_u64(mk, bs);
     ml = block_min_u64(ml, bs);
@@ -264,80 +274,51 @@ __device__ void grid_pick(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid
     if (threadIdx.x == 0) {
         if (lside && pick != kNoKey) atomicMin((unsigned long long*)&gp->ql, (unsigned long long)pick);
         if (!lside && pick != 0) atomicMax((unsigned long long*)&gp->qk, (unsigned long long)pick);
-    }
-}
-
-// Flows along the cycle change by -/+theta except on the path from the
-// entering endpoint e up to the leaving edge, whose vertices are recorded by
-// index (path) with their updated flows (pflow) for the update step.  Block
-// 0 also fixes the pivot's parameters in gp (nothing here changes depths,
-// duals or intervals, so every block computes the same ones).
-__device__ void grid_apply(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
-    const int m = c.I.m, V = m + c.I.n;
-    const bool lside = gp->ml <= gp->mk;
-    const uint64_t fmin = lside ? gp->ml : gp->mk;
-    const uint64_t pick = lside ? gp->ql : gp->qk;
-    const int q = (int)(uint32_t)pick;
-    if (fmin == kNoKey || (lside ? pick == kNoKey : pick == 0) || !FLOCK_IN(q, V) || c.parent[q] < 0) {
-        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
-        return;
-    }
-    const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
-    const int k = (int)key_idx(gp->best);
-    const int l = m + (int)key_idx(c.row_best[k]);
-    const int e = lside ? l : k, other = lside ? k : l;
-    const int de = c.depth[e], dq = c.depth[q], t = de - dq;
-    if (!FLOCK_IN(t, V)) {                         // the path indexes path/pflow (V entries)
-        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
-        return;
-    }
-    const uint64_t eside = lside ? 2 : 1;
-    if (threadIdx.x == 0) bs.i[6] = 0;
-    __syncthreads();
-    int n = 0;
-    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
-        const uint64_t sd = c.side[v];
-        if (!sd) continue;
-        const int64_t delta = (sd == 1) == (v < m) ? -th : th;
-        const int dv = c.depth[v];
-        if (sd == eside && dv >= dq) {
-            const int i = de - dv;
-            if (!FLOCK_IN(i, t + 1)) { fail_check(c.sc, 17); continue; }
-            c.path[i] = v;
-            c.pflow[i] = c.flow[v] + delta;
-            n++;
-        } else {
-            c.flow[v] += delta;
+        __threadfence();
+        // the last block to finish fixes the pivot's parameters for the
+        // update (nothing in this step changes depths, duals or intervals)
+        if (atomicAdd(&gp->fin_count, 1u) == (unsigned)nb - 1) {
+            __threadfence();
+            gp->fin_count = 0;
+            const uint64_t q64 = lside ? *(volatile uint64_t*)&gp->ql : *(volatile uint64_t*)&gp->qk;
+            const int q = (int)(uint32_t)q64;
+            const int k = (int)key_idx(gp->best);
+            const int l = m + (int)key_idx(c.row_best[k]);
+            const int e = lside ? l : k, other = lside ? k : l;
+            const int de = c.depth[e];
+            const int t = (lside ? q64 != kNoKey : q64 != 0) && FLOCK_IN(q, V) ? de - c.depth[q] : -1;
+            const int slot = lside ? V - 1 - t : t;
+            if (!FLOCK_IN(t, V) || c.path[slot] != q) {
+                fail_check(c.sc, 17);
+            } else {
+                const int2* iv = iv_now(c, V);
+                gp->th = (int64_t)(fmin ^ 0x8000000000000000ull);
+                gp->r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
+                gp->e = e; gp->other = other; gp->q = q;
+                gp->de = de; gp->dq = c.depth[q]; gp->t = t;
+                gp->dother = c.depth[other];
+                gp->eside = lside ? 2 : 1;
+                gp->Q = iv[q]; gp->O = iv[other];
+                gp->ok = 1;
+            }
         }
     }
-    if (n) atomicAdd(&bs.i[6], n);
-    __syncthreads();
-    if (threadIdx.x == 0 && bs.i[6]) atomicAdd(&gp->npath, bs.i[6]);
-    if (bid == 0 && threadIdx.x == 0) {
-        const int2* iv = iv_now(c, V);
-        gp->th = th;
-        gp->r = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
-        gp->e = e; gp->other = other; gp->q = q;
-        gp->de = de; gp->dq = dq; gp->t = t;
-        gp->dother = c.depth[other];
-        gp->eside = (int32_t)eside;
-        gp->Q = iv[q]; gp->O = iv[other];
-        gp->ok = 1;
-    }
 }
 
-// The tree update of single_pivot_iv over the grid: new intervals into the
-// other half of iv, depths and duals of the re-hung subtree, the reversed
-// path's parents and flows; every row key cleared for the next sweep.  The
-// last block to finish ends the round: the current interval buffer, the
-// int32 dual flag, the pivot count and the round cap.
+// The tree update of single_pivot_iv over the grid: the cycle's flows, new
+// intervals into the other half of iv, depths and duals of the re-hung
+// subtree, the reversed path's parents and flows; every row key cleared for
+// the next sweep.  The last block to finish ends the round: the current
+// interval buffer, the int32 dual flag, the pivot count and the round cap.
 __device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
     const int m = c.I.m, V = m + c.I.n;
-    const int t = gp->t, q = gp->q;
-    if (!gp->ok || !FLOCK_IN(t, V) || gp->npath != t + 1 || c.path[t] != q) {
+    const int t = gp->t;
+    if (!gp->ok || !FLOCK_IN(t, V)) {
         if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
         return;
     }
+    const bool lside = gp->eside == 2;
+    const int base = lside ? V - 1 : 0, dir = lside ? -1 : 1;   // e's chain entry i at path[base + dir * i]
     const int par = c.sc->ivp;
     const int2* ivA = c.iv + (par ? V : 0);
     int2* ivB = c.iv + (par ? 0 : V);
@@ -348,6 +329,7 @@ __device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
     const int other = gp->other;
     const bool erow = gp->e < m;
     const int64_t r = gp->r, th = gp->th;
+    const int eside = gp->eside;
     const int32_t* path = c.path;
     const int64_t* pflow = c.pflow;
     if (threadIdx.x == 0) bs.i[7] = 0;
@@ -356,22 +338,24 @@ __device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
     for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
         if (c.parent[v] == -2) continue;
         const int2 w = ivA[v];
+        const int side = c.side[v];
         int2 nw;
         if (iv_in(Q, w.x)) {
             int lo = 0, hi = t;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                const int pv = path[mid];
+                const int pv = path[base + dir * mid];
                 if (!FLOCK_IN(pv, V)) { bad = 1; break; }
                 if (iv_in(ivA[pv], w.x)) hi = mid; else lo = mid + 1;
             }
             const int i = lo;
-            const int pi = path[i];
+            const int pi = path[base + dir * i];
             if (!FLOCK_IN(pi, V)) { bad = 1; continue; }
             const int2 Pi = ivA[pi];
             int off = 0, rank = w.x - Pi.x;
+            int pc = -1;
             if (i > 0) {
-                const int pc = path[i - 1];
+                pc = path[base + dir * (i - 1)];
                 if (!FLOCK_IN(pc, V)) { bad = 1; continue; }
                 const int2 Pc = ivA[pc];
                 off = Pc.y;
@@ -389,11 +373,13 @@ __device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
                 c.v32[v - m] = narrow_dual(p1, w1);
                 dwide += w1 - w0;
             }
-            if (v == pi) {
-                c.parent[v] = i == 0 ? other : path[i - 1];
-                c.flow[v] = i == 0 ? th : pflow[i - 1];
+            if (v == pi) {                             // the reversed path (every cycle edge in S is on it)
+                c.parent[v] = i == 0 ? other : pc;
+                c.flow[v] = i == 0 ? th
+                                   : pflow[base + dir * (i - 1)] + ((eside == 1) == (pc < m) ? -th : th);
             }
         } else {
+            if (side) c.flow[v] += (side == 1) == (v < m) ? -th : th;
             const int y = w.x - (w.x >= P + s ? s : 0);
             nw.x = y + (y >= ins ? s : 0);
             nw.y = w.y - (iv_in(w, P) ? s : 0) + (iv_in(w, O.x) ? s : 0);
@@ -474,12 +460,6 @@ __global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
     FLOCK_GRID_STEP_PROLOGUE();
     grid_pick(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
-}
-
-__global__ void __launch_bounds__(256) k_gapply(Ctx c, GridPivot* gp) {
-    __shared__ BlockScratch bs;
-    FLOCK_GRID_STEP_PROLOGUE();
-    grid_apply(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
 }
 
 __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
@@ -1079,7 +1059,6 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                     k_gchoose<<<1, 1024, 0, P.stream>>>(c, P.gp);
                     k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
                     k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                    k_gapply<<<gg, 256, 0, P.stream>>>(c, P.gp);
                     k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
                 }
                 FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
