@@ -1369,6 +1369,7 @@ struct BatchRunner {
     std::vector<std::vector<flock_flow>> plain_flows;
     int32_t launches = 0;                   // kernels launched by the last run
     bool packed = false;                    // every bucket packed into the staging buffers
+    std::vector<uint8_t> cost_bad, cost_checked;   // per instance: cost out of range / range checked
 
     int setup() {
         if (init) return FLOCK_OK;
@@ -1401,19 +1402,29 @@ struct BatchRunner {
         cost_off.assign(cnt, 0); sd_off.assign(cnt, 0); ws_off.assign(cnt, 0);
         plain_list.clear();
         total_cells = total_pot = total_cost = total_sd = total_ws = 0;
-        // Validation in the order validate_instance uses: every shape check,
-        // then the O(m n) cost range check (threads over instances); the
-        // first failing instance reports its first failing check.  Nothing is
-        // launched before every instance has passed.
+        // Validation with the result validate_instance gives one instance at a
+        // time: the first failing instance reports its first failing check
+        // (shape, then the cost range).  Shapes are checked here; the cost
+        // range of a staged instance is checked while its bucket is packed,
+        // before that bucket is uploaded or launched (a bad one stops the
+        // call, see cost_failure); the plain-path instances' costs here.
         std::vector<int> pre(cnt, FLOCK_OK);
         std::vector<std::string> pre_msg(cnt);
-        for (int k = 0; k < cnt; k++) {
-            if ((pre[k] = validate_shape(&in[k], &pre_msg[k]))) continue;
-            m_of[k] = in[k].m; n_of[k] = in[k].n; V_of[k] = in[k].m + in[k].n;
-        }
-        std::vector<uint8_t> cost_bad(cnt, 0);
         parallel_for(cnt, [&](int k) {
-            if (!pre[k]) cost_bad[k] = !costs_in_range(in[k].cost, (size_t)m_of[k] * n_of[k]);
+            if ((pre[k] = validate_shape(&in[k], &pre_msg[k]))) return;
+            m_of[k] = in[k].m; n_of[k] = in[k].n; V_of[k] = in[k].m + in[k].n;
+        });
+        cost_bad.assign(cnt, 0);
+        cost_checked.assign(cnt, 0);
+        int first_bad = cnt;
+        for (int k = 0; k < cnt; k++) if (pre[k]) { first_bad = k; break; }
+        parallel_for(cnt, [&](int k) {
+            if (!pre[k] && (V_of[k] > kMaxStagedV || k < first_bad)) {
+                if (V_of[k] > kMaxStagedV || first_bad < cnt) {
+                    cost_bad[k] = !costs_in_range(in[k].cost, (size_t)m_of[k] * n_of[k]);
+                    cost_checked[k] = 1;
+                }
+            }
         });
         for (int k = 0; k < cnt; k++) {
             if (pre[k]) { set_error(pre_msg[k]); return pre[k]; }
@@ -1457,30 +1468,53 @@ struct BatchRunner {
     }
 
     // Pack bucket b's costs (row pitch padded to 4) and quantities into the
-    // pinned staging buffers (threads over instances).
-    void pack_bucket(int b) {
+    // pinned staging buffers (threads over instances), checking the cost
+    // range in the same pass.  Returns false if an instance of the bucket
+    // has a cost outside |c| <= 2^30 (flagged in cost_bad).
+    bool pack_bucket(int b) {
+        std::atomic<int> bad{0};
         parallel_for(bstart[b + 1] - bstart[b], [&](int q) {
             const int k = order_[bstart[b] + q];
             const int m = m_of[k], n = n_of[k], ldc = (n + 3) & ~3;
             int32_t* dst = h_cost.as<int32_t>() + cost_off[k];
+            bool ok = true;
             if (ldc == n) {
-                memcpy(dst, insts[k].cost, (size_t)m * n * 4);
+                ok = copy_costs_checked(dst, insts[k].cost, m * n);
             } else {
                 for (int i = 0; i < m; i++) {
-                    memcpy(dst + (size_t)i * ldc, insts[k].cost + (size_t)i * n, (size_t)n * 4);
+                    ok &= copy_costs_checked(dst + (size_t)i * ldc, insts[k].cost + (size_t)i * n, n);
                     for (int j = n; j < ldc; j++) dst[(size_t)i * ldc + j] = 0;
                 }
             }
+            cost_checked[k] = 1;
+            if (!ok) { cost_bad[k] = 1; bad.store(1); }
             memcpy(h_sd.as<int32_t>() + sd_off[k], insts[k].supply, (size_t)m * 4);
             memcpy(h_sd.as<int32_t>() + sd_off[k] + m, insts[k].demand, (size_t)n * 4);
         });
+        return !bad.load();
+    }
+
+    // A cost range failure found while packing: wait for the buckets already
+    // launched, check the instances not packed yet, and report the first
+    // failing instance (validate_instance's error for it).
+    int cost_failure() {
+        for (auto s : st) cudaStreamSynchronize(s);
+        parallel_for(count, [&](int k) {
+            if (!cost_checked[k]) {
+                cost_bad[k] = !costs_in_range(insts[k].cost, (size_t)m_of[k] * n_of[k]);
+                cost_checked[k] = 1;
+            }
+        });
+        packed = false;
+        set_error("cost out of range");
+        return FLOCK_ERR_RANGE;
     }
 
     // Pack and upload bucket b on stream s (its cost and quantity ranges are
     // contiguous in both arenas).
     int stage_bucket(int b, cudaStream_t s) {
         if (bstart[b + 1] == bstart[b]) return FLOCK_OK;
-        pack_bucket(b);
+        if (!pack_bucket(b)) return cost_failure();
         const int k0 = order_[bstart[b]], k1 = order_[bstart[b + 1] - 1];
         const int64_t c0 = cost_off[k0], c1 = cost_off[k1] + (int64_t)m_of[k1] * ((n_of[k1] + 3) & ~3);
         const int64_t s0 = sd_off[k0], s1 = sd_off[k1] + V_of[k1];
@@ -1668,7 +1702,9 @@ struct BatchRunner {
     int upload() {
         cudaStream_t s0 = st[0];
         if (!packed) {
-            for (int b = 0; b < kNumBuckets; b++) pack_bucket(b);
+            bool ok = true;
+            for (int b = 0; b < kNumBuckets; b++) ok &= pack_bucket(b);
+            if (!ok) return cost_failure();
             packed = true;
         }
         if (total_cost) FLOCK_CK(cudaMemcpyAsync(d_cost.p, h_cost.p, (size_t)total_cost * 4, cudaMemcpyHostToDevice, s0));

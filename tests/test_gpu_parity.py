@@ -204,6 +204,29 @@ def test_batch_validation_first_failure():
     assert all(r.status == 0 and r.certified for r in out)
 
 
+def test_batch_validation_after_launch():
+    """Costs are range-checked while each size bucket is packed, largest
+    bucket first: a bad cost in a small instance is found after the large
+    buckets were launched, and the call still fails with the first failing
+    instance's error and no results; a shape error later in the list does
+    not hide an earlier cost error in another bucket."""
+    big = [fg.generate(0, 960 + k, 300, 280, 1, 100, 10, 50) for k in range(3)]
+    small_bad = fg.generate(0, 970, 12, 9, 1, 100, 10, 50)
+    small_bad.cost = small_bad.cost.copy()
+    small_bad.cost[5, 2] = -(1 << 30) - 1
+    with pytest.raises(RuntimeError) as e1:
+        fg.batch_solve(big + [small_bad])
+    assert "cost out of range" in str(e1.value)
+    bad_shape = fg.generate(0, 971, 40, 30, 1, 100, 10, 50)
+    bad_shape.demand = bad_shape.demand.copy()
+    bad_shape.demand[1] = -5
+    with pytest.raises(RuntimeError) as e2:
+        fg.batch_solve([big[0], small_bad, big[1], bad_shape])
+    assert "cost out of range" in str(e2.value)
+    out = fg.batch_solve(big + [fg.generate(0, 972, 12, 9, 1, 100, 10, 50)])
+    assert all(r.status == 0 and r.certified for r in out)
+
+
 @pytest.mark.parametrize("form", ["persistent", "round"])
 def test_batch_partial_pricing_all_buckets(form, monkeypatch):
     """Partial pricing (candidate rows) in both batched forms on every size
