@@ -194,15 +194,18 @@ __device__ __forceinline__ int32_t clamp32(int64_t r) {
     return r < INT32_MIN ? INT32_MIN : (r > INT32_MAX ? INT32_MAX : (int32_t)r);
 }
 
+// Warp minimum / maximum of 64-bit unsigned keys, exact, with the hardware
+// 32-bit warp reductions: the high words first, then the low words among the
+// lanes holding the winning high word.
 __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) { uint64_t w = __shfl_xor_sync(0xffffffffu, v, o); v = w < v ? w : v; }
-    return v;
+    const unsigned hi = __reduce_min_sync(0xffffffffu, (unsigned)(v >> 32));
+    const unsigned lo = __reduce_min_sync(0xffffffffu, (unsigned)(v >> 32) == hi ? (unsigned)v : 0xffffffffu);
+    return ((uint64_t)hi << 32) | lo;
 }
 __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) { uint64_t w = __shfl_xor_sync(0xffffffffu, v, o); v = w > v ? w : v; }
-    return v;
+    const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32));
+    const unsigned lo = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32) == hi ? (unsigned)v : 0u);
+    return ((uint64_t)hi << 32) | lo;
 }
 __device__ __forceinline__ int64_t warp_sum_i64(int64_t v) {
     #pragma unroll
@@ -268,14 +271,21 @@ __device__ __forceinline__ int64_t block_sum_i64(int64_t v, BlockScratch& bs) {
 __device__ __forceinline__ void pair_min_into(uint64_t& a, uint64_t& b, uint64_t c, uint64_t d) {
     if (c < a || (c == a && d < b)) { a = c; b = d; }
 }
+// Warp lexicographic minimum of (a, b), exact, in four 32-bit warp
+// reductions (a's words, then b's among the lanes holding the minimal a).
+__device__ __forceinline__ void warp_min_pair(uint64_t& a, uint64_t& b) {
+    const unsigned ah = __reduce_min_sync(0xffffffffu, (unsigned)(a >> 32));
+    const unsigned al = __reduce_min_sync(0xffffffffu, (unsigned)(a >> 32) == ah ? (unsigned)a : 0xffffffffu);
+    const uint64_t amin = ((uint64_t)ah << 32) | al;
+    const bool at = a == amin;
+    const unsigned bh = __reduce_min_sync(0xffffffffu, at ? (unsigned)(b >> 32) : 0xffffffffu);
+    const unsigned bl = __reduce_min_sync(0xffffffffu, at && (unsigned)(b >> 32) == bh ? (unsigned)b : 0xffffffffu);
+    a = amin;
+    b = ((uint64_t)bh << 32) | bl;
+}
 __device__ __forceinline__ void warp_min_pairs(uint64_t& a, uint64_t& b, uint64_t& c, uint64_t& d) {
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint64_t a2 = __shfl_xor_sync(0xffffffffu, a, o), b2 = __shfl_xor_sync(0xffffffffu, b, o);
-        const uint64_t c2 = __shfl_xor_sync(0xffffffffu, c, o), d2 = __shfl_xor_sync(0xffffffffu, d, o);
-        pair_min_into(a, b, a2, b2);
-        pair_min_into(c, d, c2, d2);
-    }
+    warp_min_pair(a, b);
+    warp_min_pair(c, d);
 }
 __device__ __forceinline__ void block_min_pairs(uint64_t& a, uint64_t& b, uint64_t& c, uint64_t& d, BlockScratch& bs) {
     warp_min_pairs(a, b, c, d);

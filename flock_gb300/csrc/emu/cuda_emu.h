@@ -110,6 +110,24 @@ template <class T> inline T __shfl_up_sync(unsigned, T v, int o) {
     return emu_shfl(v, lane >= o ? (int)threadIdx.x - o : (int)threadIdx.x);
 }
 
+// Warp reductions (32-bit): every lane of the caller's warp gets the result.
+inline unsigned emu_reduce(unsigned v, bool take_max) {
+    emu::Cta* c = emu::cta();
+    emu::warp_sync_at(-5);
+    c->xchg[threadIdx.x] = v;
+    emu::warp_sync_at(-6);
+    const unsigned w0 = threadIdx.x & ~31u;
+    unsigned r = (unsigned)c->xchg[w0];
+    for (unsigned l = 1; l < 32; l++) {
+        const unsigned x = (unsigned)c->xchg[w0 + l];
+        r = take_max ? (x > r ? x : r) : (x < r ? x : r);
+    }
+    emu::warp_sync_at(-7);
+    return r;
+}
+inline unsigned __reduce_min_sync(unsigned, unsigned v) { return emu_reduce(v, false); }
+inline unsigned __reduce_max_sync(unsigned, unsigned v) { return emu_reduce(v, true); }
+
 template <class T, class U> inline T atomicAdd(T* p, U v) { return std::atomic_ref<T>(*p).fetch_add((T)v); }
 template <class T, class U> inline T atomicOr(T* p, U v) { return std::atomic_ref<T>(*p).fetch_or((T)v); }
 template <class T, class U> inline T atomicExch(T* p, U v) { return std::atomic_ref<T>(*p).exchange((T)v); }
