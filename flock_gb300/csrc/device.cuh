@@ -313,13 +313,15 @@ __device__ __forceinline__ void top2_merge(uint64_t& a1, uint64_t& a2, uint64_t 
     else         { f = b1; s = a1 < b2 ? a1 : b2; }
     a1 = f; a2 = s;
 }
+// Every lane ends with the warp's two smallest keys.  Keys other than kNoKey
+// are distinct (they carry their index), so the second is the smallest of
+// every lane's first key, except that the lane holding the overall first
+// offers its second instead.
 __device__ __forceinline__ void warp_top2(uint64_t& a1, uint64_t& a2) {
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        uint64_t b1 = __shfl_xor_sync(0xffffffffu, a1, o);
-        uint64_t b2 = __shfl_xor_sync(0xffffffffu, a2, o);
-        top2_merge(a1, a2, b1, b2);
-    }
+    const uint64_t m1 = warp_min_u64(a1);
+    const uint64_t m2 = warp_min_u64(a1 == m1 ? a2 : a1);
+    a1 = m1;
+    a2 = m2;
 }
 
 __device__ __forceinline__ int32_t cost_of(const InstDev& I, int row, int col) {
