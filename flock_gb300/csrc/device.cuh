@@ -223,19 +223,16 @@ struct BlockScratch {
     int32_t i[12];
 };
 
+// Block reductions: warp results in shared memory, then every warp reduces
+// them itself (no broadcast barrier).  The leading barrier keeps the previous
+// reduction's readers ahead of this one's writes.
 __device__ __forceinline__ uint64_t block_min_u64(uint64_t v, BlockScratch& bs) {
     v = warp_min_u64(v);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
     __syncthreads();
     if (l == 0) bs.red[w] = v;
     __syncthreads();
-    if (w == 0) {
-        uint64_t x = l < nw ? bs.red[l] : kNoKey;
-        x = warp_min_u64(x);
-        if (l == 0) bs.red[0] = x;
-    }
-    __syncthreads();
-    return bs.red[0];
+    return warp_min_u64(l < nw ? bs.red[l] : kNoKey);
 }
 __device__ __forceinline__ uint64_t block_max_u64(uint64_t v, BlockScratch& bs) {
     v = warp_max_u64(v);
@@ -243,13 +240,7 @@ __device__ __forceinline__ uint64_t block_max_u64(uint64_t v, BlockScratch& bs) 
     __syncthreads();
     if (l == 0) bs.red[w] = v;
     __syncthreads();
-    if (w == 0) {
-        uint64_t x = l < nw ? bs.red[l] : 0ull;
-        x = warp_max_u64(x);
-        if (l == 0) bs.red[0] = x;
-    }
-    __syncthreads();
-    return bs.red[0];
+    return warp_max_u64(l < nw ? bs.red[l] : 0ull);
 }
 __device__ __forceinline__ int64_t block_sum_i64(int64_t v, BlockScratch& bs) {
     v = warp_sum_i64(v);
@@ -293,14 +284,9 @@ __device__ __forceinline__ void block_min_pairs(uint64_t& a, uint64_t& b, uint64
     __syncthreads();
     if (l == 0) { bs.red[w] = a; bs.red2[w] = b; bs.red3[w] = c; bs.red4[w] = d; }
     __syncthreads();
-    if (w == 0) {
-        uint64_t x = kNoKey, y = kNoKey, z = kNoKey, u = kNoKey;
-        if (l < nw) { x = bs.red[l]; y = bs.red2[l]; z = bs.red3[l]; u = bs.red4[l]; }
-        warp_min_pairs(x, y, z, u);
-        if (l == 0) { bs.red[0] = x; bs.red2[0] = y; bs.red3[0] = z; bs.red4[0] = u; }
-    }
-    __syncthreads();
-    a = bs.red[0]; b = bs.red2[0]; c = bs.red3[0]; d = bs.red4[0];
+    a = b = c = d = kNoKey;
+    if (l < nw) { a = bs.red[l]; b = bs.red2[l]; c = bs.red3[l]; d = bs.red4[l]; }
+    warp_min_pairs(a, b, c, d);
 }
 
 // Two smallest keys: insert / merge.

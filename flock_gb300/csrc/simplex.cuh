@@ -550,7 +550,7 @@ __device__ uint64_t select_candidate_rows(const Ctx& c, BlockScratch& bs, bool c
     const int cap = min(max(c.sc->pp_rows, 1), kPPRows);
     int32_t rmin = 0;
     for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
-    rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
+    rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));
     const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
     int last = -1;                                             // highest histogram bin kept
     if (rmin < 0) {
@@ -953,7 +953,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best =
             if (k != kNoKey && key_val(k) < 0 && key_idx(k) >= ncols) { fail_check(c.sc, 18); continue; }
             if (k != kNoKey) rmin = min(rmin, key_val(k));
         }
-        rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));   // ends with a barrier
+        rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));
         if (rmin < 0) {
             const int64_t span = -(int64_t)rmin;
             if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
