@@ -124,9 +124,9 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
         }
         const int4 t = c.top2[v];
         if (!top2_valid(c, v, t)) { c.rescan[atomicAdd(&bs.i[ctr], 1)] = v; continue; }
-        const int32_t p = vogel_penalty(t);
-        c.diff[v] = p;
-        const uint64_t k = pack_i32(p, (uint32_t)v);
+        // a valid cache's penalty is the stored one: every cache rebuild
+        // stores its penalty with it
+        const uint64_t k = pack_i32(c.diff[v], (uint32_t)v);
         mx = k > mx ? k : mx;
     }
     __syncthreads();
@@ -209,22 +209,29 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
         c.covered[v] = 0;
         c.res[v] = v < m ? I.supply[v] : I.demand[v - m];
-        c.diff[v] = 0;
     }
     // initial caches: rows one warp per row (coalesced), columns one thread
     // per column walking down the rows (coalesced across the warp)
     const int nw = blockDim.x >> 5;
+    // (each cache is stored with its penalty: a refresh reuses the penalty
+    // of every line whose cache stayed valid)
     for (int i = threadIdx.x >> 5; i < m; i += nw) {
         const int32_t* row = I.cost + (size_t)i * I.ldc;
         uint64_t a1 = kNoKey, a2 = kNoKey;
         for (int j = threadIdx.x & 31; j < n; j += 32) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
         warp_top2(a1, a2);
-        if ((threadIdx.x & 31) == 0) c.top2[i] = top2_from_keys(a1, a2);
+        if ((threadIdx.x & 31) == 0) {
+            const int4 t = top2_from_keys(a1, a2);
+            c.top2[i] = t;
+            c.diff[i] = vogel_penalty(t);
+        }
     }
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
         uint64_t a1 = kNoKey, a2 = kNoKey;
         for (int i = 0; i < m; i++) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
-        c.top2[m + j] = top2_from_keys(a1, a2);
+        const int4 t = top2_from_keys(a1, a2);
+        c.top2[m + j] = t;
+        c.diff[m + j] = vogel_penalty(t);
     }
     if (threadIdx.x == 0) {
         bs.i[0] = 1; bs.i[1] = 1;   // refresh rows / columns in the next step
@@ -252,6 +259,9 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
             bs.i[0] = 0;
             bs.i[1] = 0;
             const int4 t = c.top2[L];
+            // a rebuilt cache keeps its penalty with it; the stored penalty
+            // only matters at the next refresh of L's half (stale until then)
+            if (stale) c.diff[L] = vogel_penalty(t);
             const bool found = t.z >= 0;
             const int cross = found ? t.z : bs.i[4];
             if (!found) bs.i[5]++;
