@@ -83,6 +83,7 @@ __device__ __forceinline__ void sweep_part(const Ctx& c, int tile, int ntile, co
     const int nseg = (jn + kSegCols - 1) / kSegCols;
     const int nrows = rows ? min(max(c.sc->pp_n, 0), kPPRows) : m;
     const long long units = (long long)nrows * nseg, stride = (long long)nrg * wpb;
+    if ((long long)rg * wpb >= units) return;      // no unit for this block (a candidate sweep uses few blocks)
     if (!c.sc->narrow) {
         for (long long u = (long long)rg * wpb + warp; u < units; u += stride) {
             const int i = rows ? rows[u / nseg] : (int)(u / nseg), s = (int)(u % nseg);
