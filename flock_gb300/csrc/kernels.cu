@@ -18,8 +18,10 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -900,24 +902,84 @@ static bool copy_costs_checked(int32_t* dst, const int32_t* src, int n) {
     return !bad;
 }
 
-// Run f(0..count-1) on up to hardware_concurrency() threads (dynamic chunks).
+// Host worker pool behind parallel_for.  The workers start once (first use)
+// and sleep on a condition variable between jobs, so a batch call's
+// validation, packing and result collection start no threads.  One job at a
+// time: a caller that finds the pool busy with another host thread's job runs
+// its loop alone.  A job is a body that every participant runs (the body
+// hands out the work itself); the caller runs it too, then closes the job
+// (no worker joins after that) and waits for the workers that joined.
+class HostPool {
+public:
+    static HostPool& get() {
+        static HostPool* p = new HostPool();     // never destroyed: its workers sleep until the process exits
+        return *p;
+    }
+    int size() const { return nworkers_ + 1; }
+    // Runs body on the caller and up to want - 1 workers; false (nothing run)
+    // when another job holds the pool.
+    bool try_run(int want, const std::function<void()>& body) {
+        std::unique_lock<std::mutex> job(job_mu_, std::try_to_lock);
+        if (!job.owns_lock()) return false;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            body_ = &body;
+            slots_ = std::min(want - 1, nworkers_);
+            gen_++;
+        }
+        cv_.notify_all();
+        body();
+        std::unique_lock<std::mutex> lk(mu_);
+        slots_ = 0;
+        done_cv_.wait(lk, [&] { return joined_ == 0; });
+        body_ = nullptr;
+        return true;
+    }
+
+private:
+    HostPool() {
+        const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+        nworkers_ = std::min(hw, 32) - 1;
+        for (int t = 0; t < nworkers_; t++) std::thread([this] { loop(); }).detach();
+    }
+    void loop() {
+        uint64_t seen = 0;
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [&] { return gen_ != seen; });
+            seen = gen_;
+            if (slots_ <= 0) continue;
+            slots_--;
+            joined_++;
+            const std::function<void()>* b = body_;
+            lk.unlock();
+            (*b)();
+            lk.lock();
+            if (--joined_ == 0) done_cv_.notify_all();
+        }
+    }
+    std::mutex job_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void()>* body_ = nullptr;
+    uint64_t gen_ = 0;
+    int slots_ = 0, joined_ = 0, nworkers_ = 0;
+};
+
+// Run f(0..count-1) on up to 32 host threads of the pool (dynamic chunks of 8).
 template <class F>
 static void parallel_for(int count, const F& f) {
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int nt = std::min(std::min(hw, 32), std::max(1, count / 16));
+    HostPool& pool = HostPool::get();
+    const int nt = std::min(pool.size(), std::max(1, count / 16));
     if (nt <= 1) { for (int k = 0; k < count; k++) f(k); return; }
     std::atomic<int> next{0};
-    auto body = [&] {
+    const std::function<void()> body = [&] {
         for (;;) {
             const int k0 = next.fetch_add(8);
             if (k0 >= count) return;
             for (int k = k0; k < std::min(count, k0 + 8); k++) f(k);
         }
     };
-    std::vector<std::thread> th;
-    for (int t = 1; t < nt; t++) th.emplace_back(body);
-    body();
-    for (auto& t : th) t.join();
+    if (!pool.try_run(nt, body)) body();
 }
 
 int validate_instance(const flock_instance* I) {
