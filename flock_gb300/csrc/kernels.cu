@@ -2149,6 +2149,14 @@ int flock_test_select_rows(int32_t m, const uint64_t* keys, uint64_t* keys_out, 
     return flock::test_select_rows(m, keys, keys_out, prow, pn, pp_rows, best, threads);
 }
 
+/* Test hook (host only, no CUDA call): the batch call's parallel loop over
+ * count items, each adding 1 to hits[item]. */
+int flock_test_parallel_for(int32_t count, int32_t* hits) {
+    if (count < 0 || (count > 0 && !hits)) return FLOCK_ERR_ARG;
+    flock::parallel_for(count, [&](int k) { hits[k]++; });
+    return FLOCK_OK;
+}
+
 /* Test hook: one reduced-cost sweep over host costs and duals, row keys back. */
 int flock_test_sweep(int32_t m, int32_t n, const int32_t* cost, const int64_t* pot, uint64_t* keys,
                      int32_t cta_form, int32_t threads) {

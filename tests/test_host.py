@@ -221,3 +221,32 @@ def test_binary_instance_round_trip(tmp_path):
     with pytest.raises(fg.FlockError) as ex:
         fg.read_bin(p)
     assert ex.value.status == fg.FLOCK_ERR_PARSE
+
+
+def test_parallel_loop_concurrent_callers(flock_lib):
+    """The batch call's host parallel loop (a worker pool started once): every
+    item runs exactly once, also with several host threads calling at once
+    (a caller that finds the pool busy runs its loop alone)."""
+    import threading
+    f = flock_lib.flock_test_parallel_for
+    f.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+    f.restype = ctypes.c_int
+    assert f(-1, None) == fg.FLOCK_ERR_ARG
+    assert f(0, None) == fg.FLOCK_OK
+    errors = []
+
+    def caller(seed):
+        rng = np.random.default_rng(seed)
+        for _ in range(150):
+            n = int(rng.integers(1, 6000))
+            hits = np.zeros(n, dtype=np.int32)
+            rc = f(n, hits.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+            if rc != fg.FLOCK_OK or not (hits == 1).all():
+                errors.append((seed, n, rc))
+
+    threads = [threading.Thread(target=caller, args=(s,)) for s in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:3]
