@@ -37,7 +37,7 @@ def _worker(rank, world, port, out):
 def test_two_ranks_gloo():
     world = 2
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()      # no fork: the test process may run host worker threads
     out = mgr.dict()
     mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
     assert out[0][0] == out[1][0] == 1.0          # max over ranks
