@@ -53,6 +53,8 @@ def orc() -> ctypes.CDLL:
         L = ctypes.CDLL(ORC)
         L.orc_vogel.argtypes = [i32, i32, P(i32), P(i32), P(ctypes.c_float), P(i32), P(i32), P(ctypes.c_float)]
         L.orc_nwc.argtypes = [i32, i32, P(i32), P(i32), P(i32), P(i32), P(ctypes.c_float)]
+        L.orc_vogel_device.argtypes = [i32, i32, P(i32), P(i32), P(ctypes.c_float), P(i32), P(i32),
+                                       P(ctypes.c_float)]
         L.orc_solve_ref.argtypes = [i32, i32, P(i32), P(i32), P(ctypes.c_float), i32, i32,
                                     P(i32), P(i32), P(ctypes.c_float), P(i32), P(i32), P(OrcResult)]
         L.orc_solve_ref_batch.argtypes = [i32, P(i32), P(i32), P(i64), P(i64), P(i64), P(i32), P(i32),
@@ -101,6 +103,20 @@ def vogel(s, d, c):
     q = np.zeros(m + n - 1, np.float32)
     ev = orc().orc_vogel(m, n, _p(s), _p(d), _p(cf, ctypes.c_float), _p(src), _p(dst), _p(q, ctypes.c_float))
     return src, dst, q, int(ev)
+
+
+def vogel_device(s, d, c):
+    """The reference's device Vogel ("vam_device", float costs).  Returns
+    (src, dst, qty float32, rc); rc -1: undefined in the reference from the
+    first (-1, -1) flow on."""
+    s, d, cf = _prep(s, d, c)
+    m, n = len(s), len(d)
+    src = np.zeros(m + n - 1, np.int32)
+    dst = np.zeros(m + n - 1, np.int32)
+    q = np.zeros(m + n - 1, np.float32)
+    rc = orc().orc_vogel_device(m, n, _p(s), _p(d), _p(cf, ctypes.c_float), _p(src), _p(dst),
+                                _p(q, ctypes.c_float))
+    return src, dst, q, int(rc)
 
 
 def nwc(s, d):

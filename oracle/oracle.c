@@ -146,6 +146,117 @@ int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
     return events;
 }
 
+/* ---------------------------------------------------------------------- */
+/* IBFS_vogel.cu:3-543, find_vogel_bfs_parallel ("vam_device").
+ *
+ * Books (IBFS_vogel.cu:126-350): each row lists its n cells plus two
+ * sentinels (index n and n+1, cost 32767), stably sorted by float cost, so
+ * equal costs keep index order; then the entry at position n+1 gets cost - 1
+ * (override_row_sorts).  Columns likewise over m rows.
+ * Line state (parallel_structs.h:184-187): positions il1, il2 into the book
+ * (initially 0 and 1), the entry's index and the float regret diff.
+ * A step (IBFS_vogel.cu:417-537): refresh the lines of the kind that was not
+ * eliminated last (both kinds at the first step, rows first), pick the FIRST
+ * largest diff over [rows, columns] (thrust::max_element), allocate, and
+ * reset the eliminated line to {idx -1, il1 = other-kind count, il2 = +1,
+ * diff -1}.  A refresh (computeDifferences, :3-122) only moves positions whose
+ * entry is the eliminated line: il2 advances while it is below the last real
+ * position and the line at the new position is covered (its il1 >= the
+ * count of the refreshing kind).  */
+typedef struct { int32_t idx; float cost; } orc_book_cell;
+typedef struct { int32_t idx, il1, il2; float diff; } orc_vdiff;
+
+static int cmp_book(const void* a, const void* b) {
+    const orc_book_cell *x = (const orc_book_cell*)a, *y = (const orc_book_cell*)b;
+    if (x->cost < y->cost) return -1;
+    if (y->cost < x->cost) return 1;
+    return (x->idx > y->idx) - (x->idx < y->idx);   /* stable: original (index) order */
+}
+
+/* One line's book: len real entries, two sentinels, sorted, last decremented. */
+static void build_book(orc_book_cell* b, int len, const float* cost, size_t stride) {
+    for (int k = 0; k < len; k++) { b[k].idx = k; b[k].cost = cost[(size_t)k * stride]; }
+    b[len].idx = len; b[len].cost = 1.0f * 32767;
+    b[len + 1].idx = len + 1; b[len + 1].cost = 1.0f * 32767;
+    qsort(b, (size_t)len + 2, sizeof(orc_book_cell), cmp_book);
+    b[len + 1].cost -= 1;
+}
+
+/* Refresh one line (computeDifferences).  book: the line's book (len real
+ * entries), other: the state of the other kind's lines (count len), covered
+ * when other[x].il1 >= own_count.  Returns -1 if an index leaves the arrays. */
+static int vdiff_refresh(orc_vdiff* e, const orc_book_cell* book, int len, const orc_vdiff* other,
+                         int own_count, int reject) {
+    orc_book_cell l1 = book[e->il1], l2 = book[e->il2];
+    if (l1.idx == reject || l2.idx == reject) {
+        if (l1.idx == reject) { e->il1 = e->il2; l1 = l2; }
+        while (e->il2 < len - 1) {
+            e->il2 += 1;
+            const int x = book[e->il2].idx;
+            if (x < 0 || x >= len) return -1;
+            if (other[x].il1 < own_count) break;
+        }
+        l2 = book[e->il2];
+    }
+    e->diff = l2.cost - l1.cost;
+    e->idx = l1.idx;
+    return 0;
+}
+
+int orc_vogel_device(int m, int n, const int32_t* s, const int32_t* d, const float* c,
+                     int32_t* src, int32_t* dst, float* qty) {
+    const int V = m + n;
+    orc_book_cell* rb = (orc_book_cell*)malloc(sizeof(orc_book_cell) * (size_t)m * (n + 2));
+    orc_book_cell* cb = (orc_book_cell*)malloc(sizeof(orc_book_cell) * (size_t)n * (m + 2));
+    orc_vdiff* v = (orc_vdiff*)malloc(sizeof(orc_vdiff) * (size_t)V);
+    int32_t* rs = (int32_t*)malloc(sizeof(int32_t) * (size_t)m);
+    int32_t* rd = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    for (int i = 0; i < m; i++) build_book(rb + (size_t)i * (n + 2), n, c + (size_t)i * n, 1);
+    for (int j = 0; j < n; j++) build_book(cb + (size_t)j * (m + 2), m, c + j, (size_t)n);
+    for (int x = 0; x < V; x++) { v[x].idx = 0; v[x].il1 = 0; v[x].il2 = 1; v[x].diff = 0.0f; }
+    memcpy(rs, s, sizeof(int32_t) * (size_t)m);
+    memcpy(rd, d, sizeof(int32_t) * (size_t)n);
+    int prev = -1, rc = 0, counter = 0;
+    for (; counter < V - 1; counter++) {
+        /* refresh: rows after a column (or at the start), columns after a row */
+        for (int pass = 0; pass < (counter == 0 ? 2 : 1); pass++) {
+            const int p = counter == 0 ? (pass == 0 ? V : -1) : prev;
+            if (p >= m) {
+                for (int i = 0; i < m && !rc; i++)
+                    rc = vdiff_refresh(&v[i], rb + (size_t)i * (n + 2), n, v + m, m, p - m);
+            } else {
+                for (int j = 0; j < n && !rc; j++)
+                    rc = vdiff_refresh(&v[m + j], cb + (size_t)j * (m + 2), m, v, n, p);
+            }
+        }
+        if (rc) break;
+        int best = 0;                                  /* first maximum */
+        for (int x = 1; x < V; x++) if (v[best].diff < v[x].diff) best = x;
+        int row, col;
+        if (best >= m) { col = best - m; row = v[best].idx; }
+        else { row = best; col = v[best].idx; }
+        if (row < 0 || row >= m || col < 0 || col >= n) { rc = -1; break; }
+        src[counter] = row;
+        dst[counter] = col;
+        if (rd[col] > rs[row]) {
+            qty[counter] = fmaxf(1.0f * rs[row], ORC_EPSILON);
+            rd[col] -= rs[row];
+            rs[row] = 0;
+            prev = row;
+            v[row].idx = -1; v[row].il1 = n; v[row].il2 = n + 1; v[row].diff = -1.0f;
+        } else {
+            qty[counter] = fmaxf(1.0f * rd[col], ORC_EPSILON);
+            rs[row] -= rd[col];
+            rd[col] = 0;
+            prev = m + col;
+            v[m + col].idx = -1; v[m + col].il1 = m; v[m + col].il2 = m + 1; v[m + col].diff = -1.0f;
+        }
+    }
+    if (rc) fill_undefined(src, dst, qty, counter, V - 1);
+    free(rb); free(cb); free(v); free(rs); free(rd);
+    return rc;
+}
+
 /* IBFS_nwc.cu:3-33 (reads one element past the end only after the last
  * allocation; the restatement stops first). */
 int orc_nwc(int m, int n, const int32_t* s, const int32_t* d,
@@ -234,6 +345,7 @@ int orc_solve_ref(int m, int n, const int32_t* s, const int32_t* d, const float*
     float* q0 = (float*)malloc(sizeof(float) * (size_t)V);
     int ev = 0;
     if (bfs_method == 0) orc_nwc(m, n, s, d, slot_row, slot_col, q0);
+    else if (bfs_method == 2) ev = orc_vogel_device(m, n, s, d, c, slot_row, slot_col, q0);
     else ev = orc_vogel(m, n, s, d, c, slot_row, slot_col, q0);
     if (ev < 0) {
         /* The reference's run is undefined from here on (out-of-range index). */

@@ -9,7 +9,8 @@
  *
  * Parity is pinned: tests/test_oracle_pin.py checks this restatement against
  * the published run logs (results/pure_sequencial: iterations + objective for
- * every data file present) and, where the reference sources are available,
+ * every data file present; results/parallel_uv the same with the device Vogel
+ * restatement as the BFS) and, where the reference sources are available,
  * against the reference's own functions compiled into oracle/_ref.
  */
 #ifndef FLOCK_ORACLE_H
@@ -32,6 +33,16 @@ extern "C" {
 int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
               int32_t* src, int32_t* dst, float* qty);
 
+/* Vogel's approximation as the reference's device variant
+ * find_vogel_bfs_parallel ("vam_device", IBFS_vogel.cu:3-543): regrets from
+ * positions into per-line cost-sorted books, first largest regret, its own
+ * tie rules (a different BFS from orc_vogel).  Writes m+n-1 flows in
+ * allocation order.  Returns 0, or -1 when the reference would index past
+ * its arrays (costs at or above the books' 32767 sentinels, a one-column
+ * line run dry); the flows from that step on are written as (-1, -1, 0). */
+int orc_vogel_device(int m, int n, const int32_t* s, const int32_t* d, const float* c,
+                     int32_t* src, int32_t* dst, float* qty);
+
 /* North-west corner rule (src/parallel_simplex_method/IBFS_nwc.cu:3-33). */
 int orc_nwc(int m, int n, const int32_t* s, const int32_t* d,
             int32_t* src, int32_t* dst, float* qty);
@@ -46,7 +57,7 @@ typedef struct {
     double objective;       /* sum of float(qty*cost) in double, as the reference */
 } orc_result;
 
-/* The reference CPU path: BFS (1 = vam_host, 0 = nwc_host), then loop
+/* The reference CPU path: BFS (1 = vam_host, 0 = nwc_host, 2 = vam_device), then loop
  * { duals by BFS from row 0; row-major strict-< scan; pivot } until
  * min r >= 0 or |min r| <= 0.01 or max_iter.  Outputs the active flows
  * (slot order) and, if tree_src/tree_dst are given, the m+n-1 final basis

@@ -13,8 +13,10 @@ Outputs (committed):
                            tiny degenerate instances (regenerated by seed)
   reference_synthetic.json the reference's results on generator instances
                            (regenerated by the product's generator; checksum)
-  published.json           iterations/objectives of the published CPU-path
-                           and Gurobi logs (results/pure_sequencial, gurobi)
+  published.json           iterations/objectives of the published CPU-path,
+                           GPU uv-path and Gurobi logs (results/pure_sequencial,
+                           parallel_uv, gurobi); `--published-only` rewrites
+                           just this file
 """
 import ctypes
 import json
@@ -78,6 +80,28 @@ def ref_outputs(s, d, cf):
             "active": r["active"]}
 
 
+def write_published(refdir):
+    """Iterations and objectives of the published run logs: the CPU path
+    (vam_host BFS), the GPU uv path (vam_device BFS, host duals, sequential
+    cycle search) and Gurobi."""
+    pub = {"pure_sequencial": {}, "parallel_uv": {}, "gurobi": {}}
+    for key in pub:
+        lines = open(os.path.join(refdir, "results", key)).read().splitlines()
+        fname = None
+        for ln in lines:
+            mm = re.search(r"File Name = \S*/(\S+\.dat)", ln)
+            if mm:
+                fname = mm.group(1)
+            mm = re.search(r"BASIC STATISTICS \| Objective: (\S+) \| Iterations: (\d+) \| Time: (\d+)", ln)
+            if mm and fname:
+                pub[key][fname] = {"objective": mm.group(1), "iterations": int(mm.group(2)),
+                                   "time_ms": int(mm.group(3))}
+            mm = re.search(r"Optimal objective\s+(\S+)", ln)
+            if mm and fname and key == "gurobi":
+                pub[key].setdefault(fname, {})["optimal"] = mm.group(1)
+    json.dump(pub, open(os.path.join(HERE, "published.json"), "w"), indent=1)
+
+
 def main(refdir):
     assert oracle.ref_available(), "build oracle/_ref first (make -C oracle ref)"
     # 1. the reference's own test fixtures
@@ -112,24 +136,14 @@ def main(refdir):
         syn.append(e)
     json.dump(syn, open(os.path.join(HERE, "reference_synthetic.json"), "w"), separators=(",", ":"))
     # 4. published logs
-    pub = {"pure_sequencial": {}, "gurobi": {}}
-    for key in pub:
-        lines = open(os.path.join(refdir, "results", key)).read().splitlines()
-        fname = None
-        for ln in lines:
-            mm = re.search(r"File Name = \S*/(\S+\.dat)", ln)
-            if mm:
-                fname = mm.group(1)
-            mm = re.search(r"BASIC STATISTICS \| Objective: (\S+) \| Iterations: (\d+) \| Time: (\d+)", ln)
-            if mm and fname:
-                pub[key][fname] = {"objective": mm.group(1), "iterations": int(mm.group(2)),
-                                   "time_ms": int(mm.group(3))}
-            mm = re.search(r"Optimal objective\s+(\S+)", ln)
-            if mm and fname and key == "gurobi":
-                pub[key].setdefault(fname, {})["optimal"] = mm.group(1)
-    json.dump(pub, open(os.path.join(HERE, "published.json"), "w"), indent=1)
+    write_published(refdir)
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if a != "--published-only"]
+    ref = args[0] if args else "/root/reference"
+    if "--published-only" in sys.argv:
+        write_published(ref)       # the run logs only (no reference build needed)
+    else:
+        main(ref)

@@ -72,11 +72,11 @@ def test_known_optima(orc):
             assert r["status"] == 0 and r["objective"] == known[e["file"]]
 
 
-def _published_data_files():
+def _published_data_files(key="pure_sequencial"):
     d = os.path.join(REFERENCE, "data")
     if not os.path.isdir(d):
         return []
-    pub = load("published.json")["pure_sequencial"]
+    pub = load("published.json")[key]
     out = []
     for f, v in sorted(pub.items()):
         p = os.path.join(d, f)
@@ -94,6 +94,21 @@ def test_published_cpu_path(orc, path, pub):
     d = np.array(tok[2 + m:2 + m + n], np.int32)
     c = np.array([float(x) for x in tok[2 + m + n:]], np.float32)
     r = oracle.solve_ref(s, d, c)
+    assert r["iterations"] == pub["iterations"]
+    assert "%g" % r["objective"] == pub["objective"]
+
+
+@pytest.mark.parametrize("path,pub", _published_data_files("parallel_uv"), ids=lambda x: os.path.basename(str(x)))
+def test_published_device_vogel_path(orc, path, pub):
+    """Iterations and objective of results/parallel_uv (BFS vam_device, host
+    duals, sequential cycle search, first-minimum sweep), reproduced by the
+    restatement of the reference's device Vogel feeding the CPU path."""
+    tok = open(path).read().split()
+    m, n = int(tok[0]), int(tok[1])
+    s = np.array(tok[2:2 + m], np.int32)
+    d = np.array(tok[2 + m:2 + m + n], np.int32)
+    c = np.array([float(x) for x in tok[2 + m + n:]], np.float32)
+    r = oracle.solve_ref(s, d, c, bfs=2)
     assert r["iterations"] == pub["iterations"]
     assert "%g" % r["objective"] == pub["objective"]
 
