@@ -59,7 +59,7 @@ FLOCK_OK, FLOCK_ERR_ARG, FLOCK_ERR_UNBALANCED, FLOCK_ERR_FILE, FLOCK_ERR_PARSE, 
 ST_ITER_CAP, ST_TREE_CORRUPT, ST_SF_FAIL, ST_CERT_FAIL, ST_RANGE = 1, 2, 4, 32, 64
 NOTE_VOGEL_UNDEF, NOTE_START_REPAIRED = 8, 16
 
-BFS = {"nwc": 0, "nwc_host": 0, "vogel": 1, "vam_host": 1}
+BFS = {"nwc": 0, "nwc_host": 0, "vogel": 1, "vam_host": 1, "vogel_device": 2, "vam_device": 2}
 PIVOT = {"sequential": 0, "parallel_uv": 0, "parallel": 1, "parallel_ss": 1, "switch": 2, "switch_hybrid": 2}
 
 
@@ -302,6 +302,20 @@ def vogel(inst: Instance) -> Tuple[np.ndarray, int]:
     flows = np.zeros((V - 1, 3), np.int32)
     ev = i32()
     rc = lib().flock_vogel(ctypes.byref(ci), flows.ctypes.data_as(P(CFlow)), ctypes.byref(ev))
+    if rc:
+        raise _err(rc)
+    return flows, int(ev.value)
+
+
+def vogel_device(inst: Instance) -> Tuple[np.ndarray, int]:
+    """Vogel with the reference's device semantics ("vam_device") on the GPU:
+    (m+n-1, 3) allocations in order, events (-1: undefined in the reference
+    from the first (-1, -1, 0) allocation on)."""
+    ci = inst.c()
+    V = inst.m + inst.n
+    flows = np.zeros((V - 1, 3), np.int32)
+    ev = i32()
+    rc = lib().flock_vogel_device(ctypes.byref(ci), flows.ctypes.data_as(P(CFlow)), ctypes.byref(ev))
     if rc:
         raise _err(rc)
     return flows, int(ev.value)

@@ -144,6 +144,10 @@ template <class T, class U> inline T atomicMin(T* p, U vv) {
     return cur;
 }
 inline float __ll2float_rn(long long x) { return (float)x; }
+inline unsigned __float_as_uint(float f) { unsigned u; memcpy(&u, &f, 4); return u; }
+inline float __uint_as_float(unsigned u) { float f; memcpy(&f, &u, 4); return f; }
+inline int __float_as_int(float f) { int u; memcpy(&u, &f, 4); return u; }
+inline float __int_as_float(int u) { float f; memcpy(&f, &u, 4); return f; }
 inline int __float2int_rz(float f) { return (int)f; }
 template <class T> inline T __ldcs(const T* p) { return *p; }
 using std::min;

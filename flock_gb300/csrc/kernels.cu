@@ -34,10 +34,12 @@
 namespace flock {
 
 // ------------------------------------------------------------ kernels ------
-__global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method) {
+__global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const int2* rbook, const int2* cbook) {
     __shared__ BlockScratch bs;
     if (bfs_method == FLOCK_BFS_VOGEL) {
         vogel_cta(c, bs);
+    } else if (bfs_method == FLOCK_BFS_VOGEL_DEVICE) {
+        vogel_books_cta(c, rbook, cbook, bs);
     } else {
         if (threadIdx.x == 0) { nwc_thread0(c); c.sc->events = 0; }
         __syncthreads();
@@ -51,6 +53,22 @@ __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method) {
 __global__ void __launch_bounds__(1024, 1) k_vogel_only(Ctx c) {
     __shared__ BlockScratch bs;
     vogel_cta(c, bs);
+}
+
+// "vam_device" Vogel: the books (one block per line: rows, then columns),
+// then the step loop on one CTA.
+constexpr int kBookThreads = 256;
+constexpr int kBookLineMax = 16382;     // a line's book (+ 2 sentinels) sorts in 128 KB of shared memory
+__global__ void __launch_bounds__(kBookThreads) k_books(InstDev I, int2* rbook, int2* cbook, int P) {
+    extern __shared__ uint64_t book_keys[];
+    const int line = blockIdx.x;
+    int2* out = line < I.m ? rbook + (size_t)line * (I.n + 2) : cbook + (size_t)(line - I.m) * (I.m + 2);
+    book_line_cta(I, line, book_keys, P, out);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_vogel_books_only(Ctx c, const int2* rbook, const int2* cbook) {
+    __shared__ BlockScratch bs;
+    vogel_books_cta(c, rbook, cbook, bs);
 }
 
 // Grid-wide sweep.  blockIdx.x = tile + ntile * row_group.  The block stages
@@ -1004,6 +1022,7 @@ static int threads_for(int V) {
 struct PlainSolver {
     std::mutex mu;
     DevBuf ws, cost, sd;
+    DevBuf books;                   // "vam_device" Vogel: row and column books
     GridPivot* gp = nullptr;        // grid pivot round state (large instances)
     HostBuf h_sc;
     cudaStream_t stream = nullptr;
@@ -1015,7 +1034,27 @@ struct PlainSolver {
         FLOCK_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         for (auto& e : ev) FLOCK_CK(cudaEventCreate(&e));
         FLOCK_CK(h_sc.ensure(sizeof(Scalars)));
+        FLOCK_CK(cudaFuncSetAttribute(k_books, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(uint64_t) * 16384)));
         init = true;
+        return FLOCK_OK;
+    }
+
+    // Sort the "vam_device" Vogel's books of the prepared instance on the
+    // stream (rows' books first, then the columns').
+    int build_books(const Ctx& c, int2** rb, int2** cb) {
+        const int m = c.I.m, n = c.I.n;
+        if (m > kBookLineMax || n > kBookLineMax) {
+            set_error("vam_device Vogel: a line longer than 16382 cells");
+            return FLOCK_ERR_RANGE;
+        }
+        FLOCK_CK(books.ensure(book_entries(m, n) * sizeof(int2)));
+        *rb = books.as<int2>();
+        *cb = *rb + (size_t)m * (n + 2);
+        int P = 1;
+        while (P < std::max(m, n) + 2) P <<= 1;
+        k_books<<<m + n, kBookThreads, sizeof(uint64_t) * P, stream>>>(c.I, *rb, *cb, P);
+        FLOCK_CK(cudaGetLastError());
         return FLOCK_OK;
     }
 
@@ -1095,8 +1134,12 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     const bool partial = opt.pricing == FLOCK_PRICING_PARTIAL && V >= kGridPivotV;
     if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds, partial))) return rc;
     const int nt = threads_for(V);
+    const int bfs = opt.bfs_method == FLOCK_BFS_NWC || opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE ? opt.bfs_method
+                                                                                                  : FLOCK_BFS_VOGEL;
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
-    k_setup<<<1, nt, 0, P.stream>>>(c, opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL);
+    int2 *rbook = nullptr, *cbook = nullptr;
+    if (bfs == FLOCK_BFS_VOGEL_DEVICE && (rc = P.build_books(c, &rbook, &cbook))) return rc;
+    k_setup<<<1, nt, 0, P.stream>>>(c, bfs, rbook, cbook);
     FLOCK_CK(cudaGetLastError());
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     int grid = 0, tile = 0, ntile = 0;
@@ -1205,7 +1248,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     return status ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
 }
 
-static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* events) {
+static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* events, bool books = false) {
     int rc = validate_instance(I);
     if (rc) return rc;
     PlainSolver& P = plain();
@@ -1216,7 +1259,13 @@ static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* even
     int32_t* out3 = nullptr;
     if ((rc = P.prepare(I, c, &out3))) return rc;
     if ((rc = P.reset_scalars(c.sc, 1, 1))) return rc;
-    k_vogel_only<<<1, threads_for(V), 0, P.stream>>>(c);
+    if (books) {
+        int2 *rbook = nullptr, *cbook = nullptr;
+        if ((rc = P.build_books(c, &rbook, &cbook))) return rc;
+        k_vogel_books_only<<<1, threads_for(V), 0, P.stream>>>(c, rbook, cbook);
+    } else {
+        k_vogel_only<<<1, threads_for(V), 0, P.stream>>>(c);
+    }
     FLOCK_CK(cudaGetLastError());
     std::vector<int32_t> a((size_t)V), b((size_t)V), q((size_t)V);
     FLOCK_CK(cudaMemcpyAsync(a.data(), c.bfs_src, (size_t)(V - 1) * 4, cudaMemcpyDeviceToHost, P.stream));
@@ -1458,6 +1507,10 @@ struct BatchRunner {
         if (rc) return rc;
         flock_default_options(&opt);
         if (opt_in) opt = *opt_in;
+        if (opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE) {
+            set_error("vam_device Vogel runs on flock_solve and flock_vogel_device only");
+            return FLOCK_ERR_ARG;
+        }
         insts = in;
         count = cnt;
         V_of.assign(cnt, 0); m_of.assign(cnt, 0); n_of.assign(cnt, 0);
@@ -2116,6 +2169,11 @@ const char* flock_version(void) { return "flock-gb300 0.1 (sm_103a)"; }
 int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events) {
     if (!flows) return FLOCK_ERR_ARG;
     return flock::vogel_plain(inst, flows, events);
+}
+
+int flock_vogel_device(const flock_instance* inst, flock_flow* flows, int32_t* events) {
+    if (!flows) return FLOCK_ERR_ARG;
+    return flock::vogel_plain(inst, flows, events, true);
 }
 
 int flock_solve(const flock_instance* inst, const flock_options* opt, flock_flow* flows,

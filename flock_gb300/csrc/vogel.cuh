@@ -312,4 +312,153 @@ __device__ void nwc_thread0(const Ctx& c) {
     for (; cnt < I.m + I.n - 1; cnt++) { c.bfs_src[cnt] = -1; c.bfs_dst[cnt] = -1; c.bfs_qty[cnt] = 0; }
 }
 
+// ---------------------------------------------------------------------------
+// Vogel as the reference's device variant find_vogel_bfs_parallel
+// (IBFS_vogel.cu:3-543, BFS_METHOD "vam_device"): regrets from positions into
+// per-line cost-sorted books; a different BFS from vogel_cta (other tie rules:
+// the first largest regret, no stale penalties).
+
+// Ascending floats -> ascending unsigned keys (no -0.0 arises from int costs).
+__device__ __forceinline__ uint32_t float_order_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_from_order_bits(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Book entries per line of the other kind's count plus the two sentinels.
+__host__ __device__ __forceinline__ size_t book_entries(int m, int n) {
+    return (size_t)m * (n + 2) + (size_t)n * (m + 2);
+}
+
+// The book of one line (IBFS_vogel.cu:126-350): its len cells and two
+// sentinels (index len and len + 1, cost 32767.0f) ordered by (float cost,
+// index) -- the order the reference's two stable sorts give, equal costs in
+// index order -- then the entry at position len + 1 lowered by 1.0f
+// (override_row_sorts / override_col_sorts).  line < m: row `line`, else
+// column line - m.  sk: P >= len + 2 shared keys (P a power of two); out:
+// len + 2 entries (index, float bits of the cost).
+__device__ void book_line_cta(const InstDev& I, int line, uint64_t* sk, int P, int2* out) {
+    const int m = I.m;
+    const bool row = line < m;
+    const int len = row ? I.n : m;
+    for (int k = threadIdx.x; k < P; k += blockDim.x) {
+        uint64_t key = kNoKey;
+        if (k < len + 2) {
+            const float cf = k < len ? (float)(row ? cost_of(I, line, k) : cost_of(I, k, line - m)) : 32767.0f;
+            key = ((uint64_t)float_order_bits(cf) << 32) | (uint32_t)k;
+        }
+        sk[k] = key;
+    }
+    __syncthreads();
+    // bitonic sort, ascending (keys are distinct: the index is in the low word)
+    for (int size = 2; size <= P; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < (P >> 1); t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1)), hi = lo + stride;
+                const uint64_t a = sk[lo], b = sk[hi];
+                if ((a > b) == ((lo & size) == 0)) { sk[lo] = b; sk[hi] = a; }
+            }
+            __syncthreads();
+        }
+    for (int k = threadIdx.x; k < len + 2; k += blockDim.x) {
+        const uint64_t key = sk[k];
+        float cf = float_from_order_bits((uint32_t)(key >> 32));
+        if (k == len + 1) cf = cf - 1.0f;
+        out[k] = make_int2((int)(uint32_t)key, __float_as_int(cf));
+    }
+    __syncthreads();
+}
+
+// The step loop (IBFS_vogel.cu:417-537) over books built by book_line_cta
+// (rbook: m rows of n + 2 entries, cbook: n columns of m + 2).  Line state in
+// c.top2 (position il1, position il2, entry index, float bits of the regret;
+// initially 0, 1, 0, 0.0f as the reference's vogelDifference defaults);
+// residuals in c.res.  A step refreshes the lines of the kind not eliminated
+// last (both at the first step, rows first: computeDifferences, :3-122),
+// takes the first largest regret over [rows, columns] (thrust::max_element),
+// allocates min(residuals) -- the column is eliminated on a tie -- and resets
+// the eliminated line to (count of the other kind, +1, -1, -1.0f).  Writes
+// m+n-1 allocations to c.bfs_*; c.sc->events = -1 where the reference would
+// index past its arrays (its flows from there on are written as (-1,-1,0)).
+__device__ void vogel_books_cta(const Ctx& c, const int2* rbook, const int2* cbook, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n, V = m + n;
+    int4* st = c.top2;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        st[v] = make_int4(0, 1, 0, 0);
+        c.res[v] = v < m ? I.supply[v] : I.demand[v - m];
+    }
+    // bs.i[0]: last eliminated line; bs.i[1]: stop (undefined), written by
+    // thread 0 only; bs.i[2]: a refresh left the book (read by thread 0)
+    if (threadIdx.x == 0) { bs.i[0] = -1; bs.i[1] = 0; bs.i[2] = 0; }
+    __syncthreads();
+    for (int counter = 0; counter < V - 1; counter++) {
+        const int prev = bs.i[0];
+        for (int pass = 0; pass < (counter == 0 ? 2 : 1); pass++) {
+            const int p = counter == 0 ? (pass == 0 ? V : -1) : prev;
+            const bool rows = p >= m;
+            const int lo = rows ? 0 : m, hi = rows ? m : V;
+            const int len = rows ? n : m;        // real entries of this kind's books
+            const int own = rows ? m : n;        // a line of the other kind is covered when its il1 >= own
+            const int obase = rows ? m : 0;      // first line of the other kind
+            const int reject = rows ? p - m : p;
+            int bad = 0;
+            for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
+                const int2* book = rows ? rbook + (size_t)v * (n + 2) : cbook + (size_t)(v - m) * (m + 2);
+                int4 e = st[v];
+                int2 l1 = book[e.x], l2 = book[e.y];
+                if (l1.x == reject || l2.x == reject) {
+                    if (l1.x == reject) { e.x = e.y; l1 = l2; }
+                    while (e.y < len - 1) {
+                        e.y++;
+                        const int x = book[e.y].x;
+                        if (x < 0 || x >= len) { bad = 1; break; }
+                        if (st[obase + x].x < own) break;
+                    }
+                    l2 = book[e.y];
+                }
+                e.z = l1.x;
+                e.w = __float_as_int(__int_as_float(l2.y) - __int_as_float(l1.y));
+                st[v] = e;
+            }
+            if (bad) bs.i[2] = 1;
+            __syncthreads();
+        }
+        // first largest regret: the smallest (inverted regret, line) key
+        uint64_t key = kNoKey;
+        for (int v = threadIdx.x; v < V; v += blockDim.x) {
+            const uint64_t k2 = ((uint64_t)(~float_order_bits(__int_as_float(st[v].w))) << 32) | (uint32_t)v;
+            key = k2 < key ? k2 : key;
+        }
+        key = block_min_u64(key, bs);
+        if (threadIdx.x == 0) {
+            const int L = (int)(uint32_t)key;
+            const int cross = st[L].z;
+            int row, col;
+            if (L >= m) { col = L - m; row = cross; } else { row = L; col = cross; }
+            if (bs.i[2] || row < 0 || row >= m || col < 0 || col >= n) {
+                bs.i[1] = 1;
+                for (int k = counter; k < V - 1; k++) { c.bfs_src[k] = -1; c.bfs_dst[k] = -1; c.bfs_qty[k] = 0; }
+            } else {
+                const int32_t rs = c.res[row], rd = c.res[m + col];
+                int32_t q;
+                if (rd > rs) {
+                    q = rs; c.res[m + col] = rd - rs; c.res[row] = 0; bs.i[0] = row;
+                    st[row] = make_int4(n, n + 1, -1, __float_as_int(-1.0f));
+                } else {
+                    q = rd; c.res[row] = rs - rd; c.res[m + col] = 0; bs.i[0] = m + col;
+                    st[m + col] = make_int4(m, m + 1, -1, __float_as_int(-1.0f));
+                }
+                c.bfs_src[counter] = row; c.bfs_dst[counter] = col; c.bfs_qty[counter] = q;
+            }
+        }
+        __syncthreads();
+        if (bs.i[1]) break;
+    }
+    if (threadIdx.x == 0) c.sc->events = bs.i[1] ? -1 : 0;
+    __syncthreads();
+}
+
 }  // namespace flock

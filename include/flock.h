@@ -18,6 +18,8 @@
  *                                        (ProblemInstance, src/structs.h:19-40)
  *   flock_vogel                       <- find_vogel_bfs_sequencial,
  *                                        src/parallel_simplex_method/IBFS_vogel.cu:546-769
+ *   flock_vogel_device                <- find_vogel_bfs_parallel,
+ *                                        src/parallel_simplex_method/IBFS_vogel.cu:3-543
  *   flock_solve                       <- uvModel_parallel / ssModel_parallel ctor + execute()
  *                                        + create_flows(), src/algos.h:1-4,
  *                                        parallel_uv_method/uv_model_parallel.cu:20-400,
@@ -65,7 +67,10 @@ typedef struct {
     int32_t source, destination, qty;
 } flock_flow;
 
-enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1 };            /* BFS_METHOD nwc_host / vam_host */
+/* BFS_METHOD nwc_host / vam_host / vam_device.  VOGEL_DEVICE: the reference's
+ * device Vogel semantics (flock_vogel_device); flock_solve only (batched and
+ * served forms return FLOCK_ERR_ARG), lines of at most 16382 cells. */
+enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1, FLOCK_BFS_VOGEL_DEVICE = 2 };
 /* -a parallel_uv / parallel_ss / switch_hybrid.  SWITCH runs parallel rounds
  * until one applies fewer than 10 pivots, then sequential ones
  * (switch/switch_model_parallel.cu:182-184). */
@@ -82,7 +87,7 @@ enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH 
 enum { FLOCK_PRICING_FULL = 0, FLOCK_PRICING_PARTIAL = 1 };
 
 typedef struct {
-    int32_t bfs_method;      /* FLOCK_BFS_VOGEL (default) or FLOCK_BFS_NWC */
+    int32_t bfs_method;      /* FLOCK_BFS_VOGEL (default), FLOCK_BFS_NWC or FLOCK_BFS_VOGEL_DEVICE */
     int32_t pivot_method;    /* FLOCK_PIVOT_SWITCH (default), _PARALLEL or _SEQUENTIAL */
     int32_t max_iterations;  /* cap on pricing rounds; <= 0: 1 << 30 */
     int32_t verify;          /* nonzero: run the exact certificate check (default on) */
@@ -142,6 +147,16 @@ int flock_read_bin(const char* path, int32_t m, int32_t n, int32_t* supply, int3
 /* Vogel's approximation on the GPU with the reference's exact semantics.
  * Writes m+n-1 allocations in allocation order.  *events as flock_stats. */
 int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events);
+
+/* Vogel's approximation with the semantics of the reference's device variant
+ * (find_vogel_bfs_parallel, BFS_METHOD "vam_device",
+ * src/parallel_simplex_method/IBFS_vogel.cu:3-543): regrets from positions
+ * into cost-sorted per-line books, the first largest regret; a different BFS
+ * from flock_vogel.  Writes m+n-1 allocations in allocation order.  *events:
+ * 0, or -1 where the reference indexes past its arrays (costs at or above its
+ * 32767 sentinels); its allocations from there on are written as (-1, -1, 0).
+ * FLOCK_ERR_RANGE for a line of more than 16382 cells. */
+int flock_vogel_device(const flock_instance* inst, flock_flow* flows, int32_t* events);
 
 /* No counterpart in the reference.  flock_vogel without any allocation:
  * the same kernel and identical results, but every device array of the call

@@ -4,7 +4,8 @@
 #pragma once
 #include "../flock.h"
 
-// BFS_METHOD: "vam_host" semantics (computed on the GPU) or "nwc_host".
+// BFS_METHOD: "vam_host" semantics (computed on the GPU), "nwc_host", or
+// FLOCK_BFS_VOGEL_DEVICE for "vam_device" semantics.
 #ifndef FLOCK_DEFAULT_BFS
 #define FLOCK_DEFAULT_BFS FLOCK_BFS_VOGEL
 #endif

@@ -56,3 +56,51 @@ def test_emulated_short_candidate_lists(emu):
     """Partial pricing with 8 candidate rows and a full sweep every 2 rounds:
     the first histogram bin often holds more rows than kept."""
     run(emu, [99, 6, 20, 70, 0, 5, 2, 1], {"EMU_THREADS": "64", "EMU_PP_ROWS": "8", "EMU_PP_REFRESH": "2"})
+
+
+@pytest.mark.parametrize("threads", [32, 96])
+def test_emulated_vogel_device(emu, tmp_path, threads):
+    """The "vam_device" Vogel's device functions (per-line book sort, step
+    loop) on the emulated CTA: allocations identical to the oracle's
+    restatement of the reference's device Vogel, ties and costs around the
+    32767 book sentinels included, no barrier divergence, no sanitizer
+    report."""
+    import numpy as np
+    import flock_gb300 as fg
+    import oracle
+    rng = np.random.default_rng(5 + threads)
+    files, insts = [], []
+    for k in range(40):
+        m, n = int(rng.integers(1, 40)), int(rng.integers(1, 40))
+        lo, hi = [(1, 3), (1, 10), (1, 1000), (32760, 32775)][k % 4]
+        c = rng.integers(lo, hi + 1, size=(m, n)).astype(np.int32)
+        s = rng.integers(0, 20, size=m).astype(np.int32)
+        d = rng.integers(0, 20, size=n).astype(np.int32)
+        diff = int(s.sum() - d.sum())
+        if diff > 0:
+            d[-1] += diff
+        else:
+            s[-1] -= diff
+        p = str(tmp_path / f"v{k}.fbin")
+        fg.write_bin(fg.Instance(s, d, c), p)
+        files.append(p)
+        insts.append((s, d, c))
+    exe = os.path.join(EMU_DIR, "emu_vogel_device")
+    r = subprocess.run([exe] + files, capture_output=True, text=True, env=dict(os.environ, EMU_THREADS=str(threads)),
+                       timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert not re.search(r"ERROR: AddressSanitizer|runtime error:", r.stderr), r.stderr[-2000:]
+    lines = r.stdout.splitlines()
+    assert len(lines) == len(insts)
+    undefined = 0
+    for (s, d, c), line in zip(insts, lines):
+        head, flows = line.split(" flows=")
+        assert "barrier_mismatch=0" in head
+        ev = int(re.search(r"events=(-?\d+)", head).group(1))
+        got = np.array([[int(x) for x in f.split(",")] for f in flows.strip(";").split(";")], np.int64)
+        src, dst, q, rc = oracle.vogel_device(s, d, c)
+        exp = np.stack([src, dst, np.where(q < 0.5, 0, q).astype(np.int64)], 1)
+        assert (ev < 0) == (rc < 0), head
+        np.testing.assert_array_equal(got, exp)
+        undefined += rc < 0
+    assert undefined > 0

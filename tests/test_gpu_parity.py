@@ -84,6 +84,74 @@ def test_vogel_euclid_shape():
     assert_vogel_parity(fg.config_instance("euclid8000", 5, m=200, n=300))
 
 
+def assert_vogel_device_parity(inst):
+    """The reference's device Vogel ("vam_device"): every allocation and the
+    undefined marker bit-identical to the oracle's restatement (both write
+    (-1, -1, 0) from the step where the reference indexes past its arrays)."""
+    gpu, ev = fg.vogel_device(inst)
+    src, dst, q, rc = oracle.vogel_device(inst.supply, inst.demand, inst.cost)
+    assert (ev < 0) == (rc < 0)
+    qi = np.where(q < 0.5, 0, q).astype(np.int64)     # the reference writes 1e-6 for zero
+    np.testing.assert_array_equal(gpu[:, 0], src)
+    np.testing.assert_array_equal(gpu[:, 1], dst)
+    np.testing.assert_array_equal(gpu[:, 2].astype(np.int64), qi)
+    return rc
+
+
+def test_vogel_device_tiny_degenerate():
+    for inst in tiny_instances(31, 400):
+        assert_vogel_device_parity(inst)
+
+
+@pytest.mark.parametrize("name,seed,m,n", [("uniform100", 0, None, None), ("uniform100", 1, None, None),
+                                           ("degenerate1000", 0, None, None), ("euclid8000", 5, 200, 300)])
+def test_vogel_device_shapes(name, seed, m, n):
+    assert assert_vogel_device_parity(fg.config_instance(name, seed, m=m, n=n)) == 0
+
+
+def test_vogel_device_sentinel_costs():
+    """Costs around the reference's 32767 book sentinels: defined runs agree,
+    and so does the step where the reference's run becomes undefined."""
+    rng = np.random.default_rng(77)
+    undefined = 0
+    for _ in range(60):
+        m, n = int(rng.integers(1, 30)), int(rng.integers(1, 30))
+        c = rng.integers(32760, 32776, size=(m, n)).astype(np.int32)
+        s = rng.integers(0, 20, size=m).astype(np.int32)
+        d = rng.integers(0, 20, size=n).astype(np.int32)
+        diff = int(s.sum() - d.sum())
+        if diff > 0:
+            d[-1] += diff
+        else:
+            s[-1] -= diff
+        undefined += assert_vogel_device_parity(fg.Instance(s, d, c)) < 0
+    assert undefined > 0
+
+
+def test_vogel_device_line_limit():
+    inst = fg.Instance(np.ones(16383, np.int32), np.array([16383], np.int32), np.ones((16383, 1), np.int32))
+    with pytest.raises(fg.FlockError) as ex:
+        fg.vogel_device(inst)
+    assert ex.value.status == fg.FLOCK_ERR_RANGE
+
+
+@pytest.mark.parametrize("pivot", ["sequential", "switch"])
+def test_solve_vam_device_start(pivot):
+    """flock_solve from the device-Vogel start: optimal and certified, the
+    objective of the reference path run from the same start."""
+    for inst in tiny_instances(41, 60) + [fg.config_instance("uniform100", 3),
+                                          fg.config_instance("degenerate1000", 2, m=300, n=250)]:
+        ref = oracle.solve_ref(inst.supply, inst.demand, inst.cost, bfs=2)
+        assert_optimal(inst, fg.solve(inst, bfs="vam_device", pivot=pivot), ref)
+
+
+def test_vam_device_batch_rejected():
+    inst = fg.config_instance("uniform100", 0)
+    with pytest.raises(fg.FlockError) as ex:
+        fg.batch_solve([inst], bfs="vam_device")
+    assert ex.value.status == fg.FLOCK_ERR_ARG
+
+
 @pytest.mark.parametrize("pivot", ["parallel", "sequential", "switch"])
 def test_solve_tiny(pivot):
     for inst in tiny_instances(23, 150):
