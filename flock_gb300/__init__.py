@@ -450,6 +450,12 @@ class flowInformation:
     qty: float
 
 
+# The reference's compile-time BFS switch (BFS_METHOD, parallel_structs.h:45):
+# "vam_host" (the default), "vam_device" or "nwc_host"; the model classes
+# below read it at execute().
+BFS_METHOD = "vam_host"
+
+
 class _Model:
     _pivot = "parallel"
 
@@ -465,7 +471,7 @@ class _Model:
 
     def execute(self) -> None:
         p = self.data
-        r = solve(Instance(p.supplies, p.demands, p.int_costs), bfs="vogel", pivot=self._pivot)
+        r = solve(Instance(p.supplies, p.demands, p.int_costs), bfs=BFS_METHOD, pivot=self._pivot)
         self.result = r
         self.objVal = r.objective / (10 ** p.cost_scale)
         self.totalIterations = r.iterations

@@ -145,6 +145,23 @@ def test_solve_vam_device_start(pivot):
         assert_optimal(inst, fg.solve(inst, bfs="vam_device", pivot=pivot), ref)
 
 
+def test_facade_bfs_method_switch(monkeypatch):
+    """The model classes follow the BFS_METHOD switch as the reference's
+    compile-time define: vam_device reaches the same optimum."""
+    inst = fg.config_instance("uniform100", 4)
+    prob = fg.ProblemInstance()
+    prob.numSupplies, prob.numDemands = inst.m, inst.n
+    prob.supplies, prob.demands, prob.int_costs, prob.cost_scale = inst.supply, inst.demand, inst.cost, 0
+    objs = []
+    for bfs in ["vam_host", "vam_device"]:
+        monkeypatch.setattr(fg, "BFS_METHOD", bfs)
+        model = fg.uvModel_parallel(prob, [])
+        model.execute()
+        objs.append(model.objVal)
+    ref = oracle.solve_ref(inst.supply, inst.demand, inst.cost, bfs=2)
+    assert objs[0] == objs[1] == round(ref["objective"])
+
+
 def test_vam_device_batch_rejected():
     inst = fg.config_instance("uniform100", 0)
     with pytest.raises(fg.FlockError) as ex:
