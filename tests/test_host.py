@@ -123,9 +123,10 @@ def test_cpp_facade_compiles(tmp_path):
     src.write_text('#include "flock/algos.h"\nint main(){ProblemInstance p; std::vector<flowInformation> f(1);'
                    ' uvModel_parallel a(&p, f.data()); ssModel_parallel b(&p, f.data());'
                    ' switchModel_parallel c(&p, f.data()); (void)a; (void)b; (void)c; return 0;}\n')
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
+    for define in [[], ["-DFLOCK_DEFAULT_BFS=FLOCK_BFS_VOGEL_DEVICE"], ["-DFLOCK_DEFAULT_BFS=FLOCK_BFS_NWC"]]:
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include")] + define
+                           + [str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
 
 
 def test_cli_usage_errors(tmp_path):
