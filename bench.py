@@ -388,7 +388,9 @@ def plain_configs(fg) -> dict:
     degenerate-prone (costs 1..20, quantities 1..50, seed 0) and 8000 x 8000
     Euclidean (costs = rounded distances of uniform points in [0,1000]^2,
     quantities 1..10000, seed 0): wall time of flock_solve, rounds, pivots,
-    pivots/s, objective and certificate."""
+    pivots/s, objective and certificate; and the wall time of each Vogel
+    variant alone (flock_vogel: vam_host semantics, flock_vogel_device:
+    vam_device semantics) after one untimed call."""
     out = {}
     fg.solve(fg.config_instance("uniform100", 0))
     for name in ("degenerate1000", "euclid8000"):
@@ -399,6 +401,16 @@ def plain_configs(fg) -> dict:
         out[name] = {"m": inst.m, "n": inst.n, "seconds": dt, "rounds": r.iterations, "pivots": r.pivots,
                      "pivots_per_s": r.pivots / dt, "objective": r.objective,
                      "certified": bool(r.certified and r.status == 0)}
+        bfs = {}
+        for label, f in (("vam_host", fg.vogel), ("vam_device", fg.vogel_device)):
+            try:
+                f(inst)
+                t0 = time.perf_counter()
+                _, ev = f(inst)
+                bfs[label] = {"ms": (time.perf_counter() - t0) * 1e3, "events": ev}
+            except Exception as ex:  # a side measurement, never required
+                bfs[label] = {"error": str(ex)}
+        out[name]["bfs_ms"] = bfs
     return out
 
 
