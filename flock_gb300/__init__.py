@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
     L.flock_dat_scale.argtypes = [ctypes.c_char_p, P(i32)]
     L.flock_read_dat.argtypes = [ctypes.c_char_p, i32, i32, i32, P(i32), P(i32), P(i32)]
     L.flock_write_bin.argtypes = [ctypes.c_char_p, P(CInstance)]
+    L.flock_write_dat.argtypes = [ctypes.c_char_p, P(CInstance), i32]
     L.flock_bin_shape.argtypes = [ctypes.c_char_p, P(i32), P(i32)]
     L.flock_read_bin.argtypes = [ctypes.c_char_p, i32, i32, P(i32), P(i32), P(i32)]
     L.flock_server_create.argtypes = [P(CServerConfig), P(ctypes.c_void_p)]
@@ -218,6 +219,13 @@ def read_dat(path: str, scale: Optional[int] = None) -> Tuple[Instance, int]:
     if rc:
         raise _err(rc)
     return Instance(s, d, c), scale
+
+
+def write_dat(inst: Instance, path: str, scale: int = 0) -> None:
+    """The reference's .dat layout; costs written as cost / 10**scale."""
+    rc = lib().flock_write_dat(path.encode(), ctypes.byref(inst.c()), int(scale))
+    if rc:
+        raise _err(rc)
 
 
 def write_bin(inst: Instance, path: str) -> None:

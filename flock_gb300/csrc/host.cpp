@@ -282,6 +282,65 @@ int bin_open(const char* path, FILE** f, int32_t* m, int32_t* n) {
 
 extern "C" {
 
+// The reference's .dat layout, as in its data/ files: "m n", the supplies
+// and then the demands on one line each with a tab after every value, then
+// one cost per line.  A cost is written as cost / 10^decimal_scale in decimal
+// with trailing zeros trimmed (at least one fractional digit when the scale
+// is positive); reading the file back with the same scale gives the same
+// integers.
+int flock_write_dat(const char* path, const flock_instance* inst, int32_t decimal_scale) {
+    if (!path || !inst || !inst->supply || !inst->demand || !inst->cost || inst->m < 1 || inst->n < 1 ||
+        decimal_scale < 0 || decimal_scale > 9)
+        return FLOCK_ERR_ARG;
+    FILE* f = fopen(path, "wb");
+    if (!f) { flock::set_error(std::string("cannot write: ") + path); return FLOCK_ERR_FILE; }
+    int64_t p10 = 1;
+    for (int k = 0; k < decimal_scale; k++) p10 *= 10;
+    std::string buf;
+    buf.reserve(1 << 20);
+    bool ok = true;
+    auto flush = [&] {
+        if (!buf.empty() && fwrite(buf.data(), 1, buf.size(), f) != buf.size()) ok = false;
+        buf.clear();
+    };
+    auto put_uint = [&](uint64_t u) {
+        char t[24];
+        int k = 0;
+        do { t[k++] = (char)('0' + u % 10); u /= 10; } while (u);
+        while (k) buf += t[--k];
+    };
+    auto put_int = [&](int64_t v) {
+        if (v < 0) buf += '-';
+        put_uint(v < 0 ? (uint64_t)(-v) : (uint64_t)v);
+    };
+    put_int(inst->m); buf += ' '; put_int(inst->n); buf += '\n';
+    for (int i = 0; i < inst->m; i++) { put_int(inst->supply[i]); buf += '\t'; }
+    buf += '\n';
+    for (int j = 0; j < inst->n; j++) { put_int(inst->demand[j]); buf += '\t'; }
+    buf += '\n';
+    const size_t mn = (size_t)inst->m * inst->n;
+    for (size_t x = 0; x < mn && ok; x++) {
+        const int64_t v = inst->cost[x];
+        const uint64_t u = v < 0 ? (uint64_t)(-v) : (uint64_t)v;
+        if (v < 0) buf += '-';
+        put_uint(u / (uint64_t)p10);
+        if (decimal_scale > 0) {
+            uint64_t frac = u % (uint64_t)p10;
+            int digits = decimal_scale;
+            while (digits > 1 && frac % 10 == 0) { frac /= 10; digits--; }
+            buf += '.';
+            char t[12];
+            for (int k = digits - 1; k >= 0; k--) { t[k] = (char)('0' + frac % 10); frac /= 10; }
+            buf.append(t, (size_t)digits);
+        }
+        buf += '\n';
+        if (buf.size() > (1u << 20)) flush();
+    }
+    flush();
+    if (fclose(f) != 0 || !ok) { flock::set_error(std::string("short write: ") + path); return FLOCK_ERR_FILE; }
+    return FLOCK_OK;
+}
+
 int flock_write_bin(const char* path, const flock_instance* inst) {
     if (!path || !inst || !inst->supply || !inst->demand || !inst->cost || inst->m < 1 || inst->n < 1) return FLOCK_ERR_ARG;
     if (!little_endian()) { flock::set_error("binary instance files need a little-endian host"); return FLOCK_ERR_ARG; }

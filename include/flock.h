@@ -135,6 +135,12 @@ int flock_dat_scale(const char* path, int32_t* scale);
 int flock_read_dat(const char* path, int32_t decimal_scale, int32_t m, int32_t n,
                    int32_t* supply, int32_t* demand, int32_t* cost);
 
+/* .dat writer in the reference's file layout (its data/ files): "m n", the
+ * supplies and the demands on one line each (a tab after every value), then
+ * one cost per line as cost / 10^decimal_scale (0..9), trailing zeros trimmed.
+ * flock_read_dat with the same scale returns the same integers. */
+int flock_write_dat(const char* path, const flock_instance* inst, int32_t decimal_scale);
+
 /* Binary instance file (no counterpart in the reference; for large instances,
  * where the text format's parse dominates): "FLKBIN01", int32 m, int32 n, then
  * m supplies, n demands and m*n costs as int32 little-endian, costs row-major.

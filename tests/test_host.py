@@ -251,3 +251,46 @@ def test_parallel_loop_concurrent_callers(flock_lib):
     for t in threads:
         t.join()
     assert not errors, errors[:3]
+
+
+def test_dat_writer_round_trip(tmp_path):
+    """flock_write_dat: the reference's file layout, and the reader returns the
+    same integers at the same scale (negative costs and zero included)."""
+    rng = np.random.default_rng(3)
+    s = rng.integers(0, 50, 7).astype(np.int32)
+    d = rng.integers(0, 50, 9).astype(np.int32)
+    d[-1] += int(s.sum() - d.sum())
+    c = rng.integers(-50000, 50000, (7, 9)).astype(np.int32)
+    c[0, 0] = 0
+    inst = fg.Instance(s, d, c)
+    for scale in (0, 2, 3):
+        p = str(tmp_path / f"x{scale}.dat")
+        fg.write_dat(inst, p, scale)
+        back, sc = fg.read_dat(p, scale)
+        assert sc == scale
+        np.testing.assert_array_equal(back.supply, s)
+        np.testing.assert_array_equal(back.demand, d)
+        np.testing.assert_array_equal(back.cost, c)
+    p = str(tmp_path / "small.dat")
+    small = fg.Instance(np.array([3, 2], np.int32), np.array([1, 4], np.int32),
+                        np.array([[150, 7], [-5, 200]], np.int32))
+    fg.write_dat(small, p, 2)
+    assert open(p).read() == "2 2\n3\t2\t\n1\t4\t\n1.5\n0.07\n-0.05\n2.0\n"
+    with pytest.raises(fg.FlockError):
+        fg.write_dat(small, p, 10)
+
+
+def test_dat_writer_reproduces_reference_files(tmp_path):
+    """Read at scale 2 and written back, the reference's own data files come
+    out byte for byte (where the reference checkout is present)."""
+    from conftest import REFERENCE
+    d = os.path.join(REFERENCE, "data")
+    if not os.path.isdir(d):
+        pytest.skip("reference data files not present")
+    files = sorted(f for f in os.listdir(d) if f.endswith(".dat") and os.path.getsize(os.path.join(d, f)) < 500_000)
+    assert files
+    for f in files[:4]:
+        inst, sc = fg.read_dat(os.path.join(d, f), 2)
+        out = str(tmp_path / f)
+        fg.write_dat(inst, out, 2)
+        assert open(out, "rb").read() == open(os.path.join(d, f), "rb").read(), f
