@@ -1,7 +1,8 @@
 """TEST INFRASTRUCTURE ONLY -- the checker, never the product.
 
 ctypes bindings of the C restatement of the reference CPU path (oracle.c ->
-liborc.so) and, where it was built, of the reference's own functions
+liborc.so; also the restatement of the reference's device Vogel,
+vogel_device) and, where it was built, of the reference's own functions
 (oracle/_ref/libflockref.so).  Only tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg import this package.
 """
