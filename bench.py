@@ -312,6 +312,15 @@ def extras(fg, insts, res, peaks) -> dict:
                                "sample": f"first {len(smp)} instances of the batch"}
         agree = sum(1 for k in range(len(smp)) if st[k] == 0 and int(round(obj[k])) == res[k].objective)
         out["cpu_baseline"]["objective_agreement"] = f"{agree}/{int((st == 0).sum())} optimal reference runs"
+        # the single-instance workloads on one core, beside plain_configs' GPU times
+        single = {}
+        for name in ("uniform100", "degenerate1000"):
+            x = fg.config_instance(name, 0)
+            t0 = time.perf_counter()
+            r = oracle.solve_ref(x.supply, x.demand, x.cost)
+            single[name] = {"seconds": time.perf_counter() - t0, "iterations": r["iterations"],
+                            "objective": r["objective"], "cores": 1}
+        out["cpu_baseline"]["single_instance"] = single
     except Exception as ex:  # the baseline is reported, never required
         out["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": str(ex)}
     return out
@@ -384,7 +393,8 @@ def served(fg) -> dict:
 
 
 def plain_configs(fg) -> dict:
-    """The plain solver on the two single-instance workloads: 1000 x 1000
+    """The plain solver on the single-instance workloads: 100 x 100 uniform
+    (costs 1..100, seed 0), 1000 x 1000
     degenerate-prone (costs 1..20, quantities 1..50, seed 0) and 8000 x 8000
     Euclidean (costs = rounded distances of uniform points in [0,1000]^2,
     quantities 1..10000, seed 0): wall time of flock_solve, rounds, pivots,
@@ -392,7 +402,12 @@ def plain_configs(fg) -> dict:
     variant alone (flock_vogel: vam_host semantics, flock_vogel_device:
     vam_device semantics) after one untimed call."""
     out = {}
-    fg.solve(fg.config_instance("uniform100", 0))
+    inst = fg.config_instance("uniform100", 0)
+    fg.solve(inst)
+    t0 = time.perf_counter()
+    r = fg.solve(inst)
+    out["uniform100"] = {"m": inst.m, "n": inst.n, "seconds": time.perf_counter() - t0, "rounds": r.iterations,
+                         "objective": r.objective, "certified": bool(r.certified and r.status == 0)}
     for name in ("degenerate1000", "euclid8000"):
         inst = fg.config_instance(name, 0)
         t0 = time.perf_counter()
