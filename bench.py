@@ -36,7 +36,6 @@ DRAM_BYTES_PER_BATCH = 3_327_000_000
 DRAM_BYTES_SWEEP_8000 = 259_300_000
 LO, HI = 10, 500
 SEED = 20251203
-CPU_SAMPLE = 512          # instances per CPU-baseline sample
 
 
 def dist_setup():
@@ -140,6 +139,29 @@ def make_batch(rank: int):
     return fg.mixed_batch(SEED + 7919 * rank, BATCH, LO, HI)
 
 
+def workload_config(world: int, shapes) -> dict:
+    """The `config` object of both arms (the same workload, the same keys).
+    shapes: (m, n) of this rank's instances."""
+    arena = sum(4 * m * ((n + 3) // 4 * 4) for m, n in shapes)
+    return {"workload": "mixed batch: 4096 balanced instances, m,n log-uniform [10,500], "
+                        "costs uniform 1..1000, quantities 100..1000, seed %d (+rank)" % SEED,
+            "instances_per_gpu": len(shapes), "parallelism": f"instances sharded, {world} GPU(s)",
+            "l2": "inputs (cost arena %.0f MB) larger than L2; no flush" % (arena / 1e6)}
+
+
+def cpu_model() -> str:
+    """Host CPU model as lscpu reports it (Arm hosts have no 'model name' in
+    /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
 def sweep_bytes(fg) -> int:
     """Cost bytes the batched kernels' sweeps read in the last batch: 4 bytes
     per priced cell, counted on the device (partial-pricing rounds price only
@@ -155,30 +177,34 @@ def sweep_bytes(fg) -> int:
 
 
 def run_reference(args, world, rank, pg):
-    """The reference's CPU path (the oracle port of it, on every host core),
-    on bounded samples of the same workload."""
+    """The reference's CPU path (the oracle port of it, on every host core) on
+    the whole workload: all 4096 instances per step, the same instances as
+    the GPU arm (the oracle's restatement of the instance generator, so this
+    process never loads the product library)."""
     import oracle
     if rank != 0:
         return 0
-    insts = make_batch(0)
+    batch = oracle.mixed_batch(SEED, BATCH, LO, HI)
     cores = os.cpu_count() or 1
-    sample = [(x.supply, x.demand, x.cost) for x in insts[:CPU_SAMPLE]]
     for _ in range(args.warmup):
-        oracle.solve_ref_batch(sample[:64], cores)
+        oracle.solve_ref_batch(batch[:256], cores)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        obj, it, st = oracle.solve_ref_batch(sample, cores)
+        obj, it, st = oracle.solve_ref_batch(batch, cores)
     dt = time.perf_counter() - t0
-    sps = len(sample) * args.steps / dt
+    sps = len(batch) * args.steps / dt
     line = {"metric": "exact-opt solves/sec (mixed batch 4096, m,n log-uniform [10,500])",
             "value": sps, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt * 1000.0 / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (reference float path)", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "mixed batch: 4096 instances, m,n log-uniform [10,500], costs 1..1000, "
-                                   "quantities 100..1000", "sample_per_step": len(sample)},
-            "cpu_baseline": {"value": sps, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"first {len(sample)} instances of the batch per step"},
+            "config": workload_config(1, [(len(x[0]), len(x[1])) for x in batch]),
+            "reference_solver": "oracle port of the reference CPU path (vam_host Vogel, host dual BFS, "
+                                "sequential scan, stepping-stone pivot), one instance per host thread",
+            "cpu_baseline": {"value": sps, "unit": "solves/s", "cores": cores, "cpu_model": cpu_model(),
+                             "kind": "port", "sample": f"all {len(batch)} instances per step "
+                                                       f"(warm-up steps: the first 256)",
+                             "reference_status": {"optimal": int((st == 0).sum()), "other": int((st != 0).sum())}},
             "e2e": {"value": sps, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -256,11 +282,8 @@ def main():
         "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": wall * 1000.0 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32 costs/quantities, int64 duals/flows", "data": "synthetic",
-        "config": {"workload": "mixed batch: 4096 balanced instances, m,n log-uniform [10,500], "
-                               "costs uniform 1..1000, quantities 100..1000, seed %d (+rank)" % SEED,
-                   "instances_per_gpu": len(insts), "parallelism": f"instances sharded, {world} GPU(s)",
-                   "solver": "Vogel start, switch pivots, partial pricing (library defaults)",
-                   "l2": "inputs (cost arena %.0f MB) larger than L2; no flush" % (h2d / 1e6)},
+        "config": workload_config(world, [(x.m, x.n) for x in insts]),
+        "solver": "Vogel start, switch pivots, partial pricing (library defaults)",
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -300,36 +323,77 @@ def extras(fg, insts, res, peaks) -> dict:
                          "ms": ms, "bytes": sb, "traffic": DRAM_BYTES_SWEEP_8000, "kernel": "k_sweep"}
     out["plain_configs"] = plain_configs(fg)
     out["served"] = served(fg)
-    # CPU baseline: the oracle port of the reference path on all host cores
+    out["cpu_baseline"] = cpu_baseline(fg, insts, res)
+    return out
+
+
+def cpu_baseline(fg, insts, res) -> dict:
+    """The reference CPU path (oracle port) beside the GPU numbers: the whole
+    batch on all host cores; the single-instance workloads on one core
+    (100 x 100 over 32 seeds, the 1000 x 1000 degenerate workload, and at
+    8000 x 8000, where a full CPU solve does not finish in a benchmark run,
+    one sequential reduced-cost scan and the first Vogel steps)."""
     try:
         import oracle
         cores = os.cpu_count() or 1
-        smp = [(x.supply, x.demand, x.cost) for x in insts[:CPU_SAMPLE]]
+        smp = [(x.supply, x.demand, x.cost) for x in insts]
         t0 = time.perf_counter()
         obj, it, st = oracle.solve_ref_batch(smp, cores)
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": len(smp) / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-                               "sample": f"first {len(smp)} instances of the batch"}
+        out = {"value": len(smp) / dt, "unit": "solves/s", "cores": cores, "cpu_model": cpu_model(),
+               "kind": "port", "sample": f"all {len(smp)} instances of the batch, one instance per host thread"}
         agree = sum(1 for k in range(len(smp)) if st[k] == 0 and int(round(obj[k])) == res[k].objective)
-        out["cpu_baseline"]["objective_agreement"] = f"{agree}/{int((st == 0).sum())} optimal reference runs"
-        # the single-instance workloads on one core, beside plain_configs' GPU times
+        out["objective_agreement"] = f"{agree}/{int((st == 0).sum())} optimal reference runs"
         single = {}
-        for name in ("uniform100", "degenerate1000"):
-            x = fg.config_instance(name, 0)
+        # 100 x 100 uniform, seeds 0..31, one core
+        secs, iters, agree0 = [], [], 0
+        for seed in range(32):
+            x = fg.config_instance("uniform100", seed)
             t0 = time.perf_counter()
             r = oracle.solve_ref(x.supply, x.demand, x.cost)
-            single[name] = {"seconds": time.perf_counter() - t0, "iterations": r["iterations"],
-                            "objective": r["objective"], "cores": 1}
-        out["cpu_baseline"]["single_instance"] = single
+            secs.append(time.perf_counter() - t0)
+            iters.append(r["iterations"])
+        single["uniform100"] = {"seeds": 32, "seconds_median": statistics.median(secs),
+                                "seconds_mean": sum(secs) / len(secs), "iterations_median": statistics.median(iters),
+                                "cores": 1}
+        x = fg.config_instance("degenerate1000", 0)
+        t0 = time.perf_counter()
+        r = oracle.solve_ref(x.supply, x.demand, x.cost)
+        single["degenerate1000"] = {"seconds": time.perf_counter() - t0, "iterations": r["iterations"],
+                                    "objective": r["objective"], "cores": 1}
+        # 8000 x 8000 Euclidean: partial phases on one core
+        x = fg.config_instance("euclid8000", 0)
+        cf = np.ascontiguousarray(x.cost, dtype=np.float32)
+        h = np.zeros(x.m + x.n, np.float32)
+        oracle.sweep(cf[:64], np.zeros(64 + x.n, np.float32))
+        t0 = time.perf_counter()
+        oracle.sweep(cf, h)
+        sweep_s = time.perf_counter() - t0
+        steps = VOGEL_CPU_STEPS
+        t0 = time.perf_counter()
+        _, _, _, _, done = oracle.vogel_steps(x.supply, x.demand, cf, steps)
+        vogel_s = time.perf_counter() - t0
+        single["euclid8000"] = {
+            "cores": 1,
+            "sweep_seconds": sweep_s,
+            "sweep_gbs": (4 * x.m * x.n + 4 * (x.m + x.n)) / sweep_s / 1e9,
+            "vogel_steps_timed": done, "vogel_ms_per_step": vogel_s * 1e3 / max(1, done),
+            "vogel_steps_total": x.m + x.n - 1,
+            "note": "full CPU solve not run (Vogel alone refreshes up to m*n cells per step); the first Vogel "
+                    "steps are the most expensive, so ms_per_step x steps_total bounds the full Vogel above"}
+        out["single_instance"] = single
+        return out
     except Exception as ex:  # the baseline is reported, never required
-        out["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": str(ex)}
-    return out
+        return {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": str(ex)}
+
+
+VOGEL_CPU_STEPS = 40
 
 
 SERVE_POOL = 512                 # served stream: distinct instances (reused)
 SERVE_REQUESTS = 1024            # requests per offered rate
 SERVE_RATES = (0.1, 0.25, 0.5, 1.0, 1.2)   # offered load as fractions of batched capacity
-SERVE_PLAIN_SAMPLE = 16
+SERVE_PLAIN_SAMPLE = 512          # the whole pool
 
 
 def served(fg) -> dict:

@@ -1248,6 +1248,17 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     return status ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
 }
 
+// Status of a Vogel-only kernel: an internal check that failed on the device
+// becomes FLOCK_ERR_CUDA with its site (flock_vogel, flock_vogel_device and
+// flock_vogel_static report it alike).
+int vogel_status_check(const Scalars& S, const char* who) {
+    if (S.status & ST_TREE_CORRUPT) {
+        set_error(std::string(who) + ": internal check failed at site " + std::to_string(S.fail_site));
+        return FLOCK_ERR_CUDA;
+    }
+    return FLOCK_OK;
+}
+
 static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* events, bool books = false) {
     int rc = validate_instance(I);
     if (rc) return rc;
@@ -1274,6 +1285,7 @@ static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* even
     Scalars* hs = P.h_sc.as<Scalars>();
     FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
     FLOCK_CK(cudaStreamSynchronize(P.stream));
+    if ((rc = vogel_status_check(*hs, books ? "flock_vogel_device" : "flock_vogel"))) return rc;
     for (int k = 0; k < V - 1; k++) flows[k] = {a[k], b[k], q[k]};
     if (events) *events = hs->events;
     return FLOCK_OK;
@@ -2237,8 +2249,13 @@ int flock_test_sweep(int32_t m, int32_t n, const int32_t* cost, const int64_t* p
 // rejected with FLOCK_ERR_RANGE before any CUDA call.
 //
 // Set-up: the first call on a device resolves the scratch array's device
-// address with cudaGetSymbolAddress (once per device, cached).  That first
-// call should come before any stream capture on the calling thread.
+// address with cudaGetSymbolAddress, with that device current, and caches it
+// for the device together with the id of the CUDA context it belongs to.  A
+// per-device lock makes the set-up safe when several host threads make their
+// first call at once.  A later call in a different context of that device
+// (after cudaDeviceReset the runtime makes a new primary context, where the
+// array may lie elsewhere) repeats the set-up.  The first call on a device
+// loads the module and should come before any stream capture.
 //
 // Concurrency: every call on one device uses the same scratch, so calls that
 // overlap in time (several host threads, or a caller reusing the stream while
@@ -2251,13 +2268,76 @@ constexpr size_t kStaticBytes = size_t(6) << 20;   // 6 MiB per device
 static __device__ __align__(256) unsigned char g_vogel_scratch[kStaticBytes];
 
 constexpr int kMaxDevices = 64;
-void* g_scratch_ptr[kMaxDevices] = {};
+// Per-device cache of the scratch array's address, valid in the context
+// whose id it records; guarded by its lock.
+struct ScratchSlot {
+    std::mutex mu;
+    void* ptr = nullptr;
+    unsigned long long ctx_id = 0;
+};
+ScratchSlot g_scratch_slot[kMaxDevices];
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
 int cuda_err(const char* what, cudaError_t e) {
     set_error(std::string("flock_vogel_static: ") + what + ": " + cudaGetErrorString(e));
     return FLOCK_ERR_CUDA;
+}
+
+// The driver's cuCtxGetCurrent and cuCtxGetId, fetched through the runtime
+// (no link against the driver library).  Signatures of CUDA 12.0.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+struct CtxFns {
+    CtxGetCurrentFn get_current = nullptr;
+    CtxGetIdFn get_id = nullptr;
+};
+const CtxFns& ctx_fns() {
+    static CtxFns f;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f.get_current = (CtxGetCurrentFn)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            f.get_id = (CtxGetIdFn)p;
+    });
+    return f;
+}
+
+// Id of the context current on this thread; 0 when none is current yet or
+// the driver does not say.
+unsigned long long current_ctx_id() {
+    const CtxFns& f = ctx_fns();
+    if (!f.get_current || !f.get_id) return 0;
+    void* ctx = nullptr;
+    if (f.get_current(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    return f.get_id(ctx, &id) == 0 ? id : 0;
+}
+
+// Device address of the scratch array on device `dev` (current), from the
+// device's cache when it was resolved in the current context.
+int scratch_address(int dev, unsigned char** out) {
+    ScratchSlot& slot = g_scratch_slot[dev];
+    std::lock_guard<std::mutex> lk(slot.mu);
+    unsigned long long id = current_ctx_id();
+    if (slot.ptr && id != 0 && id == slot.ctx_id) {
+        *out = (unsigned char*)slot.ptr;
+        return FLOCK_OK;
+    }
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_vogel_scratch);   // binds the context if none was
+    if (e != cudaSuccess) return cuda_err("cudaGetSymbolAddress", e);
+    if (id == 0) id = current_ctx_id();
+    slot.ptr = p;
+    slot.ctx_id = id;
+    *out = (unsigned char*)p;
+    return FLOCK_OK;
 }
 
 // Byte offsets of the regions inside the scratch array for one instance.
@@ -2308,13 +2388,8 @@ static int vogel_static(const flock_instance* I, flock_flow* flows, int32_t* eve
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_err("cudaGetDevice", e);
     if (dev < 0 || dev >= kMaxDevices) { set_error("flock_vogel_static: device ordinal out of range"); return FLOCK_ERR_ARG; }
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_vogel_scratch);
-        if (e != cudaSuccess) return cuda_err("cudaGetSymbolAddress", e);
-        g_scratch_ptr[dev] = p;
-    }
-    unsigned char* base = (unsigned char*)g_scratch_ptr[dev];
+    unsigned char* base = nullptr;
+    if ((rc = scratch_address(dev, &base))) return rc;
     const Layout L = layout_for(m, n);
     cudaStream_t s = cudaStreamPerThread;
 
@@ -2352,10 +2427,7 @@ static int vogel_static(const flock_instance* I, flock_flow* flows, int32_t* eve
     if (e != cudaSuccess) return cuda_err("scalar download", e);
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_err("k_vogel_static", e);
-    if (hs.status & ST_TREE_CORRUPT) {
-        set_error("flock_vogel_static: internal check failed at site " + std::to_string(hs.fail_site));
-        return FLOCK_ERR_CUDA;
-    }
+    if ((rc = vogel_status_check(hs, "flock_vogel_static"))) return rc;
     if (events) *events = hs.events;
     return FLOCK_OK;
 }

@@ -151,7 +151,8 @@ int flock_bin_shape(const char* path, int32_t* m, int32_t* n);
 int flock_read_bin(const char* path, int32_t m, int32_t n, int32_t* supply, int32_t* demand, int32_t* cost);
 
 /* Vogel's approximation on the GPU with the reference's exact semantics.
- * Writes m+n-1 allocations in allocation order.  *events as flock_stats. */
+ * Writes m+n-1 allocations in allocation order.  *events as flock_stats.
+ * FLOCK_ERR_CUDA for a CUDA failure or a failed internal device check. */
 int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events);
 
 /* Vogel's approximation with the semantics of the reference's device variant
@@ -165,23 +166,27 @@ int flock_vogel(const flock_instance* inst, flock_flow* flows, int32_t* events);
 int flock_vogel_device(const flock_instance* inst, flock_flow* flows, int32_t* events);
 
 /* No counterpart in the reference.  flock_vogel without any allocation:
- * the same kernel and identical results, but every device array of the call
- * lives in one static 6 MiB __device__ array per device, so the call makes no
- * cudaMalloc/cudaFree, allocates no pinned host memory and creates no stream
- * or event.  It is for callers that cannot allocate: a process whose device
- * memory is already reserved by another allocator (a caching allocator or a
- * fixed serving budget holding the device), where cudaMalloc fails or takes
- * memory promised elsewhere; and latency-bound callers on a busy device,
- * where cudaFree's implicit device-wide synchronisation would stall other
- * streams.
+ * the same kernel and the same allocation list and event count, but every
+ * device array of the call lives in one static 6 MiB __device__ array per
+ * device, so the call makes no cudaMalloc/cudaFree, allocates no pinned host
+ * memory and creates no stream or event itself.  It is for callers that
+ * cannot allocate: a process whose device memory is already reserved by
+ * another allocator (a caching allocator or a fixed serving budget holding
+ * the device), where cudaMalloc fails or takes memory promised elsewhere; and
+ * latency-bound callers on a busy device, where cudaFree's implicit
+ * device-wide synchronisation would stall other streams.
  * Limits: m + n <= FLOCK_VOGEL_STATIC_MAX_V and m * ceil4(n) <=
  * FLOCK_VOGEL_STATIC_MAX_CELLS; larger instances return FLOCK_ERR_RANGE
  * (message via flock_last_error) before any CUDA call.
  * The first call on a device does the set-up (cudaGetSymbolAddress of the
- * scratch array, cached per device) and should come before any stream
- * capture.  Work runs on cudaStreamPerThread; the call returns after
- * synchronising it.  Calls that overlap in time on one device share the
- * scratch and race: callers serialise them. */
+ * scratch array, cached per device and context under a per-device lock) and
+ * should come before any stream capture.  Work runs on the calling thread's
+ * per-thread default stream (cudaStreamPerThread, which the runtime creates
+ * on the thread's first use; it does not synchronise with the legacy default
+ * stream), and the call returns after synchronising it.  Calls that overlap
+ * in time on one device share the scratch and race: callers serialise them.
+ * Errors as flock_vogel: argument and range errors before any CUDA call,
+ * FLOCK_ERR_CUDA for a CUDA failure or a failed internal device check. */
 #define FLOCK_VOGEL_STATIC_MAX_V 8192
 #define FLOCK_VOGEL_STATIC_MAX_CELLS 1048576
 int flock_vogel_static(const flock_instance* inst, flock_flow* flows, int32_t* events);

@@ -63,6 +63,12 @@ def orc() -> ctypes.CDLL:
         L.orc_tree_duals.argtypes = [i32, i32, P(i32), i32, P(i32), P(i32), P(i64), P(i64)]
         L.orc_certify.argtypes = [i32, i32, P(i32), P(i32), P(i32), i32, P(i32), P(i32), P(i64),
                                   P(i64), P(i64), P(i64)]
+        L.orc_vogel_steps.argtypes = [i32, i32, P(i32), P(i32), P(ctypes.c_float), i32, P(i32), P(i32),
+                                      P(ctypes.c_float), P(i32)]
+        L.orc_sweep.argtypes = [i32, i32, P(ctypes.c_float), P(ctypes.c_float), P(i32), P(i32)]
+        L.orc_sweep.restype = ctypes.c_float
+        L.orc_generate.argtypes = [i32, ctypes.c_uint64, i32, i32, i32, i32, i32, i32, P(i32), P(i32), P(i32)]
+        L.orc_generate_sizes.argtypes = [ctypes.c_uint64, i32, i32, i32, P(i32), P(i32)]
         _orc = L
     return _orc
 
@@ -118,6 +124,59 @@ def vogel_device(s, d, c):
     rc = orc().orc_vogel_device(m, n, _p(s), _p(d), _p(cf, ctypes.c_float), _p(src), _p(dst),
                                 _p(q, ctypes.c_float))
     return src, dst, q, int(rc)
+
+
+def vogel_steps(s, d, c, max_steps: int):
+    """The reference Vogel stopped after max_steps allocations.  Returns
+    (src, dst, qty float32, events, steps made)."""
+    s, d, cf = _prep(s, d, c)
+    m, n = len(s), len(d)
+    src = np.zeros(m + n - 1, np.int32)
+    dst = np.zeros(m + n - 1, np.int32)
+    q = np.zeros(m + n - 1, np.float32)
+    k = i32()
+    ev = orc().orc_vogel_steps(m, n, _p(s), _p(d), _p(cf, ctypes.c_float), max_steps, _p(src), _p(dst),
+                               _p(q, ctypes.c_float), ctypes.byref(k))
+    return src, dst, q, int(ev), int(k.value)
+
+
+def sweep(c, h):
+    """One sequential reduced-cost scan (float).  c: (m, n) costs, h: m row
+    duals then n column duals.  Returns (min reduced cost, row, col)."""
+    cf = np.ascontiguousarray(c, dtype=np.float32)
+    m, n = cf.shape
+    hf = np.ascontiguousarray(h, dtype=np.float32)
+    assert hf.shape == (m + n,)
+    r, q = i32(), i32()
+    v = orc().orc_sweep(m, n, _p(cf, ctypes.c_float), _p(hf, ctypes.c_float), ctypes.byref(r), ctypes.byref(q))
+    return float(v), int(r.value), int(q.value)
+
+
+def generate(kind: int, seed: int, m: int, n: int, c_lo: int, c_hi: int, q_lo: int, q_hi: int):
+    """The benchmark's instance generator (same integers as the library's
+    flock_generate).  Returns (supply, demand, cost (m, n))."""
+    s = np.empty(m, np.int32)
+    d = np.empty(n, np.int32)
+    c = np.empty((m, n), np.int32)
+    if orc().orc_generate(kind, seed, m, n, c_lo, c_hi, q_lo, q_hi, _p(s), _p(d), _p(c)):
+        raise ValueError("bad generator arguments")
+    return s, d, c
+
+
+def generate_sizes(seed: int, count: int, lo: int, hi: int):
+    ms = np.empty(count, np.int32)
+    ns = np.empty(count, np.int32)
+    if orc().orc_generate_sizes(seed, count, lo, hi, _p(ms), _p(ns)):
+        raise ValueError("bad size arguments")
+    return ms, ns
+
+
+def mixed_batch(seed: int, count: int, lo: int, hi: int):
+    """The batched workload as (supply, demand, cost) triples: m and n
+    log-uniform in [lo, hi], costs 1..1000, quantities 100..1000 (the same
+    instances as the library's batch generator for the same seed)."""
+    ms, ns = generate_sizes(seed, count, lo, hi)
+    return [generate(0, seed * 1000003 + k + 1, int(ms[k]), int(ns[k]), 1, 1000, 100, 1000) for k in range(count)]
 
 
 def nwc(s, d):

@@ -34,9 +34,10 @@ static void fill_undefined(int32_t* src, int32_t* dst, float* qty, int from, int
     for (int k = from; k < to; k++) { src[k] = -1; dst[k] = -1; qty[k] = 0.0f; }
 }
 
-/* IBFS_vogel.cu:546-769, find_vogel_bfs_sequencial. */
-int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
-              int32_t* src, int32_t* dst, float* qty) {
+/* IBFS_vogel.cu:546-769, find_vogel_bfs_sequencial, stopped after
+ * max_steps allocations (*steps_done of them made; orc_vogel runs all m+n-1). */
+static int vogel_steps(int m, int n, const int32_t* s, const int32_t* d, const float* c, int max_steps,
+                       int32_t* src, int32_t* dst, float* qty, int* steps_done) {
     const int V = m + n;
     int32_t* rs = (int32_t*)malloc(sizeof(int32_t) * (size_t)m);
     int32_t* rd = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
@@ -55,7 +56,9 @@ int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
     int events = 0;
     const float FMAX = (float)2147483647; /* INT_MAX converted: 2^31 */
 
-    while (coveredRows + coveredCols < V - 1) {
+    int steps = 0;
+    while (coveredRows + coveredCols < V - 1 && steps < max_steps) {
+        steps++;
         if (prev_row) { /* :588-613 */
             for (int i = 0; i < m; i++) {
                 if (rowCov[i] == 0) {
@@ -143,7 +146,21 @@ int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
         qty[counter] = q;
     }
     free(rs); free(rd); free(rowCov); free(colCov); free(diff);
+    if (steps_done) *steps_done = steps;
     return events;
+}
+
+int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
+              int32_t* src, int32_t* dst, float* qty) {
+    return vogel_steps(m, n, s, d, c, m + n - 1, src, dst, qty, NULL);
+}
+
+int orc_vogel_steps(int m, int n, const int32_t* s, const int32_t* d, const float* c, int max_steps,
+                    int32_t* src, int32_t* dst, float* qty, int32_t* steps_done) {
+    int k = 0;
+    const int ev = vogel_steps(m, n, s, d, c, max_steps, src, dst, qty, &k);
+    if (steps_done) *steps_done = k;
+    return ev;
 }
 
 /* ---------------------------------------------------------------------- */
@@ -324,6 +341,31 @@ static int cmp_i64(const void* a, const void* b) {
     return (x > y) - (x < y);
 }
 
+/* uv_model_parallel.cu:178-200: the sequential reduced-cost scan, row-major,
+ * the first strict minimum of c_ij - h_i - h_{m+j} (float). */
+static void seq_sweep(int m, int n, const float* c, const float* h, float* min_out, int* row, int* col) {
+    float min_r = (float)2147483647;
+    int pr = -1, pc = -1;
+    for (int i = 0; i < m; i++) {
+        const float* ci = c + (size_t)i * n;
+        float ui = h[i];
+        for (int j = 0; j < n; j++) {
+            float r = ci[j] - ui - h[m + j];
+            if (r < min_r) { min_r = r; pr = i; pc = j; }
+        }
+    }
+    *min_out = min_r; *row = pr; *col = pc;
+}
+
+float orc_sweep(int m, int n, const float* c, const float* h, int32_t* row, int32_t* col) {
+    float r;
+    int a, b;
+    seq_sweep(m, n, c, h, &r, &a, &b);
+    if (row) *row = a;
+    if (col) *col = b;
+    return r;
+}
+
 int orc_solve_ref(int m, int n, const int32_t* s, const int32_t* d, const float* c,
                   int bfs_method, int max_iter,
                   int32_t* fsrc, int32_t* fdst, float* fqty,
@@ -404,17 +446,9 @@ int orc_solve_ref(int m, int n, const int32_t* s, const int32_t* d, const float*
                 }
             }
         }
-        /* uv_model_parallel.cu:178-200 */
-        float min_r = (float)2147483647;
-        int pr = -1, pc = -1;
-        for (int i = 0; i < m; i++) {
-            const float* ci = c + (size_t)i * n;
-            float ui = h[i];
-            for (int j = 0; j < n; j++) {
-                float r = ci[j] - ui - h[m + j];
-                if (r < min_r) { min_r = r; pr = i; pc = j; }
-            }
-        }
+        float min_r;
+        int pr, pc;
+        seq_sweep(m, n, c, h, &min_r, &pr, &pc);
         /* PIVOT_uv.cu:318-401 */
         if (min_r < 0 && (double)fabsf(min_r) > ORC_EPSILON2) {
             /* PIVOT_uv.cu:156-209 (DFS from column vertex m+pc to row pr) */
@@ -636,4 +670,91 @@ int orc_certify(int m, int n, const int32_t* s, const int32_t* d, const int32_t*
     if (objective) *objective = obj;
     free(rs); free(cs);
     return bad;
+}
+
+/* ---------------------------------------------------------------------- */
+/* The benchmark's instance generator (flock_generate / flock_generate_sizes
+ * of the native library), restated here so that the timed CPU path can make
+ * its inputs without loading the product: a splitmix64 stream, Lemire's
+ * bounded integers (multiply-shift with rejection below 2^32 mod range),
+ * 53-bit unit doubles; Euclidean costs round(sqrt(dx^2 + dy^2)) half away
+ * from zero; demands scaled to the supply total, remainder to the last.
+ * tests/test_oracle_pin.py checks it against the library bit for bit. */
+typedef struct { uint64_t s; } orc_rng;
+
+static uint64_t rng_next(orc_rng* r) {
+    uint64_t z = (r->s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint32_t rng_bounded(orc_rng* r, uint32_t range) {
+    uint32_t x = (uint32_t)(rng_next(r) >> 32);
+    uint64_t mm = (uint64_t)x * range;
+    uint32_t lo = (uint32_t)mm;
+    if (lo < range) {
+        const uint32_t t = (uint32_t)(0u - range) % range;
+        while (lo < t) { x = (uint32_t)(rng_next(r) >> 32); mm = (uint64_t)x * range; lo = (uint32_t)mm; }
+    }
+    return (uint32_t)(mm >> 32);
+}
+
+static int32_t rng_uniform(orc_rng* r, int32_t lo, int32_t hi) {
+    return lo + (int32_t)rng_bounded(r, (uint32_t)(hi - lo + 1));
+}
+
+static double rng_unit(orc_rng* r) { return (double)(rng_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+
+int orc_generate(int kind, uint64_t seed, int m, int n, int c_lo, int c_hi, int q_lo, int q_hi,
+                 int32_t* supply, int32_t* demand, int32_t* cost) {
+    if (m < 1 || n < 1 || q_lo < 0 || q_hi < q_lo) return 1;
+    orc_rng r = {seed};
+    if (kind == 0) {
+        if (c_hi < c_lo) return 1;
+        for (int64_t k = 0; k < (int64_t)m * n; k++) cost[k] = rng_uniform(&r, c_lo, c_hi);
+    } else if (kind == 1) {
+        double* px = (double*)malloc(sizeof(double) * (size_t)(2 * m + 2 * n));
+        double *py = px + m, *qx = py + m, *qy = qx + n;
+        for (int i = 0; i < m; i++) { px[i] = 1000.0 * rng_unit(&r); py[i] = 1000.0 * rng_unit(&r); }
+        for (int j = 0; j < n; j++) { qx[j] = 1000.0 * rng_unit(&r); qy[j] = 1000.0 * rng_unit(&r); }
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < n; j++) {
+                const double dx = px[i] - qx[j], dy = py[i] - qy[j];
+                const double sq = dx * dx;
+                const double s2 = sq + dy * dy;
+                cost[(size_t)i * n + j] = (int32_t)round(sqrt(s2));
+            }
+        free(px);
+    } else {
+        return 1;
+    }
+    int64_t S = 0, R = 0, D = 0;
+    for (int i = 0; i < m; i++) { supply[i] = rng_uniform(&r, q_lo, q_hi); S += supply[i]; }
+    int64_t* raw = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+    for (int j = 0; j < n; j++) { raw[j] = rng_uniform(&r, q_lo, q_hi); R += raw[j]; }
+    for (int j = 0; j < n; j++) {
+        const int64_t dj = R > 0 ? (raw[j] * S) / R : (j == n - 1 ? S : 0);
+        demand[j] = (int32_t)dj;
+        D += dj;
+    }
+    demand[n - 1] += (int32_t)(S - D);
+    free(raw);
+    return 0;
+}
+
+int orc_generate_sizes(uint64_t seed, int count, int lo, int hi, int32_t* ms, int32_t* ns) {
+    if (count < 0 || lo < 1 || hi < lo) return 1;
+    orc_rng r = {seed};
+    const double a = log((double)lo), b = log((double)hi);
+    for (int k = 0; k < count; k++) {
+        const double um = a + (b - a) * rng_unit(&r);
+        const double un = a + (b - a) * rng_unit(&r);
+        double x = round(exp(um)), y = round(exp(un));
+        x = x < lo ? lo : (x > hi ? hi : x);
+        y = y < lo ? lo : (y > hi ? hi : y);
+        ms[k] = (int32_t)x;
+        ns[k] = (int32_t)y;
+    }
+    return 0;
 }

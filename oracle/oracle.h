@@ -33,6 +33,23 @@ extern "C" {
 int orc_vogel(int m, int n, const int32_t* s, const int32_t* d, const float* c,
               int32_t* src, int32_t* dst, float* qty);
 
+/* orc_vogel stopped after max_steps allocations (a bounded CPU timing sample
+ * of a large instance); *steps_done = allocations made.  Same return value. */
+int orc_vogel_steps(int m, int n, const int32_t* s, const int32_t* d, const float* c, int max_steps,
+                    int32_t* src, int32_t* dst, float* qty, int32_t* steps_done);
+
+/* One sequential reduced-cost scan as uv_model_parallel.cu:178-200: returns
+ * the first (row-major) strict minimum of c_ij - h_i - h_{m+j} and its cell.
+ * h holds the m row duals, then the n column duals (float). */
+float orc_sweep(int m, int n, const float* c, const float* h, int32_t* row, int32_t* col);
+
+/* The benchmark's instance generator restated (no reference counterpart; it
+ * lets the timed CPU path build its inputs without the product library):
+ * the same integers as flock_generate / flock_generate_sizes.  0 = ok. */
+int orc_generate(int kind, uint64_t seed, int m, int n, int c_lo, int c_hi, int q_lo, int q_hi,
+                 int32_t* supply, int32_t* demand, int32_t* cost);
+int orc_generate_sizes(uint64_t seed, int count, int lo, int hi, int32_t* ms, int32_t* ns);
+
 /* Vogel's approximation as the reference's device variant
  * find_vogel_bfs_parallel ("vam_device", IBFS_vogel.cu:3-543): regrets from
  * positions into per-line cost-sorted books, first largest regret, its own

@@ -8,7 +8,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = "/root/reference"   # present only where the golden files were made
+# The reference checkout, present only where the golden files were made;
+# FLOCK_REFERENCE overrides the default location.
+REFERENCE = os.environ.get("FLOCK_REFERENCE", "/root/reference")
 
 
 def pytest_configure(config):

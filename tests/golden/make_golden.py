@@ -142,7 +142,7 @@ def main(refdir):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if a != "--published-only"]
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else os.environ.get("FLOCK_REFERENCE", "/root/reference")
     if "--published-only" in sys.argv:
         write_published(ref)       # the run logs only (no reference build needed)
     else:

@@ -385,3 +385,24 @@ def test_lp_optimum_cross_check():
         p = fg.solve(inst)
         assert p.status == 0 and p.certified and p.objective == opt, k
         assert batch[k].status == 0 and batch[k].certified and batch[k].objective == opt, k
+
+
+# Certified optimum of the 8000 x 8000 Euclidean workload, seed 0 (the
+# reference CPU path cannot finish an instance of this size -- its Vogel
+# refreshes up to m*n cells per allocation and its loop stops at 30000
+# iterations -- so the pin is the exact certificate, checked on the host).
+EUCLID8000_OPTIMUM = 614_260_730
+
+
+def test_euclid8000_full_size_certified():
+    """The 8000 x 8000 Euclidean workload at full size on the plain solver
+    (grid-wide rounds, partial pricing): the host oracle's exact certificate
+    over all 64 M cells (row and column sums, every reduced cost >= 0 in
+    int64, complementary slackness) and the objective, computed on the host
+    from the returned flows."""
+    inst = fg.config_instance("euclid8000", 0)
+    res = fg.solve(inst)
+    assert res.status == 0 and res.certified, (res.status, res.notes)
+    bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, res.flows, res.u, res.v)
+    assert bits == 0, f"certificate bits {bits}"
+    assert obj == res.objective == EUCLID8000_OPTIMUM

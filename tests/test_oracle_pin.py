@@ -170,3 +170,53 @@ def test_reference_path_matches_lp_optimum(orc):
         assert round(r["objective"]) == lp_optimum(inst.supply, inst.demand, inst.cost), seed
         checked += 1
     assert checked >= 8
+
+
+def test_generator_restatement_matches_library():
+    """The oracle's restatement of the instance generator (used by the
+    benchmark's reference arm, which does not load the product library)
+    makes the library's instances bit for bit: the mixed batch, the uniform
+    and the Euclidean generators."""
+    import flock_gb300 as fg
+    a = oracle.mixed_batch(20251203, 96, 10, 500)
+    b = fg.mixed_batch(20251203, 96, 10, 500)
+    for x, y in zip(a, b):
+        for u, w in zip(x, (y.supply, y.demand, y.cost)):
+            np.testing.assert_array_equal(u, w)
+    for kind, args in ((0, (1, 20, 1, 50)), (1, (0, 0, 1, 10000)), (0, (5, 5, 0, 0))):
+        s, d, c = oracle.generate(kind, 77, 123, 211, *args)
+        y = fg.generate(kind, 77, 123, 211, *args)
+        np.testing.assert_array_equal(c, y.cost)
+        np.testing.assert_array_equal(s, y.supply)
+        np.testing.assert_array_equal(d, y.demand)
+    ms, ns = oracle.generate_sizes(5, 1000, 10, 2000)
+    gm, gn = fg.generate_sizes(5, 1000, 10, 2000)
+    np.testing.assert_array_equal(ms, gm)
+    np.testing.assert_array_equal(ns, gn)
+
+
+def test_bounded_cpu_samples_follow_the_pinned_path():
+    """The bounded CPU samples of large instances (the first Vogel steps, one
+    sequential scan) are the pinned functions cut short: the first k
+    allocations equal the full Vogel's, and the scan finds the same entering
+    cell as a numpy restatement of the reference's row-major first strict
+    minimum."""
+    rng = np.random.default_rng(3)
+    for m, n in ((40, 30), (7, 90), (120, 5)):
+        s = rng.integers(1, 50, m).astype(np.int32)
+        d = rng.integers(1, 50, n).astype(np.int32)
+        d[-1] += int(s.sum() - d.sum()) if s.sum() > d.sum() else 0
+        s[-1] += int(d.sum() - s.sum()) if d.sum() > s.sum() else 0
+        c = rng.integers(1, 20, (m, n)).astype(np.int32)
+        src, dst, q, ev = oracle.vogel(s, d, c)
+        for k in (1, 5, m + n - 1):
+            a, b, qq, ev2, done = oracle.vogel_steps(s, d, c, k)
+            assert done == k
+            np.testing.assert_array_equal(a[:k], src[:k])
+            np.testing.assert_array_equal(b[:k], dst[:k])
+            np.testing.assert_array_equal(qq[:k], q[:k])
+        h = rng.integers(-30, 30, m + n).astype(np.float32)
+        r = c.astype(np.float32) - h[:m, None] - h[None, m:]
+        flat = int(np.argmin(r))       # first minimum in row-major order
+        v, i, j = oracle.sweep(c, h)
+        assert (i, j) == divmod(flat, n) and v == r.min()

@@ -1,6 +1,8 @@
 """flock_vogel_static, the allocation-free Vogel entry point (no counterpart in
 the reference): called through the C ABI twice in a row per instance, its
-allocation lists and event counts must equal flock_vogel's bit for bit.
+allocation lists and event counts must equal flock_vogel's bit for bit and
+the oracle's (the reference's Vogel restated on the CPU), and the calls must
+leave the device's free memory unchanged (nothing allocated, nothing freed).
 
 The file name sorts last so that the test also runs after every other test of
 the session (a warm library, scratch left over from other calls); it passes
@@ -13,6 +15,7 @@ import numpy as np
 import pytest
 
 import flock_gb300 as fg
+import oracle
 
 MAX_V = 8192
 MAX_CELLS = 1048576
@@ -49,15 +52,61 @@ def _cases():
     return out
 
 
+def _cudart():
+    """The CUDA runtime the native library was linked against (found among the
+    process's mapped files once the library is loaded)."""
+    fg.lib()
+    with open("/proc/self/maps") as f:
+        paths = sorted({ln.split()[-1] for ln in f if "libcudart.so" in ln})
+    assert paths, "libcudart is not mapped"
+    rt = ctypes.CDLL(paths[0])
+    rt.cudaMemGetInfo.argtypes = [ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
+    return rt
+
+
+def _free_bytes(rt):
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return int(free.value)
+
+
+def _oracle_list(inst):
+    """The oracle's allocation list in the C ABI's (source, destination, qty)
+    layout (the reference writes 1e-6 for a zero allocation), cut before the
+    first entry where the reference indexes past its arrays (events -1), from
+    where its result is undefined."""
+    src, dst, q, oev = oracle.vogel(inst.supply, inst.demand, inst.cost)
+    qi = np.where(q < 0.5, 0, q).astype(np.int64)
+    out = np.stack([src, dst, qi], 1)
+    if oev < 0:
+        out = out[:int(np.argmax(src < 0))]
+    return out, oev
+
+
 @pytest.mark.gpu
 def test_static_vogel_matches_vogel_twice():
-    for name, inst in _cases():
+    cases = _cases()
+    # expected results first: flock_vogel grows its own device buffers
+    expected = []
+    for name, inst in cases:
         ref_flows, ref_ev = fg.vogel(inst)
+        orc_flows, orc_ev = _oracle_list(inst)
+        assert ref_ev == orc_ev, (name, ref_ev, orc_ev)
+        np.testing.assert_array_equal(ref_flows[:len(orc_flows)].astype(np.int64), orc_flows, err_msg=name)
+        expected.append((ref_flows, ref_ev, orc_flows))
+    rt = _cudart()
+    rc, _, _ = vogel_static(cases[0][1])        # set-up call (module and per-thread stream)
+    assert rc == fg.FLOCK_OK, fg.lib().flock_last_error()
+    free0 = _free_bytes(rt)
+    for (name, inst), (ref_flows, ref_ev, orc_flows) in zip(cases, expected):
         for call in (1, 2):
             rc, flows, ev = vogel_static(inst)
             assert rc == fg.FLOCK_OK, (name, call, rc, fg.lib().flock_last_error())
             assert ev == ref_ev, (name, call, ev, ref_ev)
             np.testing.assert_array_equal(flows, ref_flows, err_msg=f"{name}, call {call}")
+            np.testing.assert_array_equal(flows[:len(orc_flows)].astype(np.int64), orc_flows,
+                                          err_msg=f"{name}, call {call}, oracle")
+    assert _free_bytes(rt) == free0, "device free memory changed across the calls"
 
 
 def test_static_vogel_rejects_oversize():
