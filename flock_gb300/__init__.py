@@ -41,7 +41,9 @@ class COptions(ctypes.Structure):
 class CStats(ctypes.Structure):
     _fields_ = [("objective", i64), ("iterations", i32), ("pivots", i32), ("active_flows", i32),
                 ("status", i32), ("notes", i32), ("certified", i32), ("vogel_events", i32),
-                ("ms_total", ctypes.c_double), ("ms_bfs", ctypes.c_double), ("ms_simplex", ctypes.c_double)]
+                ("ms_total", ctypes.c_double), ("ms_bfs", ctypes.c_double), ("ms_simplex", ctypes.c_double),
+                ("ms_dual", ctypes.c_double), ("ms_sweep", ctypes.c_double), ("ms_pivot", ctypes.c_double),
+                ("ms_cycle", ctypes.c_double), ("ms_resolve", ctypes.c_double), ("ms_adjust", ctypes.c_double)]
 
 
 class CServerConfig(ctypes.Structure):
@@ -60,7 +62,7 @@ ST_ITER_CAP, ST_TREE_CORRUPT, ST_SF_FAIL, ST_CERT_FAIL, ST_RANGE = 1, 2, 4, 32, 
 NOTE_VOGEL_UNDEF, NOTE_START_REPAIRED = 8, 16
 
 BFS = {"nwc": 0, "nwc_host": 0, "vogel": 1, "vam_host": 1, "vogel_device": 2, "vam_device": 2}
-PIVOT = {"sequential": 0, "parallel_uv": 0, "parallel": 1, "parallel_ss": 1, "switch": 2, "switch_hybrid": 2}
+PIVOT = {"sequential": 0, "parallel_uv": 0, "parallel": 1, "switch": 2, "switch_hybrid": 2, "ss": 3, "parallel_ss": 3}
 
 
 class FlockError(RuntimeError):
@@ -268,6 +270,13 @@ class Result:
     ms_simplex: float
     u: Optional[np.ndarray] = None
     v: Optional[np.ndarray] = None
+    # device time per simplex phase (plain solver; 0 in the batched and served forms)
+    ms_dual: float = 0.0
+    ms_sweep: float = 0.0
+    ms_pivot: float = 0.0
+    ms_cycle: float = 0.0
+    ms_resolve: float = 0.0
+    ms_adjust: float = 0.0
 
     @property
     def optimal(self) -> bool:
@@ -284,7 +293,8 @@ def _options(bfs="vogel", pivot="switch", max_iterations=0, verify=True, pricing
 def _result(st: CStats, flows: np.ndarray, u=None, v=None) -> Result:
     return Result(int(st.objective), flows, int(st.active_flows), int(st.iterations), int(st.pivots),
                   int(st.status), int(st.notes), bool(st.certified), int(st.vogel_events), float(st.ms_total),
-                  float(st.ms_bfs), float(st.ms_simplex), u, v)
+                  float(st.ms_bfs), float(st.ms_simplex), u, v, float(st.ms_dual), float(st.ms_sweep),
+                  float(st.ms_pivot), float(st.ms_cycle), float(st.ms_resolve), float(st.ms_adjust))
 
 
 def solve(inst: Instance, bfs: str = "vogel", pivot: str = "switch", max_iterations: int = 0,
@@ -484,7 +494,13 @@ class _Model:
         self.objVal = r.objective / (10 ** p.cost_scale)
         self.totalIterations = r.iterations
         self.totalSolveTime = r.ms_bfs + r.ms_simplex
-        self.pivot_time = r.ms_simplex * 1000.0
+        # phase times in microseconds, as the reference's model statistics
+        self.uv_time = r.ms_dual * 1000.0
+        self.reduced_cost_time = r.ms_sweep * 1000.0
+        self.pivot_time = r.ms_pivot * 1000.0
+        self.cycle_discovery_time = r.ms_cycle * 1000.0
+        self.resolve_time = r.ms_resolve * 1000.0
+        self.adjustment_time = r.ms_adjust * 1000.0
         p.active_flows = r.active_flows
         p.totalFlowCost = self.objVal
         p.solveTime = self.totalSolveTime
@@ -501,8 +517,9 @@ class uvModel_parallel(_Model):
 
 
 class ssModel_parallel(_Model):
-    """-a parallel_ss: deconflicted parallel stepping-stone pivots."""
-    _pivot = "parallel"
+    """-a parallel_ss: every negative cell a candidate, the greedy
+    most-negative set of tree-edge-disjoint cycles pivoted together."""
+    _pivot = "parallel_ss"
 
 
 class switchModel_parallel(_Model):

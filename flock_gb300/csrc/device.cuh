@@ -85,6 +85,98 @@ struct Scalars {
     int32_t pad_;
 };
 
+// Phase clock of the plain solver: device time per phase of the simplex,
+// the reference's model statistics (uv_model_parallel.cu:301-341, the
+// PivotTimer of parallel_structs.h:244-247): duals (a rebuild of the tree's
+// derived state), reduced costs (the sweeps and the choice of the entering
+// cells), cycle discovery, resolve (deconfliction of parallel candidates)
+// and adjustment (leaving edge, flow change, in-place update of the tree).
+// Every segment runs from one mark to the next, marks read %globaltimer, and
+// a kernel's first segment starts at its first block's start, so the phases
+// add up to the loop's device time (launch gaps included in the phase before
+// them).  Kernels that find the solve finished count as idle.
+enum : int32_t { PH_BFS = 0, PH_DUAL, PH_SWEEP, PH_CYCLE, PH_RESOLVE, PH_ADJUST, PH_IDLE, kPhases };
+struct PhaseClock {
+    uint64_t last;          // globaltimer at the start of the running segment (0: none yet)
+    int32_t cur;            // phase of the running segment
+    int32_t pad_;
+    uint64_t ns[kPhases];   // accumulated nanoseconds per phase
+};
+
+__device__ __forceinline__ uint64_t global_ns() {
+#ifdef FLOCK_EMU
+    return 0;
+#else
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+#endif
+}
+
+// Shared-memory state of one launch's phase accounting (block 0 only).
+struct PhaseLocal {
+    uint64_t prev_last;     // the clock's `last` and `cur` as the previous launch left them
+    int32_t prev_cur, pad_;
+    uint64_t t0, t;         // this launch's start, start of its running segment
+    PhaseClock* clk;        // null: no accounting in this launch
+    int32_t cur, pad2_;
+};
+
+// The phase accounting of one kernel launch, kept by thread 0 of block 0;
+// mark() may be called by every thread at block-uniform points (after a
+// barrier).  The state lives in shared memory (nothing held in registers
+// across the kernel) and the previous launch's values arrive by an
+// asynchronous copy (no wait on a global load).  At scope exit, early returns
+// included, it closes the previous launch's last segment at this launch's
+// start and leaves its own last segment running for the next launch.
+struct PhaseScope {
+    PhaseLocal* s;
+    __device__ __forceinline__ static bool leader() { return blockIdx.x == 0 && threadIdx.x == 0; }
+    __device__ __forceinline__ PhaseScope(PhaseClock* p, PhaseLocal* sl, int phase) : s(sl) {
+        if (!leader()) return;
+        s->clk = p;
+        if (!p) return;
+#ifdef FLOCK_EMU
+        s->prev_last = p->last;
+        s->prev_cur = p->cur;
+#else
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(s);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n\tcp.async.commit_group;"
+                     :: "r"(dst), "l"(p) : "memory");
+#endif
+        s->t0 = s->t = global_ns();
+        s->cur = phase;
+    }
+    __device__ __forceinline__ void mark(int next) {
+        if (!leader() || !s->clk) return;
+        const uint64_t now = global_ns();
+        atomicAdd((unsigned long long*)&s->clk->ns[s->cur], (unsigned long long)(now - s->t));
+        s->t = now;
+        s->cur = next;
+    }
+    // The solve was already finished: this launch counts as idle.
+    __device__ __forceinline__ void idle() {
+        if (leader() && s->clk) s->cur = PH_IDLE;
+    }
+    __device__ __forceinline__ ~PhaseScope() {
+        if (leader()) close(s);
+    }
+    // Out of line: the hot kernels keep their registers for their own work.
+    __device__ __noinline__ static void close(PhaseLocal* s) {
+        PhaseClock* ph = s->clk;
+        if (!ph) return;
+#ifndef FLOCK_EMU
+        asm volatile("cp.async.wait_all;" ::: "memory");
+#endif
+        const uint64_t pl = s->prev_last, t0 = s->t0;
+        const int pc = s->prev_cur;
+        if (pl && (unsigned)pc < (unsigned)kPhases && t0 > pl)
+            atomicAdd((unsigned long long*)&ph->ns[pc], (unsigned long long)(t0 - pl));
+        ph->last = s->t;
+        ph->cur = s->cur;
+    }
+};
+
 // One instance as the kernels see it.
 struct InstDev {
     int32_t m, n, ldc;        // rows, columns, padded row pitch (multiple of 4)
@@ -142,6 +234,8 @@ struct Ctx {
     int32_t* csr_adj;     // 2V
     int32_t* order;       // V  (BFS order of the start tree)
     int32_t* uf;          // V  union-find
+    // phase clock of the plain solver (null elsewhere; see PhaseClock)
+    PhaseClock* ph;
 };
 
 // Size of the pointer-jumping scratch block of V vertices.

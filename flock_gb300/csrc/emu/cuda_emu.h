@@ -128,6 +128,25 @@ inline unsigned emu_reduce(unsigned v, bool take_max) {
 inline unsigned __reduce_min_sync(unsigned, unsigned v) { return emu_reduce(v, false); }
 inline unsigned __reduce_max_sync(unsigned, unsigned v) { return emu_reduce(v, true); }
 
+// Warp sum and ballot: every lane of the caller's warp gets the result.
+inline unsigned emu_gather(unsigned v, int how) {
+    emu::Cta* c = emu::cta();
+    emu::warp_sync_at(-8);
+    c->xchg[threadIdx.x] = v;
+    emu::warp_sync_at(-9);
+    const unsigned w0 = threadIdx.x & ~31u;
+    unsigned r = 0;
+    for (unsigned l = 0; l < 32; l++) {
+        const unsigned x = (unsigned)c->xchg[w0 + l];
+        r += how == 0 ? x : (x ? 1u << l : 0u);
+    }
+    emu::warp_sync_at(-10);
+    return r;
+}
+inline unsigned __reduce_add_sync(unsigned, unsigned v) { return emu_gather(v, 0); }
+inline unsigned __ballot_sync(unsigned, int p) { return emu_gather(p ? 1u : 0u, 1); }
+inline int __popc(unsigned x) { return __builtin_popcount(x); }
+
 template <class T, class U> inline T atomicAdd(T* p, U v) { return std::atomic_ref<T>(*p).fetch_add((T)v); }
 template <class T, class U> inline T atomicOr(T* p, U v) { return std::atomic_ref<T>(*p).fetch_or((T)v); }
 template <class T, class U> inline T atomicExch(T* p, U v) { return std::atomic_ref<T>(*p).exchange((T)v); }

@@ -30,6 +30,7 @@ struct BatchArgs {
     int32_t bfs_method, mode, max_rounds;
     int32_t light;              // 1: stage only the per-step tree arrays (largest buckets)
     int32_t pricing;            // Scalars::pricing of every instance
+    PhaseClock* ph;             // phase clock (the plain solver's one-launch form only; null otherwise)
 };
 
 // A served request's device region: byte offsets of its arrays (256-aligned).
@@ -91,6 +92,7 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.csr_adj = (int32_t*)k.G(8 * v);
     c.order = (int32_t*)k.G(4 * v);
     c.uf = (int32_t*)k.G(4 * v);
+    c.ph = nullptr;
     if (smem_bytes) *smem_bytes = k.so;
     if (global_bytes) *global_bytes = (k.go + 255) & ~size_t(255);
 }

@@ -36,6 +36,8 @@ namespace flock {
 // ------------------------------------------------------------ kernels ------
 __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const int2* rbook, const int2* cbook) {
     __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_BFS);
     if (bfs_method == FLOCK_BFS_VOGEL) {
         vogel_cta(c, bs);
     } else if (bfs_method == FLOCK_BFS_VOGEL_DEVICE) {
@@ -46,8 +48,11 @@ __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const 
     }
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
     sf_init_cta(c, bs);
+    ps.mark(PH_DUAL);
     if (!c.sc->done) tree_build_cta<kJumpPlain>(c, bs);
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
+    __syncthreads();
+    ps.mark(PH_SWEEP);   // the first round's sweep
 }
 
 __global__ void __launch_bounds__(1024, 1) k_vogel_only(Ctx c) {
@@ -146,30 +151,182 @@ __device__ __forceinline__ void sweep_part(const Ctx& c, int tile, int ntile, co
     }
 }
 
-// Grid-wide sweep kernel (blockIdx.x = tile + ntile * row_group).  gate:
-// run only when *gate == gate_val (null: always).
-__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(Ctx c, int tile, int ntile, const int32_t* rows,
-                                                           const int32_t* gate, int gate_val) {
-    if (c.sc->done) return;
-    if (gate && *gate != gate_val) return;
-    __shared__ __align__(16) int32_t vt[kSweepTile];
-    sweep_part(c, tile, ntile, rows, vt, (int)blockIdx.x, (int)gridDim.x);
+// ------------------------------------------------------ bulk-copy sweep ---
+// The full reduced-cost sweep as a bulk-copy pipeline, one block per SM.
+// blockIdx.x = tile + ntile * row_group; a block stages the int32 duals of
+// its column tile and takes the work units (row i, segment of kBulkSeg
+// columns) u = row_group, row_group + nrg, ... in order.  Lane 0 of warp 0
+// streams them with cp.async.bulk into a ring of kBulkStages shared buffers,
+// each with a `full` barrier (the copy's transaction bytes) and an `empty`
+// barrier (released by the consumer); consumer warp w takes units w-1,
+// w-1+kBulkCons, ... and reduces c - v from shared memory into the row key
+// (atomicMin into row_best, which holds kNoKey before the sweep).  Every wait
+// is bounded: a wait that runs out records a failed check (the solve stops
+// with ST_TREE_CORRUPT), and the producer still waits (bounded) for its
+// copies in flight before the block exits.
+constexpr int kBulkSeg = 2048;                     // columns per unit: 8 KB of int32 costs
+constexpr int kBulkStages = 24;                    // a multiple of kBulkCons: warp w owns stages w-1 (+ kBulkCons ...)
+constexpr int kBulkCons = 12;                      // consumer warps; warp 0 produces
+constexpr int kBulkThreads = 32 * (kBulkCons + 1);
+constexpr size_t kBulkSmem = (size_t)kBulkStages * kBulkSeg * 4 + (size_t)kSweepTile * 4;
+constexpr long long kSpinLimit = 1ll << 22;        // polls of an mbarrier before its wait fails
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Wait for the phase of the given parity to complete; false after kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    for (long long it = 0; it < kSpinLimit; it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(b)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+// Global -> shared bulk copy completing on `bar` (addresses 16-byte aligned,
+// bytes a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 
-// Launch shape of k_sweep for an m x n instance: column tiles of at most
-// kSweepTile, two blocks per SM in total, no more blocks than work units.
+// Unit k of this block: row i and tile-local columns [a, b).
+struct BulkUnit {
+    int i, a, b;
+};
+__device__ __forceinline__ BulkUnit bulk_unit(long long k, int rg, int nrg, int nseg, int jn) {
+    const long long u = rg + k * nrg;
+    BulkUnit w;
+    w.i = (int)(u / nseg);
+    w.a = (int)(u % nseg) * kBulkSeg;
+    w.b = min(jn, w.a + kBulkSeg);
+    return w;
+}
+
+__global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int ntile) {
+    __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
+    __shared__ PhaseLocal phl;
+    extern __shared__ __align__(128) unsigned char bulk_smem[];
+    PhaseScope ps(c.ph, &phl, PH_SWEEP);
+    if (c.sc->done) { ps.idle(); return; }
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n;
+    const int t = (int)blockIdx.x % ntile, rg = (int)blockIdx.x / ntile, nrg = (int)gridDim.x / ntile;
+    const int j0 = t * tile, jn = min(tile, n - j0);
+    const int nseg = (jn + kBulkSeg - 1) / kBulkSeg;
+    const long long units = (long long)m * nseg;
+    const long long mine = units > rg ? (units - rg + nrg - 1) / nrg : 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (!c.sc->narrow) {      // wide duals: exact int64 keys per element, every warp over the units
+        for (long long k = warp; k < mine; k += kBulkCons + 1) {
+            const BulkUnit w = bulk_unit(k, rg, nrg, nseg, jn);
+            const uint64_t key = row_best_exact(I.cost + (size_t)w.i * I.ldc, c.pot[w.i], c.pot + m, j0 + w.a, j0 + w.b);
+            if (lane == 0) atomicMin((unsigned long long*)&c.row_best[w.i], (unsigned long long)key);
+        }
+        return;
+    }
+    int32_t* ring = reinterpret_cast<int32_t*>(bulk_smem);
+    int32_t* vt = ring + (size_t)kBulkStages * kBulkSeg;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kBulkStages; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    long long issued = 0;
+    auto issue = [&](long long k) {
+        const int st = (int)(k % kBulkStages);
+        const BulkUnit w = bulk_unit(k, rg, nrg, nseg, jn);
+        const uint32_t bytes = (uint32_t)(((w.b - w.a + 3) & ~3) * 4);   // within the row pitch (ldc = ceil4(n))
+        mbar_expect_tx(&full[st], bytes);
+        bulk_g2s(ring + (size_t)st * kBulkSeg, I.cost + (size_t)w.i * I.ldc + j0 + w.a, bytes, &full[st]);
+    };
+    if (threadIdx.x == 0)     // the first ring's worth streams while the duals are staged
+        for (; issued < mine && issued < kBulkStages; issued++) issue(issued);
+    for (int jj = threadIdx.x; jj < jn; jj += blockDim.x) vt[jj] = c.v32[j0 + jj];
+    __syncthreads();
+    if (warp == 0) {
+        if (lane != 0) return;
+        bool ok = true;
+        for (; issued < mine; issued++) {
+            const long long k = issued;
+            if (!mbar_wait(&empty[k % kBulkStages], (uint32_t)(((k / kBulkStages) & 1) ^ 1))) { ok = false; break; }
+            issue(k);
+        }
+        if (!ok) fail_check(c.sc, 30);
+        // every copy this block issued has landed before it exits
+        for (long long k = issued > kBulkStages ? issued - kBulkStages : 0; k < issued; k++)
+            if (!mbar_wait(&full[k % kBulkStages], (uint32_t)((k / kBulkStages) & 1))) fail_check(c.sc, 31);
+        return;
+    }
+    for (long long k = warp - 1; k < mine; k += kBulkCons) {
+        const int st = (int)(k % kBulkStages);
+        if (!mbar_wait(&full[st], (uint32_t)((k / kBulkStages) & 1))) {
+            if (lane == 0) fail_check(c.sc, 32);
+            return;
+        }
+        const BulkUnit w = bulk_unit(k, rg, nrg, nseg, jn);
+        const int64_t ui = c.pot[w.i];                 // used after the reduction: its latency overlaps it
+        const int32_t* src = ring + (size_t)st * kBulkSeg;
+        const int4* s4 = reinterpret_cast<const int4*>(src);
+        const int4* v4 = reinterpret_cast<const int4*>(vt + w.a);
+        const int nq = (w.b - w.a) >> 2;
+        int32_t bv = INT32_MAX, bj = INT32_MAX;
+        const int jb = j0 + w.a;
+        #pragma unroll 4
+        for (int q = lane; q < nq; q += 32) min4(bv, bj, s4[q], v4[q], jb + 4 * q);
+        if (lane < ((w.b - w.a) & 3)) {
+            const int jl = 4 * nq + lane;
+            const int32_t tv = src[jl] - vt[w.a + jl];
+            if (tv < bv) { bv = tv; bj = jb + jl; }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);       // the stage is free for the producer
+        // the row key as narrow_row_key forms it, the winning column's dual
+        // read from the staged tile
+        const uint64_t kk = warp_min_u64(pack_i32(bv, (uint32_t)bj));
+        const int jw = (int)key_idx(kk);
+        const int64_t r = (int64_t)key_val(kk) - ui;
+        const uint64_t key = vt[jw - j0] == kDead32 || r < INT32_MIN
+                                 ? row_best_exact(I.cost + (size_t)w.i * I.ldc, ui, c.pot + m, jb, j0 + w.b)
+                                 : pack_i32(clamp32(r), (uint32_t)jw);
+        if (lane == 0) atomicMin((unsigned long long*)&c.row_best[w.i], (unsigned long long)key);
+    }
+}
+
+// Launch shape of the grid-round sweeps (k_gsweep) for an m x n instance:
+// column tiles of at most kSweepTile, two blocks per SM in total, no more
+// blocks than work units.  bulk_shape: k_sweep's, one block per SM.
 static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile);
+static void bulk_shape(int m, int n, int* grid, int* tile, int* ntile);
 
 __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
     __shared__ BlockScratch bs;
-    if (c.sc->done) return;
-    pivot_round_cta<kJumpPlain>(c, bs);
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_SWEEP);   // the entering choice is part of pricing
+    if (c.sc->done) { ps.idle(); return; }
+    pivot_round_cta<kJumpPlain>(c, bs, false, kNoKey, &ps);
     if (threadIdx.x == 0) {
         c.sc->rounds++;
         if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
     }
     __syncthreads();
-    if (!c.sc->done && c.sc->stale) tree_build_cta<kJumpPlain>(c, bs);
+    if (!c.sc->done && c.sc->stale) {
+        ps.mark(PH_DUAL);
+        tree_build_cta<kJumpPlain>(c, bs);
+    }
+    ps.mark(PH_SWEEP);   // the key reset and the next round's sweep
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
 }
 
@@ -238,16 +395,13 @@ __device__ void grid_choose(const Ctx& c, GridPivot* gp, BlockScratch& bs, bool 
 // Cycle membership by intervals, each side's smallest decreasing flow, and
 // both cycle chains by distance from their endpoint with their flows
 // (path[i] / pflow[i] for the k side, path[V-1-i] / pflow[V-1-i] for the l
-// side, as single_pivot_iv records them).
-__device__ void grid_member(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
+// side, as single_pivot_iv records them), over the vertices v0, v0 + stride,
+// ...  (iv: the current interval buffer; dk, dl: the endpoints' depths).
+__device__ __forceinline__ void member_slice(const Ctx& c, const int2* iv, int k, int l, int dk, int dl, int v0,
+                                             int stride, uint64_t& mk, uint64_t& ml) {
     const int m = c.I.m, V = m + c.I.n;
-    const int k = (int)key_idx(gp->best);
-    const int l = m + (int)key_idx(c.row_best[k]);
-    const int2* iv = iv_now(c, V);
     const int pk = iv[k].x, pl = iv[l].x;
-    const int dk = c.depth[k], dl = c.depth[l];
-    uint64_t mk = kNoKey, ml = kNoKey;
-    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
+    for (int v = v0; v < V; v += stride) {
         int side = 0;
         if (c.parent[v] >= 0) {
             const int2 w = iv[v];
@@ -265,12 +419,39 @@ __device__ void grid_member(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
         if (side == 1 && v < m) { const uint64_t o = oflow(f); mk = o < mk ? o : mk; }
         if (side == 2 && v >= m) { const uint64_t o = oflow(f); ml = o < ml ? o : ml; }
     }
+}
+
+__device__ void grid_member(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
+    const int m = c.I.m, V = m + c.I.n;
+    const int k = (int)key_idx(gp->best);
+    const int l = m + (int)key_idx(c.row_best[k]);
+    uint64_t mk = kNoKey, ml = kNoKey;
+    member_slice(c, iv_now(c, V), k, l, c.depth[k], c.depth[l], bid * blockDim.x + threadIdx.x, nb * blockDim.x,
+                 mk, ml);
     mk = block_min_u64(mk, bs);
     ml = block_min_u64(ml, bs);
     if (threadIdx.x == 0) {
         if (mk != kNoKey) atomicMin((unsigned long long*)&gp->mk, (unsigned long long)mk);
         if (ml != kNoKey) atomicMin((unsigned long long*)&gp->ml, (unsigned long long)ml);
     }
+}
+
+// This thread's leaving-edge candidate over its vertices: among the cycle
+// edges of the side whose minimum flow fmin is smaller (l side on ties), the
+// (depth << 32 | child) keys with that flow -- the l side keeps the
+// shallowest (minimum), the k side the deepest (maximum; 0 = none).
+__device__ __forceinline__ uint64_t pick_slice(const Ctx& c, bool lside, uint64_t fmin, int v0, int stride) {
+    const int m = c.I.m, V = m + c.I.n;
+    uint64_t pick = lside ? kNoKey : 0ull;
+    for (int v = v0; v < V; v += stride) {
+        const uint64_t sd = c.side[v];
+        if ((lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) && oflow(c.flow[v]) == fmin) {
+            const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
+            if (lside) pick = key < pick ? key : pick;
+            else pick = key > pick ? key : pick;
+        }
+    }
+    return pick;
 }
 
 // The leaving edge among the minima: k side the deepest, l side the shallowest.
@@ -282,15 +463,7 @@ __device__ void grid_pick(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid
         if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 16);
         return;
     }
-    uint64_t pick = lside ? kNoKey : 0ull;
-    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
-        const uint64_t sd = c.side[v];
-        if ((lside ? (sd == 2 && v >= m) : (sd == 1 && v < m)) && oflow(c.flow[v]) == fmin) {
-            const uint64_t key = ((uint64_t)(uint32_t)c.depth[v] << 32) | (uint32_t)v;
-            if (lside) pick = key < pick ? key : pick;
-            else pick = key > pick ? key : pick;
-        }
-    }
+    uint64_t pick = pick_slice(c, lside, fmin, bid * blockDim.x + threadIdx.x, nb * blockDim.x);
     pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
     if (threadIdx.x == 0) {
         if (lside && pick != kNoKey) atomicMin((unsigned long long*)&gp->ql, (unsigned long long)pick);
@@ -326,37 +499,36 @@ __device__ void grid_pick(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid
     }
 }
 
-// The tree update of single_pivot_iv over the grid: the cycle's flows, new
-// intervals into the other half of iv, depths and duals of the re-hung
-// subtree, the reversed path's parents and flows; every row key cleared for
-// the next sweep.  The last block to finish ends the round: the current
-// interval buffer, the int32 dual flag, the pivot count and the round cap.
-__device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
+// The pivot as the update step needs it (fixed before anything it depends
+// on changes).
+struct PivotParams {
+    int32_t t, e, other, de, dother, eside;
+    int64_t th, r;
+    int2 Q, O;
+};
+
+// The tree update of single_pivot_iv over the vertices v0, v0 + stride, ...:
+// the cycle's flows, new intervals into ivB (old ones read from ivA), depths
+// and duals of the re-hung subtree, the reversed path's parents and flows.
+// Adds the change of the int32-window miss count to dwide; sets bad on a
+// failed index check.
+__device__ __forceinline__ void update_slice(const Ctx& c, const PivotParams& pp, const int2* ivA, int2* ivB, int v0,
+                                             int stride, int& dwide, int& bad) {
     const int m = c.I.m, V = m + c.I.n;
-    const int t = gp->t;
-    if (!gp->ok || !FLOCK_IN(t, V)) {
-        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
-        return;
-    }
-    const bool lside = gp->eside == 2;
+    const int t = pp.t;
+    const bool lside = pp.eside == 2;
     const int base = lside ? V - 1 : 0, dir = lside ? -1 : 1;   // e's chain entry i at path[base + dir * i]
-    const int par = c.sc->ivp;
-    const int2* ivA = c.iv + (par ? V : 0);
-    int2* ivB = c.iv + (par ? 0 : V);
-    const int2 Q = gp->Q, O = gp->O;
+    const int2 Q = pp.Q, O = pp.O;
     const int P = Q.x, s = Q.y;
     const int ins = O.x - (O.x >= P + s ? s : 0) + 1;
-    const int dnew = gp->dother + 1 - gp->de;
-    const int other = gp->other;
-    const bool erow = gp->e < m;
-    const int64_t r = gp->r, th = gp->th;
-    const int eside = gp->eside;
+    const int dnew = pp.dother + 1 - pp.de;
+    const int other = pp.other;
+    const bool erow = pp.e < m;
+    const int64_t r = pp.r, th = pp.th;
+    const int eside = pp.eside;
     const int32_t* path = c.path;
     const int64_t* pflow = c.pflow;
-    if (threadIdx.x == 0) bs.i[7] = 0;
-    __syncthreads();
-    int dwide = 0, bad = 0;
-    for (int v = bid * blockDim.x + threadIdx.x; v < V; v += nb * blockDim.x) {
+    for (int v = v0; v < V; v += stride) {
         if (c.parent[v] == -2) continue;
         const int2 w = ivA[v];
         const int side = c.side[v];
@@ -407,6 +579,26 @@ __device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
         }
         ivB[v] = nw;
     }
+}
+
+// The tree update over the grid, every row key cleared for the next sweep.
+// The last block to finish ends the round: the current interval buffer, the
+// int32 dual flag, the pivot count and the round cap.
+__device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int bid, int nb) {
+    const int m = c.I.m, V = m + c.I.n;
+    if (!gp->ok || !FLOCK_IN(gp->t, V)) {
+        if (bid == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
+        return;
+    }
+    PivotParams pp;
+    pp.t = gp->t; pp.e = gp->e; pp.other = gp->other; pp.de = gp->de; pp.dother = gp->dother;
+    pp.eside = gp->eside; pp.th = gp->th; pp.r = gp->r; pp.Q = gp->Q; pp.O = gp->O;
+    const int par = c.sc->ivp;
+    if (threadIdx.x == 0) bs.i[7] = 0;
+    __syncthreads();
+    int dwide = 0, bad = 0;
+    update_slice(c, pp, c.iv + (par ? V : 0), c.iv + (par ? 0 : V), bid * blockDim.x + threadIdx.x,
+                 nb * blockDim.x, dwide, bad);
     for (int i = bid * blockDim.x + threadIdx.x; i < m; i += nb * blockDim.x) c.row_best[i] = kNoKey;
     if (bad) fail_check(c.sc, 24);
     if (dwide) atomicAdd(&bs.i[7], dwide);
@@ -428,7 +620,15 @@ __device__ void grid_update(const Ctx& c, GridPivot* gp, BlockScratch& bs, int b
 
 // Step kernels of a grid round.  Each returns at once when the solve is
 // done (one thread reads the flag, so the whole block agrees).
-#define FLOCK_GRID_STEP_PROLOGUE() \
+#define FLOCK_GRID_STEP_PROLOGUE()                                 \
+    if (__syncthreads_or(threadIdx.x == 0 && c.sc->done)) {        \
+        ps.idle();                                                 \
+        return;                                                    \
+    }
+
+// The grid sweeps keep every register for the stream (no phase scope of
+// their own): the round's previous launch leaves the sweep phase running.
+#define FLOCK_SWEEP_STEP_PROLOGUE() \
     if (__syncthreads_or(threadIdx.x == 0 && c.sc->done)) return
 
 // Partial pricing decision of the round (every block computes it from the
@@ -441,7 +641,7 @@ __device__ __forceinline__ bool grid_full_round(const Ctx& c) {
 // Round start: the sweep this round's pricing asks for.
 __global__ void __launch_bounds__(kSweepThreads, 2) k_gsweep(Ctx c, GridPivot* gp, int tile, int ntile) {
     __shared__ __align__(16) int32_t vt[kSweepTile];
-    FLOCK_GRID_STEP_PROLOGUE();
+    FLOCK_SWEEP_STEP_PROLOGUE();
     const bool full = grid_full_round(c);
     if (blockIdx.x == 0 && threadIdx.x == 0) gp->full = full ? 1 : 0;
     sweep_part(c, tile, ntile, full ? nullptr : c.prow, vt, (int)blockIdx.x, (int)gridDim.x);
@@ -451,7 +651,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_gsweep(Ctx c, GridPivot* g
 // key (every block checks the same keys).
 __global__ void __launch_bounds__(kSweepThreads, 2) k_gsweep_rest(Ctx c, GridPivot* gp, int tile, int ntile) {
     __shared__ __align__(16) int32_t vt[kSweepTile];
-    FLOCK_GRID_STEP_PROLOGUE();
+    FLOCK_SWEEP_STEP_PROLOGUE();
     if (grid_full_round(c)) return;
     const int m = c.I.m, pn = c.sc->pp_n;
     int neg = 0;
@@ -466,31 +666,279 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_gsweep_rest(Ctx c, GridPiv
 
 __global__ void __launch_bounds__(1024, 1) k_gchoose(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_SWEEP);   // the entering choice is part of pricing
     FLOCK_GRID_STEP_PROLOGUE();
     const bool full = gp->full != 0;
     grid_choose(c, gp, bs, full, full && c.sc->pricing);
 }
 
+// The full round ahead of the cluster rounds: the entering cell over every
+// row (the bulk sweep just priced them all) and the next candidate rows.
+__global__ void __launch_bounds__(1024, 1) k_gchoose_all(Ctx c, GridPivot* gp) {
+    __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_SWEEP);
+    FLOCK_GRID_STEP_PROLOGUE();
+    grid_choose(c, gp, bs, true, c.sc->pricing != 0);
+}
+
 __global__ void __launch_bounds__(256) k_gmember(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_CYCLE);
     FLOCK_GRID_STEP_PROLOGUE();
     grid_member(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
 }
 
 __global__ void __launch_bounds__(256) k_gpick(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_ADJUST);   // leaving edge: the reference's adjustment step
     FLOCK_GRID_STEP_PROLOGUE();
     grid_pick(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
 }
 
 __global__ void __launch_bounds__(256) k_gupdate(Ctx c, GridPivot* gp) {
     __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_ADJUST);
     FLOCK_GRID_STEP_PROLOGUE();
     grid_update(c, gp, bs, (int)blockIdx.x, (int)gridDim.x);
+    ps.mark(PH_SWEEP);   // the next round's sweeps
+}
+
+// ------------------------------------------------- cluster pivot rounds ---
+// The partial-pricing rounds of the grid path in ONE launch of a single
+// thread-block cluster (up to kClusterMax CTAs of kCRoundThreads threads on
+// one GPC), the hardware cluster barrier in place of the kernel boundaries
+// of the six-kernel round.  A round:
+//   sweep of the candidate rows (their keys hold kNoKey)          barrier 1
+//   the entering cell (every CTA reduces the same keys), snapshots of the
+//   values the update will change, membership and side minima of each
+//   CTA's vertex slice                                             barrier 2
+//   the leaving edge's candidates of each slice                    barrier 3
+//   the pivot's parameters (every CTA reduces the same slots), the in-place
+//   update of each slice                                           barrier 0
+// with the same steps and tie rules as grid_member / grid_pick /
+// grid_update, so the pivot sequence is the six-kernel rounds'.  The rounds
+// stop -- every CTA decides from the same values, written before a barrier
+// and not rewritten until after the next one -- when the candidates hold no
+// negative key (the next full sweep decides optimality), when pp_refresh
+// rounds have passed since the last full sweep, at the round cap, or after
+// a failed check.  What the CTAs share lives in global memory in per-CTA
+// slots (ClusterPivot), so nothing is reset between rounds; the solve's
+// scalars are read at the start and written back by CTA 0 at the end.  The
+// cluster barrier waits for every thread of the cluster that has not
+// exited, and every loop here is bounded, so the barriers cannot hang.
+constexpr int kCRoundThreads = 1024;
+constexpr int kClusterMax = 16;
+
+struct ClusterPivot {
+    uint64_t mk[kClusterMax], ml[kClusterMax];     // member step: each CTA's side minima
+    uint64_t pick[kClusterMax];                    // pick step: each CTA's leaving-edge candidate
+    int32_t dwide[kClusterMax];                    // update step: change of the int32-window miss count
+    int32_t abort[2];                              // a failed check in the round of that parity
+};
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ int cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return (int)r;
+}
+__device__ __forceinline__ int cluster_ctas() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return (int)r;
+}
+
+// Sweep of the candidate rows prow[0..pn) over the cluster: (row, segment of
+// kSegCols columns) units, one warp each, keys into row_best by atomicMin.
+__device__ void cluster_cand_sweep(const Ctx& c, int pn, bool narrow, int rank, int nctas, int* bad) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n;
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const int gw = rank * wpb + (threadIdx.x >> 5), nw = nctas * wpb;
+    const int nseg = (n + kSegCols - 1) / kSegCols;
+    const int units = pn * nseg;
+    const int4* v4 = reinterpret_cast<const int4*>(c.v32);
+    for (int u = gw; u < units; u += nw) {
+        const int i = c.prow[u / nseg], sg = u % nseg;
+        if (!FLOCK_IN(i, m)) { *bad = 1; continue; }
+        const int a = sg * kSegCols, b = min(n, a + kSegCols);
+        uint64_t key;
+        if (!narrow) {
+            key = row_best_exact(I.cost + (size_t)i * I.ldc, c.pot[i], c.pot + m, a, b);
+        } else {
+            const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
+            int32_t bv = INT32_MAX, bj = INT32_MAX;
+            const int qa = a >> 2, qb = b >> 2;
+            for (int q = qa + lane; q < qb; q += 32) min4(bv, bj, row[q], v4[q], 4 * q);
+            if (lane < b - 4 * qb) {
+                const int j = 4 * qb + lane;
+                const int32_t tv = I.cost[(size_t)i * I.ldc + j] - c.v32[j];
+                if (tv < bv) { bv = tv; bj = j; }
+            }
+            key = narrow_row_key(c, i, a, b, bv, bj);
+        }
+        if (lane == 0) atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)key);
+    }
+}
+
+__global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivot* cp) {
+    __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    __shared__ uint64_t s_red[2];
+    PhaseScope ps(c.ph, &phl, PH_SWEEP);
+    const int rank = cluster_rank(), nctas = cluster_ctas();
+    const int m = c.I.m, V = m + c.I.n;
+    const uint32_t ncols = (uint32_t)c.I.n;
+    // the solve's scalars, read by every CTA before any CTA can change them
+    const int done0 = c.sc->done;
+    const int pn = min(max(c.sc->pp_n, 0), kPPRows);
+    const int refresh = max(c.sc->pp_refresh, 1);
+    const int max_rounds = c.sc->max_rounds;
+    int rounds = c.sc->rounds, age = c.sc->pp_age, pivots = c.sc->pivots, ivp = c.sc->ivp, nwide = c.sc->nwide;
+    const int pivots0 = pivots;
+    const bool partial = c.sc->pricing != 0;
+    if (rank == 0 && threadIdx.x == 0) { cp->abort[0] = 0; cp->abort[1] = 0; }
+    if (threadIdx.x == 0) cp->dwide[rank] = 0;
+    const int v0 = rank * blockDim.x + threadIdx.x, stride = nctas * blockDim.x;
+    enum { kRun, kExhausted, kAged, kCapped, kFailed };
+    int why = kRun;
+    for (int r = 0;; r++) {
+        cluster_sync_all();                                      // barrier 0
+        if (r > 0) {
+            for (int q = 0; q < nctas; q++) nwide += cp->dwide[q];
+            if (cp->abort[(r - 1) & 1]) { why = kFailed; break; }
+        }
+        if (done0 || !partial || pn <= 0) { why = kAged; break; }
+        if (rounds >= max_rounds) { why = kCapped; break; }
+        if (age >= refresh) { why = kAged; break; }
+        ps.mark(PH_SWEEP);
+        int bad = 0;
+        cluster_cand_sweep(c, pn, nwide == 0, rank, nctas, &bad);
+        if (bad) { fail_check(c.sc, 19); cp->abort[r & 1] = 1; }
+        cluster_sync_all();                                      // barrier 1
+        if (rank == 0 && threadIdx.x == 0 && r > 0) cp->abort[(r - 1) & 1] = 0;   // read by all before barrier 1
+        // the entering cell: the smallest (reduced cost, row) among the candidates
+        uint64_t best = kNoKey;
+        for (int t = threadIdx.x; t < pn; t += blockDim.x) {
+            const int i = c.prow[t];
+            if (!FLOCK_IN(i, m)) continue;
+            const uint64_t key = c.row_best[i];
+            if (key != kNoKey && key_val(key) < 0 && key_idx(key) < ncols) {
+                const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
+                best = P < best ? P : best;
+            }
+        }
+        best = block_min_u64(best, bs);
+        if (best == kNoKey) { why = kExhausted; break; }
+        rounds++;
+        age++;
+        ps.mark(PH_CYCLE);
+        const int k = (int)key_idx(best);
+        const int l = m + (int)key_idx(c.row_best[k]);
+        const int2* ivA = c.iv + (ivp ? V : 0);
+        int2* ivB = c.iv + (ivp ? 0 : V);
+        // values the update changes, read before any CTA's update of this round
+        const int dk = c.depth[k], dl = c.depth[l];
+        const int64_t r_enter = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
+        uint64_t mk = kNoKey, ml = kNoKey;
+        member_slice(c, ivA, k, l, dk, dl, v0, stride, mk, ml);
+        mk = block_min_u64(mk, bs);
+        ml = block_min_u64(ml, bs);
+        if (threadIdx.x == 0) { cp->mk[rank] = mk; cp->ml[rank] = ml; }
+        cluster_sync_all();                                      // barrier 2
+        ps.mark(PH_ADJUST);
+        if (threadIdx.x == 0) {
+            uint64_t a = kNoKey, b = kNoKey;
+            for (int q = 0; q < nctas; q++) { a = min(a, cp->mk[q]); b = min(b, cp->ml[q]); }
+            s_red[0] = a; s_red[1] = b;
+        }
+        __syncthreads();
+        const uint64_t gmk = s_red[0], gml = s_red[1];
+        const bool lside = gml <= gmk;
+        const uint64_t fmin = lside ? gml : gmk;
+        uint64_t pick = fmin == kNoKey ? (lside ? kNoKey : 0ull) : pick_slice(c, lside, fmin, v0, stride);
+        pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
+        if (threadIdx.x == 0) cp->pick[rank] = pick;
+        cluster_sync_all();                                      // barrier 3
+        if (threadIdx.x == 0) {
+            uint64_t q64 = lside ? kNoKey : 0ull;
+            for (int q = 0; q < nctas; q++) {
+                const uint64_t x = cp->pick[q];
+                q64 = lside ? min(q64, x) : max(q64, x);
+            }
+            s_red[0] = q64;
+        }
+        __syncthreads();
+        const uint64_t q64 = s_red[0];
+        const int q = (int)(uint32_t)q64;
+        const int e = lside ? l : k, other = lside ? k : l;
+        const int de = lside ? dl : dk;
+        const int t = fmin != kNoKey && (lside ? q64 != kNoKey : q64 != 0) && FLOCK_IN(q, V)
+                          ? de - (int)(uint32_t)(q64 >> 32) : -1;
+        const int slot = lside ? V - 1 - t : t;
+        if (!FLOCK_IN(t, V) || c.path[slot] != q) {               // the same outcome in every CTA
+            if (rank == 0 && threadIdx.x == 0) fail_check(c.sc, 17);
+            why = kFailed;
+            break;
+        }
+        PivotParams pp;
+        pp.t = t; pp.e = e; pp.other = other; pp.de = de; pp.dother = lside ? dk : dl;
+        pp.eside = lside ? 2 : 1;
+        pp.th = (int64_t)(fmin ^ 0x8000000000000000ull);
+        pp.r = r_enter;
+        pp.Q = ivA[q];            // intervals of the old buffer: no CTA writes it this round
+        pp.O = ivA[other];
+        if (threadIdx.x == 0) bs.i[7] = 0;
+        __syncthreads();
+        int dwide = 0, ubad = 0;
+        update_slice(c, pp, ivA, ivB, v0, stride, dwide, ubad);
+        if (ubad) { fail_check(c.sc, 24); cp->abort[r & 1] = 1; }
+        if (dwide) atomicAdd(&bs.i[7], dwide);
+        __syncthreads();
+        if (threadIdx.x == 0) cp->dwide[rank] = bs.i[7];
+        // the candidates' keys, read by every CTA before barrier 2, cleared for the next sweep
+        if (rank == 0)
+            for (int t2 = threadIdx.x; t2 < pn; t2 += blockDim.x) {
+                const int i = c.prow[t2];
+                if (FLOCK_IN(i, m)) c.row_best[i] = kNoKey;
+            }
+        ivp ^= 1;
+        pivots++;
+    }
+    // every CTA leaves the loop at the same point; CTA 0 writes the scalars back
+    if (why == kExhausted) {
+        cluster_sync_all();          // every CTA has read the candidate keys
+        if (rank == 0)
+            for (int t2 = threadIdx.x; t2 < pn; t2 += blockDim.x) {
+                const int i = c.prow[t2];
+                if (FLOCK_IN(i, m)) c.row_best[i] = kNoKey;
+            }
+    }
+    if (rank == 0 && threadIdx.x == 0 && !done0) {
+        c.sc->rounds = rounds;
+        c.sc->pp_age = why == kExhausted ? refresh : age;     // the next round sweeps every row
+        c.sc->pivots = pivots;
+        c.sc->ivp = ivp;
+        c.sc->nwide = nwide;
+        c.sc->narrow = nwide == 0;
+        if (pivots > pivots0) c.sc->last_winners = 1;
+        if (why == kCapped) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
+    }
+    ps.mark(PH_SWEEP);       // the next full round's sweep
 }
 
 __global__ void __launch_bounds__(1024, 1) k_finalize(Ctx c) {
     __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    PhaseScope ps(c.ph, &phl, PH_IDLE);   // closes the loop's last phase
     if (c.sc->status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE)) return;
     finalize_cta(c, bs);
     certify_flows_cta(c, bs);
@@ -734,7 +1182,7 @@ inline bool stage_light(int maxV, int maxM) { return staged_bytes(maxV, maxM, fa
 // round); single pivots keep it current, multi-pivot rounds mark it stale.
 template <bool kLight>
 __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs, unsigned char* smem,
-                            int max_here) {
+                            int max_here, PhaseScope* ps = nullptr) {
     Ctx g;
     batch_ctx(a, d, g);
     Ctx c = g;
@@ -744,13 +1192,17 @@ __device__ void brounds_one(const BatchArgs& a, const BatchDesc& d, BlockScratch
     if (threadIdx.x == 0) c.sc->stale = 1;
     __syncthreads();
     for (int r = 0; r < max_here; r++) {
-        if (c.sc->stale) tree_build_cta(c, bs);
+        if (c.sc->stale) {
+            if (ps) ps->mark(PH_DUAL);
+            tree_build_cta(c, bs);
+        }
         if (!c.sc->done) {
+            if (ps) ps->mark(PH_SWEEP);
             uint64_t entering = kNoKey;
             const bool partial = c.sc->pricing != 0;
             if (partial) entering = sweep_partial_cta(c, bs);
             else sweep_cta(c);
-            pivot_round_cta(c, bs, partial, entering);
+            pivot_round_cta(c, bs, partial, entering, ps);
         }
         if (threadIdx.x == 0) {
             c.sc->rounds++;
@@ -828,6 +1280,33 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_bsolve(BatchArgs a) {
         bfinal_one(a, d, bs);
         publish_done(d);
     }
+}
+
+// The plain solver's one-launch form (instances below the grid-round size):
+// one CTA runs the persistent kernel's work on a single instance -- initial
+// solution, start tree, every pricing round with the tree staged in shared
+// memory, retrieval and the certificate -- and keeps the phase clock.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 1) k_solve_one(BatchArgs a) {
+    __shared__ BlockScratch bs;
+    __shared__ PhaseLocal phl;
+    extern __shared__ __align__(16) unsigned char smem[];
+    PhaseScope ps(a.ph, &phl, PH_BFS);
+    const BatchDesc d = a.desc[0];
+    if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); return; }
+    bsetup_one<true>(a, d, bs, smem);
+    if (!d.sc->done) {
+        if (a.light) brounds_one<true>(a, d, bs, smem, 1 << 30, &ps);
+        else brounds_one<false>(a, d, bs, smem, 1 << 30, &ps);
+    }
+    ps.mark(PH_IDLE);
+    bfinal_one(a, d, bs);
+}
+
+// Block size of the one-launch form by instance size.
+static int solve_one_threads(int V) { return V <= 512 ? 256 : 1024; }
+static const void* solve_one_fn(int threads) {
+    return threads <= 256 ? (const void*)k_solve_one<256> : (const void*)k_solve_one<1024>;
 }
 
 // The persistent kernel compiled for the block size: up to 256 threads four
@@ -1008,9 +1487,21 @@ int validate_instance(const flock_instance* I) {
     return FLOCK_OK;
 }
 
-// Scalars::mode of a pivot method: 0 sequential, 1 parallel, 2 switch.
+// Scalars::mode of a pivot method: 0 sequential, 1 parallel, 2 switch, 3
+// parallel stepping stone.
 static int pivot_mode(const flock_options& o) {
-    return o.pivot_method == FLOCK_PIVOT_SEQUENTIAL ? 0 : o.pivot_method == FLOCK_PIVOT_PARALLEL ? 1 : 2;
+    switch (o.pivot_method) {
+        case FLOCK_PIVOT_SEQUENTIAL: return 0;
+        case FLOCK_PIVOT_PARALLEL: return 1;
+        case FLOCK_PIVOT_SS: return 3;
+        default: return 2;
+    }
+}
+
+// Scalars::pricing of the options: partial pricing unless FULL was asked for
+// or the pivot method prices every cell (parallel stepping stone).
+static int pricing_of(const flock_options& o) {
+    return o.pricing == FLOCK_PRICING_PARTIAL && o.pivot_method != FLOCK_PIVOT_SS ? 1 : 0;
 }
 
 static int threads_for(int V) {
@@ -1023,7 +1514,12 @@ struct PlainSolver {
     std::mutex mu;
     DevBuf ws, cost, sd;
     DevBuf books;                   // "vam_device" Vogel: row and column books
+    DevBuf one;                     // one-launch form: working set, basis, duals, scalars, descriptor
+    HostBuf h_desc;                 // one-launch form: the descriptor's pinned staging
     GridPivot* gp = nullptr;        // grid pivot round state (large instances)
+    PhaseClock* ph = nullptr;       // device time per simplex phase
+    ClusterPivot* cp = nullptr;     // cluster rounds' per-CTA slots
+    int cluster_ctas = 0;           // CTAs of the cluster rounds (0: the six-kernel rounds only)
     HostBuf h_sc;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -1036,6 +1532,22 @@ struct PlainSolver {
         FLOCK_CK(h_sc.ensure(sizeof(Scalars)));
         FLOCK_CK(cudaFuncSetAttribute(k_books, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(sizeof(uint64_t) * 16384)));
+        for (int t : {256, 1024})
+            FLOCK_CK(cudaFuncSetAttribute(solve_one_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kStageSmemMax));
+        FLOCK_CK(cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBulkSmem));
+        // the largest cluster the cluster rounds can be launched with (one cluster)
+        cluster_ctas = 0;
+        if (cudaFuncSetAttribute(k_cround, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(kClusterMax);
+            cfg.blockDim = dim3(kCRoundThreads);
+            int cs = 0;
+            if (cudaOccupancyMaxPotentialClusterSize(&cs, (const void*)k_cround, &cfg) == cudaSuccess)
+                cluster_ctas = std::min(cs, kClusterMax);
+        }
+        if (cluster_ctas < 2) cluster_ctas = 0;
+        cudaGetLastError();
         init = true;
         return FLOCK_OK;
     }
@@ -1069,9 +1581,13 @@ struct PlainSolver {
         carve_ctx(probe, nullptr, V, m, nullptr, nullptr, nullptr, &gbytes);
         const size_t extra_off = al256(gbytes);
         const size_t out_bytes = al256((size_t)3 * V * 4);
-        FLOCK_CK(ws.ensure(extra_off + out_bytes + al256(sizeof(Scalars)) + al256(sizeof(GridPivot))));
+        FLOCK_CK(ws.ensure(extra_off + out_bytes + al256(sizeof(Scalars)) + al256(sizeof(GridPivot)) +
+                           al256(sizeof(PhaseClock)) + al256(sizeof(ClusterPivot))));
         carve_ctx(c, ws.as<uint8_t>(), V, m, nullptr, nullptr);
         gp = ws.as<GridPivot>(extra_off + out_bytes + al256(sizeof(Scalars)));
+        ph = ws.as<PhaseClock>(extra_off + out_bytes + al256(sizeof(Scalars)) + al256(sizeof(GridPivot)));
+        cp = ws.as<ClusterPivot>(extra_off + out_bytes + al256(sizeof(Scalars)) + al256(sizeof(GridPivot)) +
+                                 al256(sizeof(PhaseClock)));
         c.out_src = ws.as<int32_t>(extra_off);
         c.out_dst = c.out_src + V;
         c.out_qty = c.out_dst + V;
@@ -1114,6 +1630,101 @@ static void fill_flows_from_basis(int V, const int32_t* src, const int32_t* dst,
     for (int k = 0; k < V - 1; k++) if (qty[k] <= 0) flows[w++] = {src[k], dst[k], qty[k]};
 }
 
+static size_t instance_ws_bytes(int V, int m);
+
+// The plain solve of an instance below the grid-round size in ONE launch
+// (k_solve_one): costs and quantities already uploaded by prepare() (c.I);
+// the instance's working set, basis, initial list, duals, scalars and its
+// descriptor go into P.one.  Same results and statistics as the round form;
+// the phase clock splits the launch's device time.
+static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock_options& opt, const Ctx& c, int bfs,
+                            int max_rounds, flock_flow* flows, int64_t* du, int64_t* dv, flock_stats* st,
+                            std::chrono::steady_clock::time_point t0) {
+    const int m = I->m, n = I->n, V = m + n, V1 = V - 1;
+    size_t o = 0;
+    const size_t o_ws = o;   o = al256(o + instance_ws_bytes(V, m));
+    const size_t o_out = o;  o = al256(o + (size_t)3 * V1 * 4);
+    const size_t o_bfs = o;  o = al256(o + (size_t)3 * V1 * 4);
+    const size_t o_pot = o;  o = al256(o + (size_t)V * 8);
+    const size_t o_sc = o;   o = al256(o + sizeof(Scalars));
+    const size_t o_desc = o; o = al256(o + sizeof(BatchDesc));
+    const size_t o_ph = o;   o = al256(o + sizeof(PhaseClock));
+    FLOCK_CK(P.one.ensure(o));
+    FLOCK_CK(P.h_desc.ensure(sizeof(BatchDesc)));
+    BatchDesc* hd = P.h_desc.as<BatchDesc>();
+    hd->m = m; hd->n = n; hd->ldc = c.I.ldc; hd->index = 0;
+    hd->cost = c.I.cost;
+    hd->sd = c.I.supply;
+    hd->ws = P.one.as<uint8_t>(o_ws);
+    hd->out = P.one.as<int32_t>(o_out);
+    hd->bfs = P.one.as<int32_t>(o_bfs);
+    hd->pot = P.one.as<int64_t>(o_pot);
+    hd->sc = P.one.as<Scalars>(o_sc);
+    hd->done = nullptr;
+    PhaseClock* d_ph = P.one.as<PhaseClock>(o_ph);
+    FLOCK_CK(cudaMemcpyAsync(P.one.as<BatchDesc>(o_desc), hd, sizeof(BatchDesc), cudaMemcpyHostToDevice, P.stream));
+    FLOCK_CK(cudaMemsetAsync(d_ph, 0, sizeof(PhaseClock), P.stream));
+    BatchArgs a;
+    a.desc = P.one.as<BatchDesc>(o_desc);
+    a.count = 1;
+    a.next = nullptr;
+    a.active = nullptr;
+    a.maxV = V; a.maxM = m;
+    a.bfs_method = bfs == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
+    a.mode = pivot_mode(opt);
+    a.pricing = pricing_of(opt);
+    a.max_rounds = max_rounds;
+    a.light = stage_light(V, m) ? 1 : 0;
+    a.ph = d_ph;
+    const size_t smem = launch_smem_bytes(V, m, a.light != 0);
+    const int threads = solve_one_threads(V);
+    const void* fn = solve_one_fn(threads);
+    void* kargs[] = {&a};
+    FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
+    FLOCK_CK(cudaLaunchKernel(fn, dim3(1), dim3(threads), kargs, smem, P.stream));
+    FLOCK_CK(cudaEventRecord(P.ev[2], P.stream));
+    std::vector<int32_t> h3((size_t)3 * V1);
+    std::vector<int64_t> pot((size_t)V);
+    FLOCK_CK(cudaMemcpyAsync(h3.data(), hd->out, (size_t)3 * V1 * 4, cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaMemcpyAsync(pot.data(), hd->pot, (size_t)V * 8, cudaMemcpyDeviceToHost, P.stream));
+    Scalars* hs = P.h_sc.as<Scalars>();
+    FLOCK_CK(cudaMemcpyAsync(hs, hd->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
+    PhaseClock hph;
+    FLOCK_CK(cudaMemcpyAsync(&hph, d_ph, sizeof(PhaseClock), cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaStreamSynchronize(P.stream));
+    float ms_all = 0;
+    cudaEventElapsedTime(&ms_all, P.ev[0], P.ev[2]);
+    const Scalars S = *hs;
+    const bool broken = S.status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE);
+    if (flows && !broken) fill_flows_from_basis(V, h3.data(), h3.data() + V1, h3.data() + 2 * V1, flows);
+    if (du && !broken) for (int i = 0; i < m; i++) du[i] = pot[i];
+    if (dv && !broken) for (int j = 0; j < n; j++) dv[j] = pot[m + j];
+    int status = S.status & kFailMask;
+    if (opt.verify && S.cert) status |= ST_CERT_FAIL;
+    if (st) {
+        st->notes = (S.status & ~kFailMask) | (S.fail_site << 8);
+        st->objective = S.objective;
+        st->iterations = S.rounds;
+        st->pivots = S.pivots;
+        st->active_flows = broken ? 0 : S.active;
+        st->status = status;
+        st->certified = (!broken && S.cert == 0) ? 1 : 0;
+        st->vogel_events = S.events;
+        st->ms_bfs = hph.ns[PH_BFS] * 1e-6;
+        st->ms_dual = hph.ns[PH_DUAL] * 1e-6;
+        st->ms_sweep = hph.ns[PH_SWEEP] * 1e-6;
+        st->ms_cycle = hph.ns[PH_CYCLE] * 1e-6;
+        st->ms_resolve = hph.ns[PH_RESOLVE] * 1e-6;
+        st->ms_adjust = hph.ns[PH_ADJUST] * 1e-6;
+        st->ms_pivot = st->ms_cycle + st->ms_resolve + st->ms_adjust;
+        // the loop's device time: the launch less its setup (BFS) and its
+        // retrieval and certificate (the idle tail)
+        st->ms_simplex = std::max(0.0, (double)ms_all - st->ms_bfs - hph.ns[PH_IDLE] * 1e-6);
+        st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return status ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
+}
+
 static int solve_plain(const flock_instance* I, const flock_options* opt_in, flock_flow* flows,
                        int64_t* du, int64_t* dv, flock_stats* st) {
     const auto t0 = std::chrono::steady_clock::now();
@@ -1131,26 +1742,53 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     int32_t* out3 = nullptr;
     if ((rc = P.prepare(I, c, &out3))) return rc;
     // partial pricing runs on the plain path from kGridPivotV vertices (grid rounds)
-    const bool partial = opt.pricing == FLOCK_PRICING_PARTIAL && V >= kGridPivotV;
+    const bool partial = pricing_of(opt) && V >= kGridPivotV;
     if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds, partial))) return rc;
+    FLOCK_CK(cudaMemsetAsync(P.ph, 0, sizeof(PhaseClock), P.stream));
+    c.ph = P.ph;
     const int nt = threads_for(V);
     const int bfs = opt.bfs_method == FLOCK_BFS_NWC || opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE ? opt.bfs_method
                                                                                                   : FLOCK_BFS_VOGEL;
+    if (V < kGridPivotV && bfs != FLOCK_BFS_VOGEL_DEVICE)
+        return solve_one_launch(P, I, opt, c, bfs, max_rounds, flows, du, dv, st, t0);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     int2 *rbook = nullptr, *cbook = nullptr;
     if (bfs == FLOCK_BFS_VOGEL_DEVICE && (rc = P.build_books(c, &rbook, &cbook))) return rc;
     k_setup<<<1, nt, 0, P.stream>>>(c, bfs, rbook, cbook);
     FLOCK_CK(cudaGetLastError());
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
-    int grid = 0, tile = 0, ntile = 0;
+    int grid = 0, tile = 0, ntile = 0, bgrid = 0, btile = 0, bntile = 0;
     sweep_shape(m, n, &grid, &tile, &ntile);
+    bulk_shape(m, n, &bgrid, &btile, &bntile);
     Scalars* hs = P.h_sc.as<Scalars>();
-    if (V >= kGridPivotV) {
+    // the grid rounds apply single pivots: the parallel stepping stone's
+    // multi-pivot rounds run on one block at every size
+    if (V >= kGridPivotV && pivot_mode(opt) != 3) {
         // large instance: the pivot round over the whole GPU, chunks of
         // rounds captured once as a CUDA graph
         FLOCK_CK(cudaMemsetAsync(P.gp, 0, sizeof(GridPivot), P.stream));
+        FLOCK_CK(cudaMemsetAsync(P.cp, 0, sizeof(ClusterPivot), P.stream));
         const int gg = std::max(1, std::min((V + 255) / 256, 2 * num_sms()));
-        int chunk = 8;
+        // Partial pricing: each iteration is a full round (the bulk sweep of
+        // every row, the next candidate rows, one pivot over the grid) and
+        // then the candidate rounds inside one thread-block cluster, until
+        // the candidates run out or pp_refresh rounds have passed.  The
+        // six-kernel rounds otherwise (FULL pricing, no cluster launch on
+        // this device, or FLOCK_GRID_FORM=rounds).
+        const char* form = getenv("FLOCK_GRID_FORM");
+        const bool clustered = partial && P.cluster_ctas >= 2 && !(form && !strcmp(form, "rounds"));
+        cudaLaunchConfig_t ccfg = {};
+        cudaLaunchAttribute cattr[1];
+        ccfg.gridDim = dim3(P.cluster_ctas);
+        ccfg.blockDim = dim3(kCRoundThreads);
+        ccfg.stream = P.stream;
+        cattr[0].id = cudaLaunchAttributeClusterDimension;
+        cattr[0].val.clusterDim.x = P.cluster_ctas;
+        cattr[0].val.clusterDim.y = 1;
+        cattr[0].val.clusterDim.z = 1;
+        ccfg.attrs = cattr;
+        ccfg.numAttrs = 1;
+        int chunk = clustered ? 2 : 8;
         cudaGraphExec_t exec = nullptr;
         int exec_chunk = 0;
         for (;;) {
@@ -1160,12 +1798,18 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                 cudaGraph_t g;
                 FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
                 for (int r = 0; r < chunk; r++) {
-                    k_gsweep<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
-                    if (partial) k_gsweep_rest<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
-                    k_gchoose<<<1, 1024, 0, P.stream>>>(c, P.gp);
+                    if (clustered) {
+                        k_sweep<<<bgrid, kBulkThreads, kBulkSmem, P.stream>>>(c, btile, bntile);
+                        k_gchoose_all<<<1, 1024, 0, P.stream>>>(c, P.gp);
+                    } else {
+                        k_gsweep<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
+                        if (partial) k_gsweep_rest<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
+                        k_gchoose<<<1, 1024, 0, P.stream>>>(c, P.gp);
+                    }
                     k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
                     k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
                     k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                    if (clustered) FLOCK_CK(cudaLaunchKernelEx(&ccfg, k_cround, c, P.cp));
                 }
                 FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
                 FLOCK_CK(cudaGraphInstantiate(&exec, g, 0));
@@ -1176,7 +1820,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
             FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
             FLOCK_CK(cudaStreamSynchronize(P.stream));
             if (hs->done) break;
-            if (chunk < 256) chunk *= 2;
+            if (chunk < (clustered ? 16 : 256)) chunk *= 2;
         }
         if (exec) cudaGraphExecDestroy(exec);
     } else {
@@ -1192,7 +1836,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                 cudaGraph_t g;
                 FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
                 for (int r = 0; r < chunk; r++) {
-                    k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+                    k_sweep<<<bgrid, kBulkThreads, kBulkSmem, P.stream>>>(c, btile, bntile);
                     k_pivot<<<1, nt, 0, P.stream>>>(c);
                 }
                 FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
@@ -1221,6 +1865,8 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     std::vector<int64_t> pot((size_t)V);
     FLOCK_CK(cudaMemcpyAsync(pot.data(), c.pot, (size_t)V * 8, cudaMemcpyDeviceToHost, P.stream));
     FLOCK_CK(cudaMemcpyAsync(hs, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
+    PhaseClock hph;
+    FLOCK_CK(cudaMemcpyAsync(&hph, P.ph, sizeof(PhaseClock), cudaMemcpyDeviceToHost, P.stream));
     FLOCK_CK(cudaStreamSynchronize(P.stream));
     float ms_bfs = 0, ms_loop = 0;
     cudaEventElapsedTime(&ms_bfs, P.ev[0], P.ev[1]);
@@ -1244,6 +1890,12 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
         st->ms_bfs = ms_bfs;
         st->ms_simplex = ms_loop;
         st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        st->ms_dual = hph.ns[PH_DUAL] * 1e-6;
+        st->ms_sweep = hph.ns[PH_SWEEP] * 1e-6;
+        st->ms_cycle = hph.ns[PH_CYCLE] * 1e-6;
+        st->ms_resolve = hph.ns[PH_RESOLVE] * 1e-6;
+        st->ms_adjust = hph.ns[PH_ADJUST] * 1e-6;
+        st->ms_pivot = st->ms_cycle + st->ms_resolve + st->ms_adjust;
     }
     return status ? FLOCK_ERR_NOT_OPTIMAL : FLOCK_OK;
 }
@@ -1296,6 +1948,15 @@ static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* even
 // Benchmark hook: time `iters` launches of the fused sweep on an m x n matrix
 // with random costs and duals already resident (no pivots).  Writes the
 // average launch time (CUDA events on the launching stream).
+static void bulk_shape(int m, int n, int* grid, int* tile, int* ntile) {
+    const int ldc = (n + 3) & ~3;
+    *tile = std::min(ldc, kSweepTile);
+    *ntile = (n + *tile - 1) / *tile;
+    const long long units = (long long)m * ((std::min(*tile, n) + kBulkSeg - 1) / kBulkSeg);
+    const int nrg = (int)std::max(1LL, std::min(units, (long long)std::max(1, num_sms() / *ntile)));
+    *grid = *ntile * nrg;
+}
+
 static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile) {
     const int ldc = (n + 3) & ~3;
     *tile = std::min(ldc, kSweepTile);
@@ -1341,8 +2002,8 @@ static int test_sweep(int m, int n, const int32_t* cost, const int64_t* pot, uin
         k_sweep_cta_only<<<1, threads, 0, P.stream>>>(c);
     } else {
         int grid = 0, tile = 0, ntile = 0;
-        sweep_shape(m, n, &grid, &tile, &ntile);
-        k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+        bulk_shape(m, n, &grid, &tile, &ntile);
+        k_sweep<<<grid, kBulkThreads, kBulkSmem, P.stream>>>(c, tile, ntile);
     }
     FLOCK_CK(cudaGetLastError());
     FLOCK_CK(cudaMemcpyAsync(keys, c.row_best, (size_t)m * 8, cudaMemcpyDeviceToHost, P.stream));
@@ -1414,10 +2075,10 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
     k_publish_duals<<<1, 1024, 0, P.stream>>>(c);
     FLOCK_CK(cudaMemsetAsync(c.row_best, 0xff, (size_t)m * 8, P.stream));
     int grid = 0, tile = 0, ntile = 0;
-    sweep_shape(m, n, &grid, &tile, &ntile);
-    for (int w = 0; w < 3; w++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+    bulk_shape(m, n, &grid, &tile, &ntile);
+    for (int w = 0; w < 3; w++) k_sweep<<<grid, kBulkThreads, kBulkSmem, P.stream>>>(c, tile, ntile);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
-    for (int k = 0; k < iters; k++) k_sweep<<<grid, kSweepThreads, 0, P.stream>>>(c, tile, ntile, nullptr, nullptr, 0);
+    for (int k = 0; k < iters; k++) k_sweep<<<grid, kBulkThreads, kBulkSmem, P.stream>>>(c, tile, ntile);
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     FLOCK_CK(cudaEventSynchronize(P.ev[1]));
     float ms = 0;
@@ -1707,6 +2368,7 @@ struct BatchRunner {
 
     BatchArgs args_for(int b) {
         BatchArgs a;
+        a.ph = nullptr;
         a.desc = d_desc.as<BatchDesc>() + bstart[b];
         a.count = bstart[b + 1] - bstart[b];
         a.next = nullptr; a.active = nullptr;
@@ -1714,7 +2376,7 @@ struct BatchRunner {
         a.light = stage_light(bmaxV[b], bmaxM[b]) ? 1 : 0;
         a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
         a.mode = pivot_mode(opt);
-        a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
+        a.pricing = pricing_of(opt);
         a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
         return a;
     }
@@ -1918,6 +2580,8 @@ struct BatchRunner {
             st_out->certified = (!broken && S.cert == 0) ? 1 : 0;
             st_out->vogel_events = S.events;
             st_out->ms_total = 0; st_out->ms_bfs = 0; st_out->ms_simplex = 0;
+            st_out->ms_dual = st_out->ms_sweep = st_out->ms_pivot = 0;
+            st_out->ms_cycle = st_out->ms_resolve = st_out->ms_adjust = 0;
         }
     }
 
@@ -2058,6 +2722,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
                  cudaStream_t s) {
     if (count < 1 || maxV > kMaxStagedV) return FLOCK_ERR_ARG;
     BatchArgs a;
+    a.ph = nullptr;
     a.desc = d_desc;
     a.count = count;
     a.next = d_next;
@@ -2065,7 +2730,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     a.maxV = maxV; a.maxM = maxM;
     a.bfs_method = opt.bfs_method == FLOCK_BFS_NWC ? FLOCK_BFS_NWC : FLOCK_BFS_VOGEL;
     a.mode = pivot_mode(opt);
-    a.pricing = opt.pricing == FLOCK_PRICING_PARTIAL ? 1 : 0;
+    a.pricing = pricing_of(opt);
     a.max_rounds = opt.max_iterations > 0 ? opt.max_iterations : (1 << 30);
     a.light = stage_light(maxV, maxM) ? 1 : 0;
     const size_t smem = launch_smem_bytes(maxV, maxM, a.light != 0);

@@ -761,7 +761,7 @@ __device__ __forceinline__ uint64_t oflow(int64_t f) { return (uint64_t)f ^ 0x80
 // ones written to the other.  Two passes over the vertices, four barriers.
 // Returns 1 if the pivot was applied (block-uniform).
 template <int J = kJump>
-__device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int V) {
+__device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int V, PhaseScope* ps = nullptr) {
     const int m = c.I.m;
     const int par = c.sc->ivp;
     const int2* ivA = c.iv + (par ? V : 0);
@@ -815,6 +815,7 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
         __syncthreads();
         return 0;
     }
+    if (ps) ps->mark(PH_ADJUST);                          // cycle known; leaving edge chosen by the reduction
     const int64_t th = (int64_t)(fmin ^ 0x8000000000000000ull);
     const int eside = lside ? 2 : 1;
     const int dother = lside ? dk : dl;
@@ -892,6 +893,167 @@ __device__ int single_pivot_iv(const Ctx& c, BlockScratch& bs, int k, int l, int
     return bad ? 0 : 1;
 }
 
+// ------------------------------------------------- parallel stepping stone --
+// -a parallel_ss (ss_model_parallel.cu:128-246, PIVOT_ss.cu:294-571,
+// parallel_kernels.cu:396-660): every cell with a negative cycle cost is a
+// candidate; candidates are taken most negative first (ties in row-major
+// order) and one is accepted unless its cycle shares a tree edge with a
+// cycle accepted before it; all accepted cycles pivot in the same round.
+// The reference computes each cell's cycle cost from per-row tree searches
+// (alternating sums of the path costs, no duals); along any tree path those
+// sums telescope to u_i + v_j, so the cycle cost of cell (i, j) is exactly
+// c_ij - u_i - v_j in integer arithmetic, which the round reads from the
+// full sweep's duals.  Candidates: the negative cells below a 32-bin
+// histogram threshold over [min, 0), at most kSSCap (and m) of them, in
+// row-major order -- the most negative ones, so the accepted set is the
+// reference's greedy choice restricted to them.  Selection: rounds of edge
+// claims (atomicMin of the candidate's priority (cost, slot)) among the
+// undecided candidates; one that owns every edge of its cycle is accepted
+// and marks its edges taken, one whose cycle holds a taken edge is
+// rejected.  Each selection round accepts at least the best undecided
+// candidate, and the result is the lexicographically first independent set
+// by priority: the sequential greedy's.
+constexpr int kSSCap = 1024;
+
+// Candidate s of an ss round: row cand[s], column uf[s], priority row_best[s],
+// theta cand_theta[s], leaving edge cand_q[s], cand_info[s]: bit 0 leaving
+// edge on the column side, bit 1 accepted, bit 2 rejected, bit 3 walk failed.
+__device__ __forceinline__ int64_t cell_reduced(const Ctx& c, int i, int j) {
+    return (int64_t)cost_of(c.I, i, j) - c.pot[i] - c.pot[c.I.m + j];
+}
+
+template <int J = kJump>
+__device__ void ss_round_cta(const Ctx& c, BlockScratch& bs, PhaseScope* ps) {
+    const InstDev& I = c.I;
+    const int m = I.m, n = I.n, V = m + n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int cap = min(kSSCap, m);
+    // the most negative cycle cost (the full sweep's row keys)
+    int32_t rmin = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) rmin = min(rmin, key_val(c.row_best[i]));
+    rmin = key_val(block_min_u64(pack_i32(rmin, 0u), bs));
+    if (rmin >= 0) {
+        if (threadIdx.x == 0) { c.sc->done = 1; c.sc->ncand = 0; }
+        return;
+    }
+    const int64_t span = -(int64_t)rmin;
+    // histogram of every negative cell
+    if (threadIdx.x < 32) bs.red2[threadIdx.x] = 0;
+    __syncthreads();
+    for (int i = warp; i < m; i += nw)
+        for (int j = lane; j < n; j += 32) {
+            const int64_t r = cell_reduced(c, i, j);
+            if (r < 0) atomicAdd((unsigned long long*)&bs.red2[((int64_t)clamp32(r) - rmin) * 32 / span], 1ull);
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t cum = bs.red2[0];
+        int last = 0;
+        for (int b = 1; b < 32 && cum + bs.red2[b] <= (uint64_t)cap; b++) { cum += bs.red2[b]; last = b; }
+        bs.i[1] = last;
+    }
+    __syncthreads();
+    const int last = bs.i[1];
+    auto chosen = [&](int64_t r) { return r < 0 && ((int64_t)clamp32(r) - rmin) * 32 / span <= last; };
+    // per-row counts, their exclusive scan, then each row's cells in column order
+    for (int i = warp; i < m; i += nw) {
+        int cnt = 0;
+        for (int j = lane; j < n; j += 32) cnt += chosen(cell_reduced(c, i, j)) ? 1 : 0;
+        cnt = (int)__reduce_add_sync(0xffffffffu, (unsigned)cnt);
+        if (lane == 0) c.cand_info[i] = cnt;
+    }
+    __syncthreads();
+    const int total = block_exclusive_scan_i32(c.cand_info, m, bs);
+    const int ncand = min(total, cap);
+    for (int i = warp; i < m; i += nw) {
+        int pos = c.cand_info[i];
+        if (pos >= ncand) continue;
+        for (int j0 = 0; j0 < n && pos < ncand; j0 += 32) {
+            const int j = j0 + lane;
+            const int64_t r = j < n ? cell_reduced(c, i, j) : 0;
+            const bool sel = j < n && chosen(r);
+            const unsigned mask = __ballot_sync(0xffffffffu, sel);
+            const int slot = pos + __popc(mask & ((1u << lane) - 1u));
+            if (sel && slot < ncand) {
+                c.cand[slot] = i;
+                c.uf[slot] = j;
+                c.row_best[slot] = pack_i32(clamp32(r), (uint32_t)slot);
+            }
+            pos += __popc(mask);
+        }
+    }
+    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.claim[v] = kNoKey; c.side[v] = 0; }
+    __syncthreads();
+    for (int t = threadIdx.x; t < ncand; t += blockDim.x) c.cand_info[t] = 0;
+    if (ps) ps->mark(PH_RESOLVE);
+    // selection rounds (each accepts the best undecided candidate at least)
+    int bad = 0;
+    for (int it = 0; it <= ncand; it++) {
+        // claims of the undecided candidates; theta and the leaving edge on the first walk
+        for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+            if (c.cand_info[t] & 14) continue;
+            const int k = c.cand[t], l = m + c.uf[t];
+            const uint64_t P = c.row_best[t];
+            bool taken = false;
+            const int w = walk_path(c, k, l, V, [&](int v, int) {
+                if (c.side[v]) { taken = true; return false; }
+                return true;
+            });
+            if (w < 0) { c.cand_info[t] |= 8; bad = 1; continue; }
+            if (taken) { c.cand_info[t] |= 4; continue; }
+            if (it == 0) {
+                const CycleResult cr = cycle_walk(c, k, l, P, V);
+                if (!cr.ok) { c.cand_info[t] |= 8; bad = 1; continue; }
+                c.cand_theta[t] = cr.theta;
+                c.cand_q[t] = cr.q;
+                c.cand_info[t] |= cr.lside;
+            } else {
+                walk_path(c, k, l, V, [&](int v, int) {
+                    atomicMin((unsigned long long*)&c.claim[v], (unsigned long long)P);
+                    return true;
+                });
+            }
+        }
+        __syncthreads();
+        int undecided = 0;
+        for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+            if (c.cand_info[t] & 14) continue;
+            if (cycle_owned(c, c.cand[t], m + c.uf[t], c.row_best[t], V)) c.cand_info[t] |= 2 | 16;   // 16: new this round
+            else undecided++;
+        }
+        __syncthreads();
+        // the new winners mark their edges taken; every claim is reset
+        for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+            if (!(c.cand_info[t] & 16)) continue;
+            c.cand_info[t] &= ~16;
+            walk_path(c, c.cand[t], m + c.uf[t], V, [&](int v, int) { c.side[v] = 1; return true; });
+        }
+        for (int v = threadIdx.x; v < V; v += blockDim.x) c.claim[v] = kNoKey;
+        undecided = (int)block_sum_i64(undecided, bs);     // its barriers order the marks and resets
+        if (undecided == 0) break;
+    }
+    if (ps) ps->mark(PH_ADJUST);
+    // the accepted cycles are edge-disjoint: they pivot together
+    int wins = 0;
+    for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
+        if ((c.cand_info[t] & 2) == 0) continue;
+        CycleResult cr;
+        cr.theta = c.cand_theta[t]; cr.q = c.cand_q[t]; cr.lside = c.cand_info[t] & 1; cr.ok = 1;
+        cycle_apply(c, c.cand[t], m + c.uf[t], cr, V);
+        wins++;
+    }
+    const int64_t w = block_sum_i64(wins, bs);
+    const int any_bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        c.sc->pivots += (int32_t)w;
+        c.sc->ncand = ncand;
+        c.sc->last_winners = (int32_t)w;
+        c.sc->stale = 1;
+        if (any_bad || w == 0) { c.sc->status |= ST_TREE_CORRUPT; c.sc->done = 1; }
+    }
+    __syncthreads();
+}
+
 // Parallel mode: candidates walked per round (the rest wait for later rounds).
 constexpr int kMaxCand = 32;
 // Switch mode: a parallel round applying fewer pivots than this switches the
@@ -903,10 +1065,16 @@ constexpr int kSwitchPivots = 10;
 // (pre_best, kNoKey: none).  With partial pricing only the listed candidate
 // rows hold keys this round, and only they are read.
 template <int J = kJump>
-__device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best = false, uint64_t pre_best = kNoKey) {
+__device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best = false, uint64_t pre_best = kNoKey,
+                                PhaseScope* ps = nullptr) {
     const InstDev& I = c.I;
     const int m = I.m, V = m + I.n;
     const int mode = c.sc->mode;
+    if (mode == 3) {          // parallel stepping stone (full pricing: every row key is current)
+        if (ps) ps->mark(PH_CYCLE);
+        ss_round_cta<J>(c, bs, ps);
+        return;
+    }
     // a candidate key whose column is outside the instance is an internal
     // error: recorded, never used as an index
     const uint32_t ncols = (uint32_t)I.n;
@@ -995,8 +1163,9 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best =
         if (threadIdx.x == 0) { c.sc->done = 1; c.sc->ncand = 0; }
         return;
     }
+    if (ps) ps->mark(PH_CYCLE);
     if (ncand == 1) {
-        const int ok = single_pivot_iv<J>(c, bs, first, m + (int)key_idx(c.row_best[first]), V);
+        const int ok = single_pivot_iv<J>(c, bs, first, m + (int)key_idx(c.row_best[first]), V, ps);
         if (threadIdx.x == 0) {
             c.sc->pivots += ok;
             c.sc->ncand = 1;
@@ -1023,6 +1192,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best =
         bad |= !cr.ok;
     }
     __syncthreads();
+    if (ps) ps->mark(PH_RESOLVE);
     int wins = 0;
     for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
         if (c.cand_info[t] & 4) continue;
@@ -1033,6 +1203,7 @@ __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best =
         if (cycle_owned(c, i, l, P, V)) { c.cand_info[t] |= 2; wins++; }
     }
     __syncthreads();
+    if (ps) ps->mark(PH_ADJUST);
     for (int t = threadIdx.x; t < ncand; t += blockDim.x) {
         if (!(c.cand_info[t] & 2)) continue;
         const int i = c.cand[t];

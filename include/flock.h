@@ -71,10 +71,20 @@ typedef struct {
  * device Vogel semantics (flock_vogel_device); flock_solve only (batched and
  * served forms return FLOCK_ERR_ARG), lines of at most 16382 cells. */
 enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1, FLOCK_BFS_VOGEL_DEVICE = 2 };
-/* -a parallel_uv / parallel_ss / switch_hybrid.  SWITCH runs parallel rounds
- * until one applies fewer than 10 pivots, then sequential ones
- * (switch/switch_model_parallel.cu:182-184). */
-enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2 };
+/* Pivoting.  SEQUENTIAL (-a parallel_uv): one pivot per round, the most
+ * negative reduced cost (Dantzig, row-major first minimum).  PARALLEL: the
+ * rows with the most negative keys (at most 32) walk their cycles and the
+ * edge-disjoint ones pivot together.  SWITCH (-a switch_hybrid) runs
+ * parallel rounds until one applies fewer than 10 pivots, then sequential
+ * ones (switch/switch_model_parallel.cu:182-184).  SS (-a parallel_ss,
+ * parallel_ss_method/PIVOT_ss.cu:294-571): every cell with a negative cycle
+ * cost is a candidate (the most negative ones, at most min(1024, m) per
+ * round); they are taken most negative first and a cycle is accepted unless
+ * it shares a tree edge with one accepted before it; all accepted cycles
+ * pivot in the same round.  SS prices every cell each round (the pricing
+ * option is ignored); instances of 4096 or more vertices run its rounds on
+ * one block. */
+enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2, FLOCK_PIVOT_SS = 3 };
 /* Pricing.  FULL: every round sweeps every cell (the reference's Dantzig rule,
  * uv_model_parallel.cu:151-200).  PARTIAL (the default; no counterpart in the
  * reference):
@@ -88,7 +98,7 @@ enum { FLOCK_PRICING_FULL = 0, FLOCK_PRICING_PARTIAL = 1 };
 
 typedef struct {
     int32_t bfs_method;      /* FLOCK_BFS_VOGEL (default), FLOCK_BFS_NWC or FLOCK_BFS_VOGEL_DEVICE */
-    int32_t pivot_method;    /* FLOCK_PIVOT_SWITCH (default), _PARALLEL or _SEQUENTIAL */
+    int32_t pivot_method;    /* FLOCK_PIVOT_SWITCH (default), _PARALLEL, _SEQUENTIAL or _SS */
     int32_t max_iterations;  /* cap on pricing rounds; <= 0: 1 << 30 */
     int32_t verify;          /* nonzero: run the exact certificate check (default on) */
     int32_t pricing;         /* FLOCK_PRICING_PARTIAL (default) or FLOCK_PRICING_FULL */
@@ -120,6 +130,22 @@ typedef struct {
     double ms_total;         /* wall time of the call (ms) */
     double ms_bfs;           /* device time of the initial solution + start tree */
     double ms_simplex;       /* device time of the pivot loop */
+    /* Device time per simplex phase (ms), the reference's model statistics
+     * (uv_time, reduced_cost_time, pivot_time, cycle_discovery_time,
+     * resolve_time, adjustment_time; uv_model_parallel.cu:301-341).  Set by
+     * the plain solver (flock_solve, and the instances of more than 4096
+     * vertices that the batched and served forms hand to it); 0 otherwise.
+     *   ms_dual:    rebuilds of the tree's duals, depths and intervals (at the
+     *               start and after a round that applied several pivots; a
+     *               single pivot updates the duals in place, inside ms_adjust)
+     *   ms_sweep:   reduced-cost sweeps and the choice of the entering cells
+     *   ms_cycle:   cycle discovery (tree paths of the entering cells)
+     *   ms_resolve: deconfliction of the candidates of a parallel round
+     *   ms_adjust:  leaving edge, flow change and the in-place tree update
+     *   ms_pivot = ms_cycle + ms_resolve + ms_adjust.
+     * Launch gaps count toward the phase before them, so ms_dual + ms_sweep
+     * + ms_pivot is close to ms_simplex plus the start tree's dual rebuild. */
+    double ms_dual, ms_sweep, ms_pivot, ms_cycle, ms_resolve, ms_adjust;
 } flock_stats;
 
 void flock_default_options(flock_options* opt);

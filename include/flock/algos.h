@@ -4,83 +4,20 @@
 // ProblemInstance and a caller-owned flow array of m+n-1 entries, call
 // execute(), then create_flows(), and read objVal / totalIterations /
 // totalSolveTime and the phase timers.  Header-only over the C ABI in flock.h.
+// With this directory on the include path, the reference's own src/main.cpp
+// compiles unchanged: structs.h, instance.h, logger.h and parameters.h carry
+// the reference's names.
 //
 // Differences from the reference, by design: costs are exact integers
 // (ProblemInstance::cost_scale decimal digits; the float `costs` array is kept
 // for source compatibility), errors are reported by exceptions carrying the
-// flock_status instead of exit(), and every model runs on the GPU.
+// flock_status instead of exit(), every model runs on the GPU, and the
+// Gurobi model (lpModel) is present only as a name: its execute() throws.
 #pragma once
-#include <cmath>
-#include <cstdint>
-#include <cstdlib>
-#include <cstring>
-#include <stdexcept>
-#include <string>
-#include <vector>
-
-#include "../flock.h"
+#include "instance.h"
+#include "logger.h"
 #include "parameters.h"
-
-struct FileNotFoundException : public std::exception {
-    const char* what() const throw() { return "File not found!"; }
-};
-
-struct flock_error : public std::runtime_error {
-    int status;
-    flock_error(int s, const std::string& w) : std::runtime_error(w), status(s) {}
-};
-
-// Container for the problem (src/structs.h:19-40).
-class ProblemInstance {
-public:
-    bool read_mode = false;
-    std::string filename;
-    enum my_algo { cpu_lp_solve, parallel_uv, parallel_ss, switch_hybrid };
-    my_algo algo = parallel_uv;
-    int numDemands = 0, numSupplies = 0, *demands = nullptr, *supplies = nullptr, active_flows = 0;
-    double readTime = 0, preprocessTime = 0, solveTime = 0, postprocessTime = 0;
-    double totalFlowCost = 0;
-    float* costs = nullptr;               // reference-compatible view
-    std::vector<int32_t> int_costs;       // exact costs * 10^cost_scale
-    int cost_scale = 0;
-
-    void allocate_memory() {
-        supplies = (int*)malloc(sizeof(int) * numSupplies);
-        demands = (int*)malloc(sizeof(int) * numDemands);
-        costs = (float*)malloc(sizeof(float) * (size_t)numSupplies * numDemands);
-        int_costs.assign((size_t)numSupplies * numDemands, 0);
-    }
-    ProblemInstance() {}
-    ~ProblemInstance() { free(supplies); free(demands); free(costs); }
-    ProblemInstance(const ProblemInstance&) = delete;
-    ProblemInstance& operator=(const ProblemInstance&) = delete;
-};
-
-// Information for a flow variable (src/structs.h:45-52).
-struct flowInformation {
-    int source, destination;
-    float qty;
-};
-
-// .dat reader (src/instance.cpp:80-141 readSize/readCosts): exact decimal costs.
-inline void make_problem(const std::string& filename, ProblemInstance& problem) {
-    problem.filename = filename;
-    problem.read_mode = true;
-    int32_t m = 0, n = 0, scale = 0;
-    int rc = flock_dat_shape(filename.c_str(), &m, &n);
-    if (rc == FLOCK_ERR_FILE) throw FileNotFoundException();
-    if (rc) throw flock_error(rc, flock_last_error());
-    if ((rc = flock_dat_scale(filename.c_str(), &scale))) throw flock_error(rc, flock_last_error());
-    problem.numSupplies = m;
-    problem.numDemands = n;
-    problem.allocate_memory();
-    problem.cost_scale = scale;
-    rc = flock_read_dat(filename.c_str(), scale, m, n, problem.supplies, problem.demands, problem.int_costs.data());
-    if (rc) throw flock_error(rc, flock_last_error());
-    const double p = std::pow(10.0, scale);
-    for (size_t k = 0; k < problem.int_costs.size(); k++) problem.costs[k] = (float)(problem.int_costs[k] / p);
-    problem.active_flows = m + n - 1;
-}
+#include "structs.h"
 
 namespace flock_detail {
 class ModelBase {
@@ -121,7 +58,13 @@ public:
         objVal = (double)stats.objective / std::pow(10.0, data->cost_scale);
         totalIterations = stats.iterations;
         totalSolveTime = stats.ms_bfs + stats.ms_simplex;
-        pivot_time = stats.ms_simplex * 1000.0;
+        // phase times in microseconds (the reference's unit; main.cpp divides by 1000)
+        uv_time = stats.ms_dual * 1000.0;
+        reduced_cost_time = stats.ms_sweep * 1000.0;
+        pivot_time = stats.ms_pivot * 1000.0;
+        cycle_discovery_time = stats.ms_cycle * 1000.0;
+        resolve_time = stats.ms_resolve * 1000.0;
+        adjustment_time = stats.ms_adjust * 1000.0;
         data->active_flows = stats.active_flows;
         data->totalFlowCost = objVal;
         data->solveTime = totalSolveTime;
@@ -143,14 +86,30 @@ class uvModel_parallel : public flock_detail::ModelBase {
 public:
     uvModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_SEQUENTIAL) {}
 };
-// -a parallel_ss: deconflicted parallel stepping-stone pivots per sweep.
+// -a parallel_ss: every negative cell a candidate, the greedy most-negative
+// set of tree-edge-disjoint cycles pivoted together each round.
 class ssModel_parallel : public flock_detail::ModelBase {
 public:
-    ssModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_PARALLEL) {}
+    ssModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_SS) {}
 };
 // -a switch_hybrid: parallel rounds until one applies fewer than 10 pivots,
 // then sequential ones (switch/switch_model_parallel.cu:182-184).
 class switchModel_parallel : public flock_detail::ModelBase {
 public:
     switchModel_parallel(ProblemInstance* p, flowInformation* f) : ModelBase(p, f, FLOCK_PIVOT_SWITCH) {}
+};
+
+// -a cpu_lp_solve: the reference's Gurobi model (gurobi_lp_method/lp_model.h).
+// Not part of this library: execute() throws flock_error; main.cpp only
+// reaches it when built with MAKE_WITH_GUROBI.
+class lpModel {
+public:
+    ProblemInstance* data;
+    flowInformation* optimal_flows;
+    double objVal = 0;
+    int totalIterations = 0;
+    double totalSolveTime = 0;
+    lpModel(ProblemInstance* problem, flowInformation* flows) : data(problem), optimal_flows(flows) {}
+    void execute() { throw flock_error(FLOCK_ERR_ARG, "cpu_lp_solve needs Gurobi, which this build does not include"); }
+    void create_flows() {}
 };

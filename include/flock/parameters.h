@@ -16,3 +16,9 @@
 #ifndef MAX_ITERATIONS
 #define MAX_ITERATIONS 0
 #endif
+
+// MAKE_WITH_GUROBI: the reference's build switch for its LP model
+// (src/parameters.h); this library has no Gurobi model.
+#ifndef MAKE_WITH_GUROBI
+#define MAKE_WITH_GUROBI 0
+#endif

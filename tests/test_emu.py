@@ -39,9 +39,11 @@ def run(emu, args, env=None, timeout=300):
     return lines
 
 
-# (mode, pricing, threads): mode 0 sequential, 1 parallel, 2 switch; pricing 0
-# full, 1 partial, 2 partial with the row keys overwritten between rounds
-@pytest.mark.parametrize("mode,pricing,threads", [(0, 1, 64), (1, 1, 96), (2, 1, 32), (2, 2, 128), (1, 0, 64)])
+# (mode, pricing, threads): mode 0 sequential, 1 parallel, 2 switch, 3 parallel
+# stepping stone (full pricing only); pricing 0 full, 1 partial, 2 partial with
+# the row keys overwritten between rounds
+@pytest.mark.parametrize("mode,pricing,threads", [(0, 1, 64), (1, 1, 96), (2, 1, 32), (2, 2, 128), (1, 0, 64),
+                                                  (3, 0, 64), (3, 0, 32)])
 def test_emulated_solves(emu, mode, pricing, threads):
     run(emu, [20251203, 6, 10, 60, 0, 5, mode, pricing], {"EMU_THREADS": str(threads)})
 
@@ -104,3 +106,10 @@ def test_emulated_vogel_device(emu, tmp_path, threads):
         np.testing.assert_array_equal(got, exp)
         undefined += rc < 0
     assert undefined > 0
+
+
+def test_emulated_stepping_stone_degenerate(emu):
+    """The parallel stepping-stone rounds on tied, degenerate instances: many
+    candidate cells per round, overlapping cycles resolved by claim rounds."""
+    run(emu, [78, 6, 5, 50, 0, 5, 3, 0], {"EMU_THREADS": "64", "EMU_COST_HI": "3", "EMU_QTY_LO": "1",
+                                          "EMU_QTY_HI": "3"})

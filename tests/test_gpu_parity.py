@@ -406,3 +406,71 @@ def test_euclid8000_full_size_certified():
     bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, res.flows, res.u, res.v)
     assert bits == 0, f"certificate bits {bits}"
     assert obj == res.objective == EUCLID8000_OPTIMUM
+
+
+@pytest.mark.parametrize("kind", ["uniform", "degenerate"])
+def test_grid_cluster_rounds_match_six_kernel_rounds(kind, monkeypatch):
+    """Partial pricing on the grid path (m + n >= 4096): the candidate rounds
+    inside one thread-block cluster take the same pivots as the six-kernel
+    rounds (same rounds, pivots and objective), both certified by the host
+    oracle."""
+    if kind == "uniform":
+        inst = fg.generate(0, 91, 2048, 2600, 1, 1000, 100, 1000)
+    else:
+        inst = fg.config_instance("degenerate1000", 13, m=2500, n=2048)
+    monkeypatch.setenv("FLOCK_GRID_FORM", "rounds")
+    a = fg.solve(inst)
+    monkeypatch.delenv("FLOCK_GRID_FORM")
+    b = fg.solve(inst)
+    for r in (a, b):
+        assert r.status == 0 and r.certified
+        bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, r.flows, r.u, r.v)
+        assert bits == 0 and obj == r.objective
+    assert (a.objective, a.iterations, a.pivots) == (b.objective, b.iterations, b.pivots)
+
+
+def test_ss_tiny_degenerate():
+    """-a parallel_ss (every negative cell a candidate, greedy edge-disjoint
+    cycles) on tiny tied instances: certified, the reference path's optimum."""
+    for inst in tiny_instances(41, 200):
+        r = fg.solve(inst, pivot="ss")
+        assert_optimal(inst, r)
+
+
+@pytest.mark.parametrize("name,seed,m,n", [("uniform100", 0, None, None), ("uniform100", 3, None, None),
+                                           ("degenerate1000", 2, 300, 250), ("euclid8000", 4, 150, 260)])
+def test_ss_shapes(name, seed, m, n):
+    inst = fg.config_instance(name, seed, m=m, n=n)
+    r = fg.solve(inst, pivot="ss")
+    assert_optimal(inst, r)
+    assert r.pivots >= r.iterations - 1       # several pivots in some rounds, at least one in each but the last
+
+
+def test_ss_degenerate_1000_full_size():
+    """The 1000 x 1000 degenerate workload: the same optimum as the reference
+    CPU path (which certifies optimal), in fewer rounds than the u-v mode's
+    sequential pivots."""
+    inst = fg.config_instance("degenerate1000", 0)
+    ss = fg.solve(inst, pivot="ss")
+    uv = fg.solve(inst, pivot="sequential", pricing="full")
+    assert ss.status == 0 and ss.certified and uv.status == 0 and uv.certified
+    bits, obj = oracle.certify(inst.supply, inst.demand, inst.cost, ss.flows, ss.u, ss.v)
+    assert bits == 0 and obj == ss.objective == uv.objective == 25797
+    assert ss.iterations < uv.iterations
+
+
+def test_ss_batched_and_large_plain():
+    """The batched form with ss pivots on every size bucket up to 4096
+    vertices, and a plain instance of 4096 vertices (its ss rounds on one
+    block): same optima as the default pivots."""
+    sizes = [(20, 30), (60, 60), (100, 120), (200, 250), (400, 500), (900, 1000), (1400, 1500), (2000, 2000)]
+    insts = [fg.generate(0, 600 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(sizes)]
+    a = fg.batch_solve(insts, pivot="ss")
+    b = fg.batch_solve(insts)
+    for k, inst in enumerate(insts):
+        assert a[k].status == 0 and a[k].certified, k
+        assert a[k].objective == b[k].objective, k
+    big = fg.generate(0, 700, 2048, 2048, 1, 1000, 100, 1000)
+    r = fg.solve(big, pivot="ss")
+    d = fg.solve(big)
+    assert r.status == 0 and r.certified and r.objective == d.objective

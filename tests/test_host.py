@@ -129,6 +129,39 @@ def test_cpp_facade_compiles(tmp_path):
         assert r.returncode == 0, r.stderr
 
 
+def test_reference_main_compiles_unchanged(tmp_path):
+    """The reference's own driver (src/main.cpp) compiles and links unchanged
+    against the facade headers (include/flock: algos.h, instance.h, structs.h,
+    logger.h, parameters.h) and the library.  Needs the reference checkout;
+    the file is copied so that its own directory's headers are not found."""
+    import shutil
+    from conftest import REFERENCE
+    src = os.path.join(REFERENCE, "src", "main.cpp")
+    lib_dir = os.path.join(ROOT, "flock_gb300")
+    if not os.path.exists(src):
+        pytest.skip("reference checkout not present")
+    if not os.path.exists(os.path.join(lib_dir, "libflock_gb300.so")):
+        pytest.skip("library not built")
+    shutil.copy(src, tmp_path / "main.cpp")
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include", "flock"), str(tmp_path / "main.cpp"),
+                        "-L", lib_dir, "-lflock_gb300", f"-Wl,-rpath,{lib_dir}", "-o", str(tmp_path / "ref_main")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+
+
+def test_facade_driver_compiles(tmp_path):
+    """The committed facade driver (run on the GPU by tests/test_gpu_facade.py)
+    compiles and links here."""
+    lib_dir = os.path.join(ROOT, "flock_gb300")
+    if not os.path.exists(os.path.join(lib_dir, "libflock_gb300.so")):
+        pytest.skip("library not built")
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "drivers", "facade_main.cpp"), "-L", lib_dir, "-lflock_gb300",
+                        f"-Wl,-rpath,{lib_dir}", "-o", str(tmp_path / "facade_main")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+
+
 def test_cli_usage_errors(tmp_path):
     cli = os.path.join(ROOT, "flock_gb300", "flock")
     if not os.path.exists(cli):
