@@ -413,36 +413,50 @@ def served(fg) -> dict:
                        f"pool of {SERVE_POOL} seeded instances, {SERVE_REQUESTS} requests per rate, 40 GB budget",
            "capacity_solves_s": cap, "rates": []}
     rng = np.random.default_rng(SEED)
+    classes = ((0, 512), (513, 1024), (1025, 2048), (2049, 4000))
+
+    def pct(xs, q):
+        xs = sorted(xs)
+        return xs[min(len(xs) - 1, (len(xs) * q) // 100)] if xs else None
+
     for frac in SERVE_RATES:
         lam = frac * cap
         srv = fg.Server(memory_budget_bytes=40 << 30, max_inflight_batches=16, max_batch=512)
-        lat, bad = [], 0
+        lat, bad, size_of, by_size = [], 0, {}, {c: [] for c in classes}
+
+        def take(results):
+            nonlocal bad
+            for (ticket, status, _, l_ms, st, cert) in results:
+                lat.append(l_ms)
+                bad += not (status == 0 and st == 0 and cert)
+                v = size_of.pop(ticket, 0)
+                for cl in classes:
+                    if cl[0] <= v <= cl[1]:
+                        by_size[cl].append(l_ms)
+
         t_start = time.perf_counter()
         t_next = t_start
         k = 0
         while k < SERVE_REQUESTS:
             now = time.perf_counter()
             if now >= t_next:
-                srv.submit(pool[k % SERVE_POOL])
+                x = pool[k % SERVE_POOL]
+                size_of[srv.submit(x)] = x.m + x.n
                 k += 1
                 t_next += rng.exponential(1.0 / lam)
                 continue
-            for (_, status, _, l_ms, st, cert) in srv.poll():
-                lat.append(l_ms)
-                bad += not (status == 0 and st == 0 and cert)
+            take(srv.poll())
             if t_next - time.perf_counter() > 0.0005:
                 time.sleep(0.0002)
         srv.drain()
         while len(lat) < SERVE_REQUESTS:
-            for (_, status, _, l_ms, st, cert) in srv.poll():
-                lat.append(l_ms)
-                bad += not (status == 0 and st == 0 and cert)
+            take(srv.poll())
         t_end = time.perf_counter()
         srv.close()
-        lat.sort()
         out["rates"].append({"offered_frac": frac, "offered_per_s": lam, "solves_s": SERVE_REQUESTS / (t_end - t_start),
-                             "p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, (len(lat) * 99) // 100)],
-                             "non_certified": bad})
+                             "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "non_certified": bad,
+                             "by_size": {f"V {lo}-{hi}": {"requests": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99)}
+                                         for (lo, hi), v in by_size.items()}})
     # the plain one-at-a-time GPU solver on a sample of the same stream
     smp = pool[:SERVE_PLAIN_SAMPLE]
     fg.solve(smp[0])
@@ -456,30 +470,58 @@ def served(fg) -> dict:
     return out
 
 
+def _phases(r) -> dict:
+    """Device time per simplex phase of a plain solve (ms)."""
+    return {"bfs": r.ms_bfs, "dual": r.ms_dual, "sweep": r.ms_sweep, "pivot": r.ms_pivot, "cycle": r.ms_cycle,
+            "resolve": r.ms_resolve, "adjust": r.ms_adjust}
+
+
 def plain_configs(fg) -> dict:
     """The plain solver on the single-instance workloads: 100 x 100 uniform
-    (costs 1..100, seed 0), 1000 x 1000
-    degenerate-prone (costs 1..20, quantities 1..50, seed 0) and 8000 x 8000
-    Euclidean (costs = rounded distances of uniform points in [0,1000]^2,
-    quantities 1..10000, seed 0): wall time of flock_solve, rounds, pivots,
-    pivots/s, objective and certificate; and the wall time of each Vogel
-    variant alone (flock_vogel: vam_host semantics, flock_vogel_device:
-    vam_device semantics) after one untimed call."""
+    (costs 1..100, seeds 0..31), 1000 x 1000 degenerate-prone (costs 1..20,
+    quantities 1..50, seed 0) and 8000 x 8000 Euclidean (costs = rounded
+    distances of uniform points in [0,1000]^2, quantities 1..10000, seed 0):
+    wall time of flock_solve, rounds, pivots, pivots/s, objective,
+    certificate and the phase split; at 1000 x 1000 also the parallel
+    stepping-stone mode (-a parallel_ss) beside the u-v mode's sequential
+    pivots; and the wall time of each Vogel variant alone (flock_vogel:
+    vam_host semantics, flock_vogel_device: vam_device semantics) after one
+    untimed call."""
     out = {}
-    inst = fg.config_instance("uniform100", 0)
-    fg.solve(inst)
-    t0 = time.perf_counter()
-    r = fg.solve(inst)
-    out["uniform100"] = {"m": inst.m, "n": inst.n, "seconds": time.perf_counter() - t0, "rounds": r.iterations,
-                         "objective": r.objective, "certified": bool(r.certified and r.status == 0)}
+    secs = []
+    for seed in range(32):
+        inst = fg.config_instance("uniform100", seed)
+        fg.solve(inst)
+        t0 = time.perf_counter()
+        r = fg.solve(inst)
+        secs.append(time.perf_counter() - t0)
+        if seed == 0:
+            out["uniform100"] = {"m": inst.m, "n": inst.n, "seconds": secs[0], "rounds": r.iterations,
+                                 "objective": r.objective, "certified": bool(r.certified and r.status == 0),
+                                 "phases_ms": _phases(r)}
+    out["uniform100"]["seeds"] = 32
+    out["uniform100"]["seconds_median"] = statistics.median(secs)
     for name in ("degenerate1000", "euclid8000"):
         inst = fg.config_instance(name, 0)
+        if name == "degenerate1000":
+            fg.solve(inst)
         t0 = time.perf_counter()
         r = fg.solve(inst)
         dt = time.perf_counter() - t0
         out[name] = {"m": inst.m, "n": inst.n, "seconds": dt, "rounds": r.iterations, "pivots": r.pivots,
                      "pivots_per_s": r.pivots / dt, "objective": r.objective,
-                     "certified": bool(r.certified and r.status == 0)}
+                     "certified": bool(r.certified and r.status == 0), "phases_ms": _phases(r)}
+        if name == "degenerate1000":
+            modes = {}
+            for label, kw in (("uv_sequential_full", dict(pivot="sequential", pricing="full")),
+                              ("parallel_ss", dict(pivot="ss"))):
+                fg.solve(inst, **kw)
+                t0 = time.perf_counter()
+                q = fg.solve(inst, **kw)
+                modes[label] = {"seconds": time.perf_counter() - t0, "rounds": q.iterations, "pivots": q.pivots,
+                                "objective": q.objective, "certified": bool(q.certified and q.status == 0),
+                                "phases_ms": _phases(q)}
+            out[name]["pivot_modes"] = modes
         bfs = {}
         for label, f in (("vam_host", fg.vogel), ("vam_device", fg.vogel_device)):
             try:

@@ -44,7 +44,7 @@ constexpr uint64_t kNoKey = ~0ull;
 // default of the batched kernels (64 registers) and the plain solver's.
 constexpr int kJump = 2;
 constexpr int kJumpPlain = 4;
-constexpr int kPPRows = 64;      // partial pricing: capacity of the candidate-row list
+constexpr int kPPRows = 128;     // partial pricing: capacity of the candidate-row list
 // Partial pricing settings (Scalars::pp_rows / pp_refresh): candidate rows
 // kept by a full sweep and rounds between full sweeps.  Instances of up to
 // kPPSmallV vertices (a full sweep is cheap next to a round's fixed cost)

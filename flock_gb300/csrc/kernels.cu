@@ -155,20 +155,20 @@ __device__ __forceinline__ void sweep_part(const Ctx& c, int tile, int ntile, co
 // The full reduced-cost sweep as a bulk-copy pipeline, one block per SM.
 // blockIdx.x = tile + ntile * row_group; a block stages the int32 duals of
 // its column tile and takes the work units (row i, segment of kBulkSeg
-// columns) u = row_group, row_group + nrg, ... in order.  Lane 0 of warp 0
-// streams them with cp.async.bulk into a ring of kBulkStages shared buffers,
-// each with a `full` barrier (the copy's transaction bytes) and an `empty`
-// barrier (released by the consumer); consumer warp w takes units w-1,
-// w-1+kBulkCons, ... and reduces c - v from shared memory into the row key
-// (atomicMin into row_best, which holds kNoKey before the sweep).  Every wait
-// is bounded: a wait that runs out records a failed check (the solve stops
-// with ST_TREE_CORRUPT), and the producer still waits (bounded) for its
-// copies in flight before the block exits.
-constexpr int kBulkSeg = 2048;                     // columns per unit: 8 KB of int32 costs
-constexpr int kBulkStages = 24;                    // a multiple of kBulkCons: warp w owns stages w-1 (+ kBulkCons ...)
-constexpr int kBulkCons = 12;                      // consumer warps; warp 0 produces
-constexpr int kBulkThreads = 32 * (kBulkCons + 1);
-constexpr size_t kBulkSmem = (size_t)kBulkStages * kBulkSeg * 4 + (size_t)kSweepTile * 4;
+// columns) u = row_group, row_group + nrg, ...  Each warp owns kBulkDepth
+// shared buffers and the block's units w, w + kBulkWarps, ...: lane 0 keeps
+// kBulkDepth of them in flight with cp.async.bulk (each buffer completes on
+// its own mbarrier by transaction bytes) and refills a buffer as soon as the
+// warp has read it, so no warp waits for another.  The warp reduces c - v
+// from shared memory into the row key (atomicMin into row_best, which holds
+// kNoKey before the sweep).  Every wait is bounded: a wait that runs out
+// records a failed check (the solve stops with ST_TREE_CORRUPT), and the
+// warp still waits (bounded) for its copies in flight before it exits.
+constexpr int kBulkSeg = 1024;                     // columns per unit: 4 KB of int32 costs
+constexpr int kBulkWarps = 16;
+constexpr int kBulkDepth = 3;                      // buffers (units in flight) per warp
+constexpr int kBulkThreads = 32 * kBulkWarps;
+constexpr size_t kBulkSmem = (size_t)kBulkWarps * kBulkDepth * kBulkSeg * 4 + (size_t)kSweepTile * 4;
 constexpr long long kSpinLimit = 1ll << 22;        // polls of an mbarrier before its wait fails
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -216,7 +216,7 @@ __device__ __forceinline__ BulkUnit bulk_unit(long long k, int rg, int nrg, int 
 }
 
 __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int ntile) {
-    __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
+    __shared__ __align__(8) uint64_t full[kBulkWarps * kBulkDepth];
     __shared__ PhaseLocal phl;
     extern __shared__ __align__(128) unsigned char bulk_smem[];
     PhaseScope ps(c.ph, &phl, PH_SWEEP);
@@ -229,56 +229,52 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
     const long long units = (long long)m * nseg;
     const long long mine = units > rg ? (units - rg + nrg - 1) / nrg : 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (!c.sc->narrow) {      // wide duals: exact int64 keys per element, every warp over the units
-        for (long long k = warp; k < mine; k += kBulkCons + 1) {
-            const BulkUnit w = bulk_unit(k, rg, nrg, nseg, jn);
+    // this warp's units: k = warp + j * kBulkWarps, j = 0 .. cnt-1
+    const long long cnt = mine > warp ? (mine - warp + kBulkWarps - 1) / kBulkWarps : 0;
+    if (!c.sc->narrow) {      // wide duals: exact int64 keys per element
+        for (long long j = 0; j < cnt; j++) {
+            const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn);
             const uint64_t key = row_best_exact(I.cost + (size_t)w.i * I.ldc, c.pot[w.i], c.pot + m, j0 + w.a, j0 + w.b);
             if (lane == 0) atomicMin((unsigned long long*)&c.row_best[w.i], (unsigned long long)key);
         }
         return;
     }
-    int32_t* ring = reinterpret_cast<int32_t*>(bulk_smem);
-    int32_t* vt = ring + (size_t)kBulkStages * kBulkSeg;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kBulkStages; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    int32_t* ring = reinterpret_cast<int32_t*>(bulk_smem) + (size_t)warp * kBulkDepth * kBulkSeg;
+    int32_t* vt = reinterpret_cast<int32_t*>(bulk_smem) + (size_t)kBulkWarps * kBulkDepth * kBulkSeg;
+    uint64_t* bar = full + warp * kBulkDepth;
+    if (lane == 0) {
+        for (int d = 0; d < kBulkDepth; d++) mbar_init(&bar[d], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
-    long long issued = 0;
-    auto issue = [&](long long k) {
-        const int st = (int)(k % kBulkStages);
-        const BulkUnit w = bulk_unit(k, rg, nrg, nseg, jn);
+    __syncwarp();
+    auto issue = [&](long long j) {          // lane 0: unit j of this warp into buffer j % kBulkDepth
+        const int d = (int)(j % kBulkDepth);
+        const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn);
         const uint32_t bytes = (uint32_t)(((w.b - w.a + 3) & ~3) * 4);   // within the row pitch (ldc = ceil4(n))
-        mbar_expect_tx(&full[st], bytes);
-        bulk_g2s(ring + (size_t)st * kBulkSeg, I.cost + (size_t)w.i * I.ldc + j0 + w.a, bytes, &full[st]);
+        mbar_expect_tx(&bar[d], bytes);
+        bulk_g2s(ring + (size_t)d * kBulkSeg, I.cost + (size_t)w.i * I.ldc + j0 + w.a, bytes, &bar[d]);
     };
-    if (threadIdx.x == 0)     // the first ring's worth streams while the duals are staged
-        for (; issued < mine && issued < kBulkStages; issued++) issue(issued);
+    if (lane == 0)            // the first units stream while the duals are staged
+        for (long long j = 0; j < cnt && j < kBulkDepth; j++) issue(j);
     for (int jj = threadIdx.x; jj < jn; jj += blockDim.x) vt[jj] = c.v32[j0 + jj];
     __syncthreads();
-    if (warp == 0) {
-        if (lane != 0) return;
-        bool ok = true;
-        for (; issued < mine; issued++) {
-            const long long k = issued;
-            if (!mbar_wait(&empty[k % kBulkStages], (uint32_t)(((k / kBulkStages) & 1) ^ 1))) { ok = false; break; }
-            issue(k);
-        }
-        if (!ok) fail_check(c.sc, 30);
-        // every copy this block issued has landed before it exits
-        for (long long k = issued > kBulkStages ? issued - kBulkStages : 0; k < issued; k++)
-            if (!mbar_wait(&full[k % kBulkStages], (uint32_t)((k / kBulkStages) & 1))) fail_check(c.sc, 31);
-        return;
-    }
-    for (long long k = warp - 1; k < mine; k += kBulkCons) {
-        const int st = (int)(k % kBulkStages);
-        if (!mbar_wait(&full[st], (uint32_t)((k / kBulkStages) & 1))) {
-            if (lane == 0) fail_check(c.sc, 32);
+    for (long long j = 0; j < cnt; j++) {
+        const int d = (int)(j % kBulkDepth);
+        // every lane waits (the copy's bytes become visible to the lanes that
+        // observe the phase); the outcome is made the same for the whole warp
+        if (!__all_sync(0xffffffffu, mbar_wait(&bar[d], (uint32_t)((j / kBulkDepth) & 1)))) {
+            if (lane == 0) {
+                fail_check(c.sc, 32);
+                // the copies still in flight land before the warp exits
+                const long long last = min(cnt, j + kBulkDepth);
+                for (long long q = j + 1; q < last; q++)
+                    mbar_wait(&bar[q % kBulkDepth], (uint32_t)((q / kBulkDepth) & 1));
+            }
             return;
         }
-        const BulkUnit w = bulk_unit(k, rg, nrg, nseg, jn);
+        const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn);
         const int64_t ui = c.pot[w.i];                 // used after the reduction: its latency overlaps it
-        const int32_t* src = ring + (size_t)st * kBulkSeg;
+        const int32_t* src = ring + (size_t)d * kBulkSeg;
         const int4* s4 = reinterpret_cast<const int4*>(src);
         const int4* v4 = reinterpret_cast<const int4*>(vt + w.a);
         const int nq = (w.b - w.a) >> 2;
@@ -291,8 +287,11 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
             const int32_t tv = src[jl] - vt[w.a + jl];
             if (tv < bv) { bv = tv; bj = jb + jl; }
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[st]);       // the stage is free for the producer
+        __syncwarp();                                  // every lane has read the buffer
+        if (lane == 0 && j + kBulkDepth < cnt) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the reads before the copy's writes
+            issue(j + kBulkDepth);
+        }
         // the row key as narrow_row_key forms it, the winning column's dual
         // read from the staged tile
         const uint64_t kk = warp_min_u64(pack_i32(bv, (uint32_t)bj));
@@ -512,8 +511,12 @@ struct PivotParams {
 // and duals of the re-hung subtree, the reversed path's parents and flows.
 // Adds the change of the int32-window miss count to dwide; sets bad on a
 // failed index check.
+// spv / siv (optional, shared memory): path[base + dir * i] and its old
+// interval for i = 0..t, which the binary searches read in place of global
+// memory.
 __device__ __forceinline__ void update_slice(const Ctx& c, const PivotParams& pp, const int2* ivA, int2* ivB, int v0,
-                                             int stride, int& dwide, int& bad) {
+                                             int stride, int& dwide, int& bad, const int32_t* spv = nullptr,
+                                             const int2* siv = nullptr) {
     const int m = c.I.m, V = m + c.I.n;
     const int t = pp.t;
     const bool lside = pp.eside == 2;
@@ -537,20 +540,20 @@ __device__ __forceinline__ void update_slice(const Ctx& c, const PivotParams& pp
             int lo = 0, hi = t;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
-                const int pv = path[base + dir * mid];
+                const int pv = spv ? spv[mid] : path[base + dir * mid];
                 if (!FLOCK_IN(pv, V)) { bad = 1; break; }
-                if (iv_in(ivA[pv], w.x)) hi = mid; else lo = mid + 1;
+                if (iv_in(siv ? siv[mid] : ivA[pv], w.x)) hi = mid; else lo = mid + 1;
             }
             const int i = lo;
-            const int pi = path[base + dir * i];
+            const int pi = spv ? spv[i] : path[base + dir * i];
             if (!FLOCK_IN(pi, V)) { bad = 1; continue; }
-            const int2 Pi = ivA[pi];
+            const int2 Pi = siv ? siv[i] : ivA[pi];
             int off = 0, rank = w.x - Pi.x;
             int pc = -1;
             if (i > 0) {
-                pc = path[base + dir * (i - 1)];
+                pc = spv ? spv[i - 1] : path[base + dir * (i - 1)];
                 if (!FLOCK_IN(pc, V)) { bad = 1; continue; }
-                const int2 Pc = ivA[pc];
+                const int2 Pc = siv ? siv[i - 1] : ivA[pc];
                 off = Pc.y;
                 if (w.x >= Pc.x) rank -= Pc.y;
             }
@@ -770,29 +773,59 @@ __device__ void cluster_cand_sweep(const Ctx& c, int pn, bool narrow, int rank, 
         const int i = c.prow[u / nseg], sg = u % nseg;
         if (!FLOCK_IN(i, m)) { *bad = 1; continue; }
         const int a = sg * kSegCols, b = min(n, a + kSegCols);
+        const int64_t ui = c.pot[i];                   // used after the reduction: its latency overlaps it
         uint64_t key;
         if (!narrow) {
-            key = row_best_exact(I.cost + (size_t)i * I.ldc, c.pot[i], c.pot + m, a, b);
+            key = row_best_exact(I.cost + (size_t)i * I.ldc, ui, c.pot + m, a, b);
         } else {
             const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
-            int32_t bv = INT32_MAX, bj = INT32_MAX;
+            int32_t bv = INT32_MAX, bj = INT32_MAX, bdual = 0;
             const int qa = a >> 2, qb = b >> 2;
-            for (int q = qa + lane; q < qb; q += 32) min4(bv, bj, row[q], v4[q], 4 * q);
+            for (int q = qa + lane; q < qb; q += 32) {
+                const int4 cv = row[q], vv = v4[q];
+                int32_t t;
+                t = cv.x - vv.x; if (t < bv) { bv = t; bj = 4 * q; bdual = vv.x; }
+                t = cv.y - vv.y; if (t < bv) { bv = t; bj = 4 * q + 1; bdual = vv.y; }
+                t = cv.z - vv.z; if (t < bv) { bv = t; bj = 4 * q + 2; bdual = vv.z; }
+                t = cv.w - vv.w; if (t < bv) { bv = t; bj = 4 * q + 3; bdual = vv.w; }
+            }
             if (lane < b - 4 * qb) {
                 const int j = 4 * qb + lane;
-                const int32_t tv = I.cost[(size_t)i * I.ldc + j] - c.v32[j];
-                if (tv < bv) { bv = tv; bj = j; }
+                const int32_t vj = c.v32[j];
+                const int32_t tv = I.cost[(size_t)i * I.ldc + j] - vj;
+                if (tv < bv) { bv = tv; bj = j; bdual = vj; }
             }
-            key = narrow_row_key(c, i, a, b, bv, bj);
+            // the row key as narrow_row_key forms it; the winning column's
+            // dual comes from the lane that found it
+            const uint64_t mine = pack_i32(bv, (uint32_t)bj);
+            const uint64_t kk = warp_min_u64(mine);
+            const unsigned who = __ballot_sync(0xffffffffu, mine == kk);
+            const int32_t vw = __shfl_sync(0xffffffffu, bdual, __ffs(who) - 1);
+            const int jw = (int)key_idx(kk);
+            const int64_t r = (int64_t)key_val(kk) - ui;
+            key = vw == kDead32 || r < INT32_MIN ? row_best_exact(I.cost + (size_t)i * I.ldc, ui, c.pot + m, a, b)
+                                                 : pack_i32(clamp32(r), (uint32_t)jw);
         }
         if (lane == 0) atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)key);
     }
 }
 
-__global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivot* cp) {
+// Entries of the re-hung path the cluster rounds cache in shared memory for
+// the update's binary searches (a longer path is searched in global memory).
+constexpr int kPathCache = 8192;
+constexpr size_t kCRoundSmem = (size_t)kPathCache * (sizeof(int2) + sizeof(int32_t));
+
+// full_first: round 0 is the pivot of the full round that k_gchoose_all has
+// just priced and counted (its entering cell in gp->best, every row key
+// current); its update clears every row key for the coming candidate sweeps.
+__global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivot* cp, const GridPivot* gp,
+                                                              int full_first) {
     __shared__ BlockScratch bs;
     __shared__ PhaseLocal phl;
     __shared__ uint64_t s_red[2];
+    extern __shared__ __align__(16) unsigned char cr_smem[];
+    int2* siv = reinterpret_cast<int2*>(cr_smem);
+    int32_t* spv = reinterpret_cast<int32_t*>(siv + kPathCache);
     PhaseScope ps(c.ph, &phl, PH_SWEEP);
     const int rank = cluster_rank(), nctas = cluster_ctas();
     const int m = c.I.m, V = m + c.I.n;
@@ -805,6 +838,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     int rounds = c.sc->rounds, age = c.sc->pp_age, pivots = c.sc->pivots, ivp = c.sc->ivp, nwide = c.sc->nwide;
     const int pivots0 = pivots;
     const bool partial = c.sc->pricing != 0;
+    const uint64_t full_best = full_first ? gp->best : kNoKey;
     if (rank == 0 && threadIdx.x == 0) { cp->abort[0] = 0; cp->abort[1] = 0; }
     if (threadIdx.x == 0) cp->dwide[rank] = 0;
     const int v0 = rank * blockDim.x + threadIdx.x, stride = nctas * blockDim.x;
@@ -816,30 +850,38 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
             for (int q = 0; q < nctas; q++) nwide += cp->dwide[q];
             if (cp->abort[(r - 1) & 1]) { why = kFailed; break; }
         }
-        if (done0 || !partial || pn <= 0) { why = kAged; break; }
-        if (rounds >= max_rounds) { why = kCapped; break; }
-        if (age >= refresh) { why = kAged; break; }
+        const bool full_round = full_first && r == 0;   // the same in every CTA
+        if (done0 || (!full_round && (!partial || pn <= 0))) { why = kAged; break; }
+        if (!full_round && rounds >= max_rounds) { why = kCapped; break; }
+        if (!full_round && age >= refresh) { why = kAged; break; }
         ps.mark(PH_SWEEP);
         int bad = 0;
-        cluster_cand_sweep(c, pn, nwide == 0, rank, nctas, &bad);
+        if (!full_round) cluster_cand_sweep(c, pn, nwide == 0, rank, nctas, &bad);
         if (bad) { fail_check(c.sc, 19); cp->abort[r & 1] = 1; }
         cluster_sync_all();                                      // barrier 1
         if (rank == 0 && threadIdx.x == 0 && r > 0) cp->abort[(r - 1) & 1] = 0;   // read by all before barrier 1
-        // the entering cell: the smallest (reduced cost, row) among the candidates
+        // the entering cell: the full round's, else the smallest (reduced
+        // cost, row) among the candidates
         uint64_t best = kNoKey;
-        for (int t = threadIdx.x; t < pn; t += blockDim.x) {
-            const int i = c.prow[t];
-            if (!FLOCK_IN(i, m)) continue;
-            const uint64_t key = c.row_best[i];
-            if (key != kNoKey && key_val(key) < 0 && key_idx(key) < ncols) {
-                const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
-                best = P < best ? P : best;
+        if (full_round) {
+            best = full_best;
+        } else {
+            for (int t = threadIdx.x; t < pn; t += blockDim.x) {
+                const int i = c.prow[t];
+                if (!FLOCK_IN(i, m)) continue;
+                const uint64_t key = c.row_best[i];
+                if (key != kNoKey && key_val(key) < 0 && key_idx(key) < ncols) {
+                    const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
+                    best = P < best ? P : best;
+                }
             }
+            best = block_min_u64(best, bs);
         }
-        best = block_min_u64(best, bs);
-        if (best == kNoKey) { why = kExhausted; break; }
-        rounds++;
-        age++;
+        if (best == kNoKey || !FLOCK_IN((int)key_idx(best), m)) { why = kExhausted; break; }
+        if (!full_round) {           // the full round was counted when it was priced
+            rounds++;
+            age++;
+        }
         ps.mark(PH_CYCLE);
         const int k = (int)key_idx(best);
         const int l = m + (int)key_idx(c.row_best[k]);
@@ -896,20 +938,34 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         pp.r = r_enter;
         pp.Q = ivA[q];            // intervals of the old buffer: no CTA writes it this round
         pp.O = ivA[other];
+        // e's chain p_0..p_t and its old intervals, for the binary searches
+        const bool cached = t < kPathCache;
+        if (cached) {
+            const int base = lside ? V - 1 : 0, dir = lside ? -1 : 1;
+            for (int i = threadIdx.x; i <= t; i += blockDim.x) {
+                const int pv = c.path[base + dir * i];
+                spv[i] = pv;
+                siv[i] = FLOCK_IN(pv, V) ? ivA[pv] : make_int2(0, 0);
+            }
+        }
         if (threadIdx.x == 0) bs.i[7] = 0;
         __syncthreads();
         int dwide = 0, ubad = 0;
-        update_slice(c, pp, ivA, ivB, v0, stride, dwide, ubad);
+        update_slice(c, pp, ivA, ivB, v0, stride, dwide, ubad, cached ? spv : nullptr, cached ? siv : nullptr);
         if (ubad) { fail_check(c.sc, 24); cp->abort[r & 1] = 1; }
         if (dwide) atomicAdd(&bs.i[7], dwide);
         __syncthreads();
         if (threadIdx.x == 0) cp->dwide[rank] = bs.i[7];
-        // the candidates' keys, read by every CTA before barrier 2, cleared for the next sweep
-        if (rank == 0)
+        // the keys read by every CTA before barrier 2, cleared for the next
+        // sweep: every row's after the full round, else the candidates'
+        if (full_round) {
+            for (int i = v0; i < m; i += stride) c.row_best[i] = kNoKey;
+        } else if (rank == 0) {
             for (int t2 = threadIdx.x; t2 < pn; t2 += blockDim.x) {
                 const int i = c.prow[t2];
                 if (FLOCK_IN(i, m)) c.row_best[i] = kNoKey;
             }
+        }
         ivp ^= 1;
         pivots++;
     }
@@ -1303,8 +1359,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_solve_one(BatchArgs a) {
     bfinal_one(a, d, bs);
 }
 
-// Block size of the one-launch form by instance size.
-static int solve_one_threads(int V) { return V <= 512 ? 256 : 1024; }
+// Block size of the one-launch form by instance size (FLOCK_PLAIN_THREADS=256
+// or 1024 overrides it, for tuning).
+static int solve_one_threads(int V) {
+    const char* e = getenv("FLOCK_PLAIN_THREADS");
+    if (e && (!strcmp(e, "256") || !strcmp(e, "1024"))) return atoi(e);
+    return V <= 512 ? 256 : 1024;
+}
 static const void* solve_one_fn(int threads) {
     return threads <= 256 ? (const void*)k_solve_one<256> : (const void*)k_solve_one<1024>;
 }
@@ -1538,10 +1599,13 @@ struct PlainSolver {
         FLOCK_CK(cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBulkSmem));
         // the largest cluster the cluster rounds can be launched with (one cluster)
         cluster_ctas = 0;
-        if (cudaFuncSetAttribute(k_cround, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        if (cudaFuncSetAttribute(k_cround, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            cudaFuncSetAttribute(k_cround, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCRoundSmem) ==
+                cudaSuccess) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(kClusterMax);
             cfg.blockDim = dim3(kCRoundThreads);
+            cfg.dynamicSmemBytes = kCRoundSmem;
             int cs = 0;
             if (cudaOccupancyMaxPotentialClusterSize(&cs, (const void*)k_cround, &cfg) == cudaSuccess)
                 cluster_ctas = std::min(cs, kClusterMax);
@@ -1612,6 +1676,9 @@ struct PlainSolver {
         z.pricing = partial ? 1 : 0;
         z.pp_rows = kPPRowsLarge;             // partial pricing runs on the plain path from kGridPivotV vertices
         z.pp_refresh = kPPRefreshLarge;
+        // FLOCK_PP_ROWS (1..kPPRows) / FLOCK_PP_REFRESH (>= 1) override them, for tuning
+        if (const char* e = getenv("FLOCK_PP_ROWS")) z.pp_rows = std::min(kPPRows, std::max(1, atoi(e)));
+        if (const char* e = getenv("FLOCK_PP_REFRESH")) z.pp_refresh = std::max(1, atoi(e));
         memcpy(h_sc.p, &z, sizeof(z));
         FLOCK_CK(cudaMemcpyAsync(dsc, h_sc.p, sizeof(z), cudaMemcpyHostToDevice, stream));
         return FLOCK_OK;
@@ -1781,6 +1848,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
         cudaLaunchAttribute cattr[1];
         ccfg.gridDim = dim3(P.cluster_ctas);
         ccfg.blockDim = dim3(kCRoundThreads);
+        ccfg.dynamicSmemBytes = kCRoundSmem;
         ccfg.stream = P.stream;
         cattr[0].id = cudaLaunchAttributeClusterDimension;
         cattr[0].val.clusterDim.x = P.cluster_ctas;
@@ -1799,17 +1867,22 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                 FLOCK_CK(cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal));
                 for (int r = 0; r < chunk; r++) {
                     if (clustered) {
-                        k_sweep<<<bgrid, kBulkThreads, kBulkSmem, P.stream>>>(c, btile, bntile);
+                        // the cluster rounds leave only full sweeps to the grid
+                        k_gsweep<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
                         k_gchoose_all<<<1, 1024, 0, P.stream>>>(c, P.gp);
                     } else {
                         k_gsweep<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
                         if (partial) k_gsweep_rest<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
                         k_gchoose<<<1, 1024, 0, P.stream>>>(c, P.gp);
                     }
-                    k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                    k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                    k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
-                    if (clustered) FLOCK_CK(cudaLaunchKernelEx(&ccfg, k_cround, c, P.cp));
+                    if (clustered) {
+                        // the full round's pivot and the candidate rounds in one cluster launch
+                        FLOCK_CK(cudaLaunchKernelEx(&ccfg, k_cround, c, P.cp, (const GridPivot*)P.gp, 1));
+                    } else {
+                        k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                        k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                        k_gupdate<<<gg, 256, 0, P.stream>>>(c, P.gp);
+                    }
                 }
                 FLOCK_CK(cudaStreamEndCapture(P.stream, &g));
                 FLOCK_CK(cudaGraphInstantiate(&exec, g, 0));
@@ -2873,6 +2946,18 @@ int flock_bench_batch_cells(int64_t* cells) { return flock::batch_cells(cells); 
 
 /* Benchmark hook: average device time of the fused reduced-cost sweep on an
  * m x n matrix (random costs and duals, inputs resident). */
+// Benchmark hook: CTAs of the grid path's cluster rounds on this device (0:
+// the six-kernel rounds only).
+int flock_bench_cluster_ctas(int32_t* ctas) {
+    if (!ctas) return FLOCK_ERR_ARG;
+    flock::PlainSolver& P = flock::plain();
+    std::lock_guard<std::mutex> lk(P.mu);
+    const int rc = P.setup();
+    if (rc) return rc;
+    *ctas = P.cluster_ctas;
+    return FLOCK_OK;
+}
+
 int flock_bench_sweep(int32_t m, int32_t n, int32_t iters, float* avg_ms, int32_t* tile) {
     return flock::bench_sweep(m, n, iters, avg_ms, tile);
 }
