@@ -87,13 +87,14 @@ enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1, FLOCK_BFS_VOGEL_DEVICE = 2 };
 enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2, FLOCK_PIVOT_SS = 3 };
 /* Pricing.  FULL: every round sweeps every cell (the reference's Dantzig rule,
  * uv_model_parallel.cu:151-200).  PARTIAL (the default; no counterpart in the
- * reference):
- * a full sweep keeps the 64 rows with the most negative reduced costs as
- * candidates and the following rounds re-price only those rows, until they
- * hold no negative reduced cost or 32 rounds have passed; optimality is only
- * declared after a full sweep.  Batched and served forms, and the plain
- * solver's grid-wide rounds (m + n >= 4096); smaller plain instances always
- * price fully.  The optimum is the same; the pivot sequence differs. */
+ * reference): a full sweep keeps the R rows with the most negative reduced
+ * costs as candidates and the following rounds re-price only those rows,
+ * until they hold no negative reduced cost or K rounds have passed;
+ * optimality is only declared after a full sweep.  R / K: 32 / 8 for
+ * instances of up to 1024 vertices, 64 / 32 up to 4095 (batched and served
+ * forms, the plain one-launch solve), 128 / 64 for the plain solver from 4096
+ * vertices.  The optimum is the same; the pivot sequence differs.  FLOCK_PIVOT_SS
+ * always prices fully. */
 enum { FLOCK_PRICING_FULL = 0, FLOCK_PRICING_PARTIAL = 1 };
 
 typedef struct {
