@@ -163,18 +163,17 @@ def cpu_model() -> str:
 
 
 def sweep_bytes(fg) -> int:
-    """Cost bytes the batched kernels' sweeps read in the last batch, counted
-    on the device: per priced cell 2 bytes when the instance's costs fit the
-    16-bit copy the sweeps read, else 4 (partial-pricing rounds price only
+    """Cost bytes the batched kernels' sweeps read in the last batch: 4 bytes
+    per priced cell, counted on the device (partial-pricing rounds price only
     their candidate rows)."""
     import ctypes
     L = fg.lib()
-    L.flock_bench_batch_sweep_bytes.argtypes = [ctypes.POINTER(ctypes.c_int64)]
-    b = ctypes.c_int64()
-    rc = L.flock_bench_batch_sweep_bytes(ctypes.byref(b))
+    L.flock_bench_batch_cells.argtypes = [ctypes.POINTER(ctypes.c_int64)]
+    cells = ctypes.c_int64()
+    rc = L.flock_bench_batch_cells(ctypes.byref(cells))
     if rc:
-        raise RuntimeError(f"sweep byte count failed: {rc}")
-    return int(b.value)
+        raise RuntimeError(f"cell count failed: {rc}")
+    return 4 * int(cells.value)
 
 
 def run_reference(args, world, rank, pg):
@@ -290,10 +289,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": DRAM_BYTES_PER_BATCH,
                      "kernel": "k_bsolve (persistent batched solve)", "peak_src": peaks["src"],
-                     "note": "algorithmic bytes = cost bytes read by the sweeps (counted on the device: 2 per "
-                             "cell priced from the 16-bit copy, 4 otherwise; partial-pricing rounds price their "
-                             "candidate rows only); per-instance matrices are re-read from L2, so this is not "
-                             "DRAM traffic"},
+                     "note": "algorithmic bytes = 4 x cost cells priced by the sweeps (counted on the device; "
+                             "partial-pricing rounds price their candidate rows only); per-instance matrices "
+                             "are re-read from L2, so this is not DRAM traffic"},
         "clocks": clk,
     }
     if rank == 0 and not args.no_extras:

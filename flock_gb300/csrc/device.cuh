@@ -44,7 +44,7 @@ constexpr uint64_t kNoKey = ~0ull;
 // default of the batched kernels (64 registers) and the plain solver's.
 constexpr int kJump = 2;
 constexpr int kJumpPlain = 4;
-constexpr int kPPRows = 256;     // partial pricing: capacity of the candidate-row list
+constexpr int kPPRows = 128;     // partial pricing: capacity of the candidate-row list
 // Partial pricing settings (Scalars::pp_rows / pp_refresh): candidate rows
 // kept by a full sweep and rounds between full sweeps.  Instances of up to
 // kPPSmallV vertices (a full sweep is cheap next to a round's fixed cost)
@@ -88,7 +88,7 @@ struct Scalars {
     int32_t ivp;           // which half of Ctx::iv holds the current preorder intervals
     int32_t nwide;         // live column duals outside the int32 window (narrow == (nwide == 0))
     int32_t stale;         // 1: depth, duals and intervals must be rebuilt from parent[] (tree_build_cta)
-    int32_t c16;           // 1: Ctx::cost16 holds every cost (they all fit 16 bits); the block sweeps read it
+    int32_t pad_;
 };
 
 // Phase clock of the plain solver: device time per phase of the simplex,
@@ -240,9 +240,6 @@ struct Ctx {
     int32_t* csr_adj;     // 2V
     int32_t* order;       // V  (BFS order of the start tree)
     int32_t* uf;          // V  union-find
-    // 16-bit copy of the costs, m rows of ceil8(n), for the block sweeps
-    // (null unless carved; used only when Scalars::c16 says every cost fits)
-    int16_t* cost16;
     // phase clock of the plain solver (null elsewhere; see PhaseClock)
     PhaseClock* ph;
 };

@@ -7,8 +7,7 @@
 // Environment: EMU_THREADS (block size, a multiple of 32, default 32),
 // EMU_VERIFY (1, default: after every single pivot the incrementally updated
 // depths, duals, int32 duals and preorder intervals are checked against a full
-// rebuild), EMU_COST16 (1: the sweeps read a 16-bit copy of the costs),
-// EMU_COST_HI / EMU_QTY_LO / EMU_QTY_HI (generator ranges; small
+// rebuild), EMU_COST_HI / EMU_QTY_LO / EMU_QTY_HI (generator ranges; small
 // ranges give ties and degenerate bases), EMU_PP_ROWS / EMU_PP_REFRESH
 // (partial pricing settings, default 64 and 32), EMU_FILE (solve the
 // instance of that binary instance file instead).
@@ -121,9 +120,6 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
     c.top2 = arr<int4>(keep, V); c.rescan = arr<int32_t>(keep, V);
     c.bsum = arr<int64_t>(keep, V); c.csr_start = arr<int32_t>(keep, V + 1);
     c.csr_adj = arr<int32_t>(keep, 2 * V); c.order = arr<int32_t>(keep, V); c.uf = arr<int32_t>(keep, V);
-    // EMU_COST16=1: the block sweeps read the 16-bit copy of the costs
-    const bool c16 = getenv("EMU_COST16") && atoi(getenv("EMU_COST16"));
-    c.cost16 = c16 ? arr<int16_t>(keep, (size_t)m * ((n + 7) & ~7)) : nullptr;
     c.ph = nullptr;
     BlockScratch bs;
     TreeState saved;
@@ -132,7 +128,6 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
         vogel_cta(c, bs);
         if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
         __syncthreads();
-        cost16_cta(c);
         sf_init_cta(c, bs);
         if (!c.sc->done) tree_build_cta(c, bs);
         uint64_t junk = 0x9E3779B97F4A7C15ull;
@@ -149,7 +144,7 @@ static int solve_one(int m, int n, const int32_t* s, const int32_t* d, const int
             const bool partial = c.sc->pricing != 0;
             if (partial) entering = sweep_partial_cta(c, bs);
             else sweep_cta(c);
-            pivot_round_cta(c, bs, partial, entering);
+            pivot_round_cta<kJump, true>(c, bs, partial, entering);
             if (threadIdx.x == 0) c.sc->rounds++;
             __syncthreads();
             if (c.sc->done) break;

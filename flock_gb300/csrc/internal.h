@@ -31,7 +31,6 @@ struct BatchArgs {
     int32_t light;              // 1: stage only the per-step tree arrays (largest buckets)
     int32_t pricing;            // Scalars::pricing of every instance
     PhaseClock* ph;             // phase clock (the plain solver's one-launch form only; null otherwise)
-    int32_t c16;                // 1: make the 16-bit copy of the costs for the sweeps where they fit
 };
 
 // A served request's device region: byte offsets of its arrays (256-aligned).
@@ -58,11 +57,9 @@ struct Carver {
 // Assign every working array of `c` for instances with at most V vertices and
 // M rows.  With `smem` the arrays touched by every pivot step live in shared
 // memory, the rest in the global region `g`.  Returns the bytes used in both.
-// with16: also the 16-bit copy of the costs (the block forms: batched,
-// served and the plain one-launch solve).
 __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsigned char* smem,
                                           int64_t* pot_global, size_t* smem_bytes = nullptr,
-                                          size_t* global_bytes = nullptr, bool with16 = false) {
+                                          size_t* global_bytes = nullptr) {
     Carver k{g, 0, smem, 0};
     const size_t v = (size_t)V, mm = (size_t)M;
     c.parent = (int32_t*)k.S(4 * v);
@@ -95,7 +92,6 @@ __host__ __device__ inline void carve_ctx(Ctx& c, uint8_t* g, int V, int M, unsi
     c.csr_adj = (int32_t*)k.G(8 * v);
     c.order = (int32_t*)k.G(4 * v);
     c.uf = (int32_t*)k.G(4 * v);
-    c.cost16 = with16 ? (int16_t*)k.G(2 * mm * (((size_t)(V - M) + 7) & ~size_t(7))) : nullptr;
     c.ph = nullptr;
     if (smem_bytes) *smem_bytes = k.so;
     if (global_bytes) *global_bytes = (k.go + 255) & ~size_t(255);

@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(1024, 1) k_pivot(Ctx c) {
     __shared__ PhaseLocal phl;
     PhaseScope ps(c.ph, &phl, PH_SWEEP);   // the entering choice is part of pricing
     if (c.sc->done) { ps.idle(); return; }
-    pivot_round_cta<kJumpPlain>(c, bs, false, kNoKey, &ps);
+    pivot_round_cta<kJumpPlain, true>(c, bs, false, kNoKey, &ps);
     if (threadIdx.x == 0) {
         c.sc->rounds++;
         if (!c.sc->done && c.sc->rounds >= c.sc->max_rounds) { c.sc->status |= ST_ITER_CAP; c.sc->done = 1; }
@@ -1067,7 +1067,7 @@ __device__ __forceinline__ void batch_ctx(const BatchArgs& a, const BatchDesc& d
     g.I.demand = d.sd + d.m;
     g.sc = d.sc;
     g.out_src = d.out; g.out_dst = d.out + V1; g.out_qty = d.out + 2 * V1;
-    carve_ctx(g, d.ws, d.m + d.n, d.m, nullptr, d.pot, nullptr, nullptr, true);
+    carve_ctx(g, d.ws, d.m + d.n, d.m, nullptr, d.pot);
 }
 
 // returns the next instance of this launch for the CTA, or -1
@@ -1164,7 +1164,6 @@ __device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& 
         Carver kt = k;
         SetupStage::tree(c, kt, V);
     }
-    if (a.c16) cost16_cta(g);   // the sweeps' 16-bit copy when every cost fits
     sf_init_cta(c, bs);
     if (kStage) {
         for (int v = threadIdx.x; v < V; v += blockDim.x) g.parent[v] = c.parent[v];
@@ -1560,13 +1559,6 @@ static int pivot_mode(const flock_options& o) {
     }
 }
 
-// BatchArgs::c16: the 16-bit copy of the costs for the block sweeps, on
-// unless FLOCK_COST16=0 (for comparisons).
-static int cost16_enabled() {
-    const char* e = getenv("FLOCK_COST16");
-    return e && !strcmp(e, "0") ? 0 : 1;
-}
-
 // Scalars::pricing of the options: partial pricing unless FULL was asked for
 // or the pivot method prices every cell (parallel stepping stone).
 static int pricing_of(const flock_options& o) {
@@ -1751,7 +1743,6 @@ static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock
     a.max_rounds = max_rounds;
     a.light = stage_light(V, m) ? 1 : 0;
     a.ph = d_ph;
-    a.c16 = cost16_enabled();
     const size_t smem = launch_smem_bytes(V, m, a.light != 0);
     const int threads = solve_one_threads(V);
     const void* fn = solve_one_fn(threads);
@@ -1825,7 +1816,9 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     const int nt = threads_for(V);
     const int bfs = opt.bfs_method == FLOCK_BFS_NWC || opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE ? opt.bfs_method
                                                                                                   : FLOCK_BFS_VOGEL;
-    if (V < kGridPivotV && bfs != FLOCK_BFS_VOGEL_DEVICE)
+    // the one-launch form below the grid size (the stepping-stone mode runs
+    // its rounds on the round kernel at every size)
+    if (V < kGridPivotV && bfs != FLOCK_BFS_VOGEL_DEVICE && pivot_mode(opt) != 3)
         return solve_one_launch(P, I, opt, c, bfs, max_rounds, flows, du, dv, st, t0);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     int2 *rbook = nullptr, *cbook = nullptr;
@@ -2210,7 +2203,7 @@ static TuneCfg default_cfg(int maxV) {
 static size_t instance_ws_bytes(int V, int m) {
     Ctx probe;
     size_t gb = 0;
-    carve_ctx(probe, nullptr, V, m, nullptr, (int64_t*)16, nullptr, &gb, true);
+    carve_ctx(probe, nullptr, V, m, nullptr, (int64_t*)16, nullptr, &gb);
     return al256(gb);
 }
 
@@ -2264,6 +2257,10 @@ struct BatchRunner {
         if (opt_in) opt = *opt_in;
         if (opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE) {
             set_error("vam_device Vogel runs on flock_solve and flock_vogel_device only");
+            return FLOCK_ERR_ARG;
+        }
+        if (opt.pivot_method == FLOCK_PIVOT_SS) {
+            set_error("the parallel stepping-stone mode runs on flock_solve only");
             return FLOCK_ERR_ARG;
         }
         insts = in;
@@ -2451,7 +2448,6 @@ struct BatchRunner {
     BatchArgs args_for(int b) {
         BatchArgs a;
         a.ph = nullptr;
-        a.c16 = cost16_enabled();
         a.desc = d_desc.as<BatchDesc>() + bstart[b];
         a.count = bstart[b + 1] - bstart[b];
         a.next = nullptr; a.active = nullptr;
@@ -2806,7 +2802,6 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     if (count < 1 || maxV > kMaxStagedV) return FLOCK_ERR_ARG;
     BatchArgs a;
     a.ph = nullptr;
-    a.c16 = cost16_enabled();
     a.desc = d_desc;
     a.count = count;
     a.next = d_next;
@@ -2890,20 +2885,13 @@ static int batch_solve(int cnt, const flock_instance* insts, const flock_options
 
 // Benchmark hook: cost cells priced by the CTA sweeps of the last batch
 // (every instance solved by the batched kernels).
-// cells: cost cells priced; bytes (optional): the cost bytes those sweeps
-// read (2 per cell from an instance's 16-bit copy, else 4).
-int batch_cells(int64_t* cells, int64_t* bytes = nullptr) {
+int batch_cells(int64_t* cells) {
     std::lock_guard<std::mutex> lk(g_batch_mu);
     if (!g_batch || !cells) return FLOCK_ERR_ARG;
-    int64_t t = 0, b = 0;
+    int64_t t = 0;
     for (int k = 0; k < g_batch->count; k++)
-        if (g_batch->V_of[k] <= kMaxStagedV) {
-            const Scalars& S = g_batch->h_sc.as<Scalars>()[k];
-            t += S.cells;
-            b += S.cells * (S.c16 ? 2 : 4);
-        }
+        if (g_batch->V_of[k] <= kMaxStagedV) t += g_batch->h_sc.as<Scalars>()[k].cells;
     *cells = t;
-    if (bytes) *bytes = b;
     return FLOCK_OK;
 }
 
@@ -2961,13 +2949,6 @@ int flock_bench_batch_rerun(float* ms, int32_t* launches) { return flock::batch_
 /* Benchmark hook: cost cells priced by the batched kernels' sweeps in the last
  * batch (after a re-solve, the re-solve's count). */
 int flock_bench_batch_cells(int64_t* cells) { return flock::batch_cells(cells); }
-
-/* Benchmark hook: cost bytes the batched kernels' sweeps read in the last
- * batch (2 per cell priced from a 16-bit copy, 4 otherwise). */
-int flock_bench_batch_sweep_bytes(int64_t* bytes) {
-    int64_t cells = 0;
-    return flock::batch_cells(&cells, bytes);
-}
 
 /* Benchmark hook: average device time of the fused reduced-cost sweep on an
  * m x n matrix (random costs and duals, inputs resident). */

@@ -453,6 +453,7 @@ int64_t flock_server_request_bytes(int32_t m, int32_t n) {
 int flock_server_create(const flock_server_config* cfg, flock_server** out) {
     if (!out) return FLOCK_ERR_ARG;
     if (cfg && cfg->options.bfs_method == FLOCK_BFS_VOGEL_DEVICE) return FLOCK_ERR_ARG;   // plain solve only
+    if (cfg && cfg->options.pivot_method == FLOCK_PIVOT_SS) return FLOCK_ERR_ARG;       // plain solve only
     flock_server* s = new flock_server();
     if (cfg) s->cfg = *cfg; else flock_default_server_config(&s->cfg);
     if (s->cfg.max_inflight_batches < 1) s->cfg.max_inflight_batches = 1;

@@ -470,40 +470,6 @@ __device__ __forceinline__ uint64_t narrow_row_key(const Ctx& c, int i, int j0, 
     return pack_i32(clamp32(r), (uint32_t)jw);
 }
 
-// Narrow form over 8 costs of the 16-bit copy (one 16-byte load) against
-// 8 int32 duals: element 2k is the low half of word k.
-__device__ __forceinline__ void min8(int32_t& bv, int32_t& bj, const int4 c8, const int4 v0, const int4 v1, int j) {
-    int32_t t;
-    t = (int32_t)(int16_t)c8.x - v0.x; if (t < bv) { bv = t; bj = j; }
-    t = (c8.x >> 16) - v0.y;           if (t < bv) { bv = t; bj = j + 1; }
-    t = (int32_t)(int16_t)c8.y - v0.z; if (t < bv) { bv = t; bj = j + 2; }
-    t = (c8.y >> 16) - v0.w;           if (t < bv) { bv = t; bj = j + 3; }
-    t = (int32_t)(int16_t)c8.z - v1.x; if (t < bv) { bv = t; bj = j + 4; }
-    t = (c8.z >> 16) - v1.y;           if (t < bv) { bv = t; bj = j + 5; }
-    t = (int32_t)(int16_t)c8.w - v1.z; if (t < bv) { bv = t; bj = j + 6; }
-    t = (c8.w >> 16) - v1.w;           if (t < bv) { bv = t; bj = j + 7; }
-}
-
-// The 16-bit copy of the costs (rows of ceil8(n), padding zero) when every
-// cost fits 16 bits; sets Scalars::c16.  All threads of the block; ends with
-// a barrier.  Nothing happens without a carved copy.
-__device__ void cost16_cta(const Ctx& c) {
-    if (!c.cost16) return;                                    // uniform
-    const InstDev& I = c.I;
-    const int ld16 = (I.n + 7) & ~7;
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    int bad = 0;
-    for (int i = threadIdx.x >> 5; i < I.m; i += nw)
-        for (int j = lane; j < ld16; j += 32) {
-            const int32_t v = j < I.n ? I.cost[(size_t)i * I.ldc + j] : 0;
-            bad |= v < -32768 || v > 32767;
-            c.cost16[(size_t)i * ld16 + j] = (int16_t)v;
-        }
-    bad = __syncthreads_or(bad);
-    if (threadIdx.x == 0) c.sc->c16 = bad ? 0 : 1;
-    __syncthreads();
-}
-
 // CTA-local sweep of the rows list[0..cnt) (all rows 0..cnt-1 when list is
 // null): best (reduced cost, column) of each into row_best[].  Rows are
 // int4-vectorised (row pitch a multiple of 4, 16-byte aligned); a warp takes
@@ -525,27 +491,6 @@ __device__ void sweep_rows_cta(const Ctx& c, const int32_t* list, int cnt) {
         return;
     }
     const int4* v4 = reinterpret_cast<const int4*>(c.v32);
-    if (c.sc->c16 && c.cost16) {       // every cost in the 16-bit copy: 8 per load, one row per warp pass
-        const int ld16 = (n + 7) & ~7;
-        const int noct = n >> 3, tail8 = n & 7;
-        for (int t = threadIdx.x >> 5; t < cnt; t += nw) {
-            const int i = list ? list[t] : t;
-            if (!FLOCK_IN(i, m)) { if (lane == 0) fail_check(c.sc, 19); continue; }
-            const int16_t* row = c.cost16 + (size_t)i * ld16;
-            const int4* r8 = reinterpret_cast<const int4*>(row);
-            int32_t bv = INT32_MAX, bj = INT32_MAX;
-            for (int q = lane; q < noct; q += 32) min8(bv, bj, r8[q], v4[2 * q], v4[2 * q + 1], 8 * q);
-            if (lane < tail8) {
-                const int j = 8 * noct + lane;
-                const int32_t tv = (int32_t)row[j] - c.v32[j];
-                if (tv < bv) { bv = tv; bj = j; }
-            }
-            const uint64_t k = narrow_row_key(c, i, 0, n, bv, bj);
-            if (lane == 0) c.row_best[i] = k;
-        }
-        __syncthreads();
-        return;
-    }
     const int nfull = n >> 2, tail = n & 3;
     for (int t = threadIdx.x >> 5; t < cnt; t += 2 * nw) {
         const int t2 = t + nw;
@@ -1119,13 +1064,16 @@ constexpr int kSwitchPivots = 10;
 // have_best: the sweep already reduced the sequential rule's entering row
 // (pre_best, kNoKey: none).  With partial pricing only the listed candidate
 // rows hold keys this round, and only they are read.
-template <int J = kJump>
+// kSS: the parallel stepping-stone mode (Scalars::mode 3) is compiled in
+// (the plain solver's round kernel); the persistent kernels leave it out and
+// keep their registers.
+template <int J = kJump, bool kSS = false>
 __device__ void pivot_round_cta(const Ctx& c, BlockScratch& bs, bool have_best = false, uint64_t pre_best = kNoKey,
                                 PhaseScope* ps = nullptr) {
     const InstDev& I = c.I;
     const int m = I.m, V = m + I.n;
     const int mode = c.sc->mode;
-    if (mode == 3) {          // parallel stepping stone (full pricing: every row key is current)
+    if (kSS && mode == 3) {   // parallel stepping stone (full pricing: every row key is current)
         if (ps) ps->mark(PH_CYCLE);
         ss_round_cta<J>(c, bs, ps);
         return;

@@ -82,8 +82,8 @@ enum { FLOCK_BFS_NWC = 0, FLOCK_BFS_VOGEL = 1, FLOCK_BFS_VOGEL_DEVICE = 2 };
  * round); they are taken most negative first and a cycle is accepted unless
  * it shares a tree edge with one accepted before it; all accepted cycles
  * pivot in the same round.  SS prices every cell each round (the pricing
- * option is ignored); instances of 4096 or more vertices run its rounds on
- * one block. */
+ * option is ignored), runs its rounds on one block at every size, and is
+ * flock_solve's only (the batched and served forms return FLOCK_ERR_ARG). */
 enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH = 2, FLOCK_PIVOT_SS = 3 };
 /* Pricing.  FULL: every round sweeps every cell (the reference's Dantzig rule,
  * uv_model_parallel.cu:151-200).  PARTIAL (the default; no counterpart in the

@@ -113,10 +113,3 @@ def test_emulated_stepping_stone_degenerate(emu):
     candidate cells per round, overlapping cycles resolved by claim rounds."""
     run(emu, [78, 6, 5, 50, 0, 5, 3, 0], {"EMU_THREADS": "64", "EMU_COST_HI": "3", "EMU_QTY_LO": "1",
                                           "EMU_QTY_HI": "3"})
-
-
-@pytest.mark.parametrize("mode,pricing", [(2, 1), (0, 0), (3, 0)])
-def test_emulated_cost16_sweeps(emu, mode, pricing):
-    """The block sweeps on the 16-bit copy of the costs (every cost fits 16
-    bits): the same certified optima, row widths not a multiple of 8."""
-    run(emu, [20251204, 6, 10, 61, 0, 5, mode, pricing], {"EMU_THREADS": "64", "EMU_COST16": "1"})

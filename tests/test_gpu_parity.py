@@ -459,18 +459,17 @@ def test_ss_degenerate_1000_full_size():
     assert ss.pivots >= ss.iterations - 1
 
 
-def test_ss_batched_and_large_plain():
-    """The batched form with ss pivots on every size bucket up to 4096
-    vertices, and a plain instance of 4096 vertices (its ss rounds on one
-    block): same optima as the default pivots."""
-    sizes = [(20, 30), (60, 60), (100, 120), (200, 250), (400, 500), (900, 1000), (1400, 1500), (2000, 2000)]
-    insts = [fg.generate(0, 600 + k, m, n, 1, 1000, 100, 1000) for k, (m, n) in enumerate(sizes)]
-    a = fg.batch_solve(insts, pivot="ss")
-    b = fg.batch_solve(insts)
-    for k, inst in enumerate(insts):
-        assert a[k].status == 0 and a[k].certified, k
-        assert a[k].objective == b[k].objective, k
-    big = fg.generate(0, 700, 2048, 2048, 1, 1000, 100, 1000)
-    r = fg.solve(big, pivot="ss")
-    d = fg.solve(big)
-    assert r.status == 0 and r.certified and r.objective == d.objective
+def test_ss_plain_sizes_and_batched_rejected():
+    """ss pivots on plain instances across the size range (round kernel at
+    every size, up to 4096 vertices): the same optima as the default pivots.
+    The batched and served forms refuse the mode (flock_solve only)."""
+    sizes = [(20, 30), (100, 120), (400, 500), (1400, 1500), (2048, 2048)]
+    for k, (m, n) in enumerate(sizes):
+        inst = fg.generate(0, 600 + k, m, n, 1, 1000, 100, 1000)
+        r = fg.solve(inst, pivot="ss")
+        d = fg.solve(inst)
+        assert r.status == 0 and r.certified and r.objective == d.objective, (m, n)
+    small = fg.generate(0, 650, 30, 40, 1, 1000, 100, 1000)
+    with pytest.raises(fg.FlockError) as ex:
+        fg.batch_solve([small], pivot="ss")
+    assert ex.value.status == fg.FLOCK_ERR_ARG
