@@ -32,8 +32,8 @@ BATCH = 4096
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one batched
 # solve of this workload (the autotuned block sizes pinned) and of one
 # 8000 x 8000 sweep, from ncu captures of this benchmark's own launches.
-DRAM_BYTES_PER_BATCH = 3_327_000_000
-DRAM_BYTES_SWEEP_8000 = 259_300_000
+DRAM_BYTES_PER_BATCH = 886_000_000
+DRAM_BYTES_SWEEP_8000 = 259_900_000
 LO, HI = 10, 500
 SEED = 20251203
 

@@ -31,6 +31,9 @@ struct BatchArgs {
     int32_t light;              // 1: stage only the per-step tree arrays (largest buckets)
     int32_t pricing;            // Scalars::pricing of every instance
     PhaseClock* ph;             // phase clock (the plain solver's one-launch form only; null otherwise)
+    // partial pricing per instance: candidate rows and rounds between full
+    // sweeps up to kPPSmallV vertices ([0], [1]) and above ([2], [3])
+    int32_t pp[4];
 };
 
 // A served request's device region: byte offsets of its arrays (256-aligned).

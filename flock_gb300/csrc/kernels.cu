@@ -1142,8 +1142,8 @@ __device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& 
         z.mode = a.mode;
         z.pricing = a.pricing;
         const bool small = d.m + d.n <= kPPSmallV;
-        z.pp_rows = small ? kPPRowsSmall : kPPRowsLarge;
-        z.pp_refresh = small ? kPPRefreshSmall : kPPRefreshLarge;
+        z.pp_rows = min(max(small ? a.pp[0] : a.pp[2], 1), kPPRows);
+        z.pp_refresh = max(small ? a.pp[1] : a.pp[3], 1);
         *c.sc = z;
     }
     __syncthreads();
@@ -1559,6 +1559,18 @@ static int pivot_mode(const flock_options& o) {
     }
 }
 
+// BatchArgs::pp: the partial-pricing settings of the block forms
+// (kPPRowsSmall, kPPRefreshSmall, kPPRowsLarge, kPPRefreshLarge);
+// FLOCK_BPP="r,k,R,K" overrides them, for tuning.
+static void block_pricing(int32_t* pp) {
+    pp[0] = kPPRowsSmall; pp[1] = kPPRefreshSmall; pp[2] = kPPRowsLarge; pp[3] = kPPRefreshLarge;
+    if (const char* e = getenv("FLOCK_BPP")) {
+        int v[4];
+        if (sscanf(e, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) == 4)
+            for (int k = 0; k < 4; k++) pp[k] = v[k];
+    }
+}
+
 // Scalars::pricing of the options: partial pricing unless FULL was asked for
 // or the pivot method prices every cell (parallel stepping stone).
 static int pricing_of(const flock_options& o) {
@@ -1743,6 +1755,7 @@ static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock
     a.max_rounds = max_rounds;
     a.light = stage_light(V, m) ? 1 : 0;
     a.ph = d_ph;
+    block_pricing(a.pp);
     const size_t smem = launch_smem_bytes(V, m, a.light != 0);
     const int threads = solve_one_threads(V);
     const void* fn = solve_one_fn(threads);
@@ -2448,6 +2461,7 @@ struct BatchRunner {
     BatchArgs args_for(int b) {
         BatchArgs a;
         a.ph = nullptr;
+        block_pricing(a.pp);
         a.desc = d_desc.as<BatchDesc>() + bstart[b];
         a.count = bstart[b + 1] - bstart[b];
         a.next = nullptr; a.active = nullptr;
@@ -2802,6 +2816,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     if (count < 1 || maxV > kMaxStagedV) return FLOCK_ERR_ARG;
     BatchArgs a;
     a.ph = nullptr;
+    block_pricing(a.pp);
     a.desc = d_desc;
     a.count = count;
     a.next = d_next;
