@@ -277,6 +277,7 @@ def main():
 
     peaks = measured_peaks()
     achieved = alg_bytes / (avg_launch_ms * 1e-3) / 1e9
+    l2 = l2_peak(fg)
     line = {
         "metric": "exact-opt solves/sec (mixed batch 4096, m,n log-uniform [10,500])",
         "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
@@ -291,7 +292,9 @@ def main():
                      "kernel": "k_bsolve (persistent batched solve)", "peak_src": peaks["src"],
                      "note": "algorithmic bytes = 4 x cost cells priced by the sweeps (counted on the device; "
                              "partial-pricing rounds price their candidate rows only); per-instance matrices "
-                             "are re-read from L2, so this is not DRAM traffic"},
+                             "are re-read from L2, so this is not DRAM traffic",
+                     "l2": {"peak": l2["gbs"], "frac": achieved / l2["gbs"], "unit": "GB/s",
+                            "peak_src": "builder-measured: " + l2["how"]}},
         "clocks": clk,
     }
     if rank == 0 and not args.no_extras:
@@ -321,6 +324,10 @@ def extras(fg, insts, res, peaks) -> dict:
     gbs = sb / (ms * 1e-3) / 1e9
     out["sweep_8000"] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                          "ms": ms, "bytes": sb, "traffic": DRAM_BYTES_SWEEP_8000, "kernel": "k_sweep"}
+    ms16 = fg_sweep_ms(fg, 16000, 16000, 20)
+    sb16 = 4 * 16000 * 16000 + 4 * 32000
+    out["sweep_16000"] = {"achieved": sb16 / (ms16 * 1e-3) / 1e9, "frac": sb16 / (ms16 * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                          "ms": ms16, "bytes": sb16, "kernel": "k_sweep"}
     out["plain_configs"] = plain_configs(fg)
     out["served"] = served(fg)
     out["cpu_baseline"] = cpu_baseline(fg, insts, res)
@@ -533,6 +540,25 @@ def plain_configs(fg) -> dict:
                 bfs[label] = {"error": str(ex)}
         out[name]["bfs_ms"] = bfs
     return out
+
+
+def l2_peak(fg) -> dict:
+    """L2 read bandwidth of this GPU, measured here: k_l2_read makes passes
+    over an L2-resident buffer (ld.global.cg, L1 bypassed, 2 GB read per
+    launch), best of 64 MB and 96 MB buffers, 10 launches each."""
+    import ctypes
+    L = fg.lib()
+    L.flock_bench_l2.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]
+    best = 0.0
+    for mb in (64, 96):
+        b = mb << 20
+        passes = max(1, (2 << 30) // b)
+        ms = ctypes.c_float()
+        rc = L.flock_bench_l2(b, passes, 10, ctypes.byref(ms))
+        if rc:
+            raise RuntimeError(f"L2 bench failed: {rc}")
+        best = max(best, b * passes / (ms.value * 1e-3) / 1e9)
+    return {"gbs": best, "how": "k_l2_read, passes over a 64/96 MB buffer, 2 GB per launch"}
 
 
 def fg_sweep_ms(fg, m, n, iters) -> float:

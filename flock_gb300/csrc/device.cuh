@@ -102,7 +102,7 @@ struct Scalars {
 // add up to the loop's device time (launch gaps included in the phase before
 // them).  Kernels that find the solve finished count as idle.
 enum : int32_t { PH_BFS = 0, PH_DUAL, PH_SWEEP, PH_CYCLE, PH_RESOLVE, PH_ADJUST, PH_IDLE, kPhases };
-struct PhaseClock {
+struct __align__(16) PhaseClock {
     uint64_t last;          // globaltimer at the start of the running segment (0: none yet)
     int32_t cur;            // phase of the running segment
     int32_t pad_;
@@ -119,8 +119,10 @@ __device__ __forceinline__ uint64_t global_ns() {
 #endif
 }
 
-// Shared-memory state of one launch's phase accounting (block 0 only).
-struct PhaseLocal {
+// Shared-memory state of one launch's phase accounting (block 0 only).  Its
+// first 16 bytes are the destination of a 16-byte cp.async, which needs a
+// 16-byte aligned shared address.
+struct __align__(16) PhaseLocal {
     uint64_t prev_last;     // the clock's `last` and `cur` as the previous launch left them
     int32_t prev_cur, pad_;
     uint64_t t0, t;         // this launch's start, start of its running segment

@@ -146,6 +146,7 @@ inline unsigned emu_gather(unsigned v, int how) {
 inline unsigned __reduce_add_sync(unsigned, unsigned v) { return emu_gather(v, 0); }
 inline unsigned __ballot_sync(unsigned, int p) { return emu_gather(p ? 1u : 0u, 1); }
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
+inline int __ffs(int x) { return __builtin_ffs(x); }
 
 template <class T, class U> inline T atomicAdd(T* p, U v) { return std::atomic_ref<T>(*p).fetch_add((T)v); }
 template <class T, class U> inline T atomicOr(T* p, U v) { return std::atomic_ref<T>(*p).fetch_or((T)v); }

@@ -1,7 +1,8 @@
 // emu_vogel_device.cpp -- runs the device functions of the "vam_device" Vogel
-// variant (book_line_cta for every line, then vogel_books_cta) on an emulated
-// CTA (cuda_emu.h) under AddressSanitizer / UBSan, for the binary instance
-// files given as arguments, and prints each allocation list:
+// variant (book_line_cta for every line, then vogel_books_cta) or, with
+// EMU_VOGEL=host, the "vam_host" Vogel (vogel_cta) on an emulated CTA
+// (cuda_emu.h) under AddressSanitizer / UBSan, for the binary instance files
+// given as arguments, and prints each allocation list:
 //   <file> events=<e> barrier_mismatch=<k> flows=<src>,<dst>,<qty>;...
 // The test harness compares the lists with its own expectation.
 // Environment: EMU_THREADS (block size, a multiple of 32, default 64).
@@ -42,6 +43,20 @@ static int run_one(const char* path) {
     c.bfs_src = arr<int32_t>(keep, V); c.bfs_dst = arr<int32_t>(keep, V); c.bfs_qty = arr<int32_t>(keep, V);
     c.res = arr<int32_t>(keep, V);
     c.top2 = arr<int4>(keep, V);
+    const char* variant = getenv("EMU_VOGEL");
+    if (variant && !strcmp(variant, "host")) {
+        c.covered = arr<uint8_t>(keep, V);
+        c.diff = arr<int32_t>(keep, V);
+        c.rescan = arr<int32_t>(keep, V);
+        BlockScratch bs;
+        const int r = emu::run_cta([&] { vogel_cta(c, bs); });
+        const int mism = r ? (r < 0 ? 1000 : r) : 0;
+        printf("%s events=%d barrier_mismatch=%d flows=", path, sc->events, mism);
+        for (int k = 0; k < V - 1; k++) printf("%d,%d,%d;", c.bfs_src[k], c.bfs_dst[k], c.bfs_qty[k]);
+        printf("\n");
+        fflush(stdout);
+        return mism ? 1 : 0;
+    }
     int2* rbook = arr<int2>(keep, (size_t)m * (n + 2));
     int2* cbook = arr<int2>(keep, (size_t)n * (m + 2));
     int P = 1;

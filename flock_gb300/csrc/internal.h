@@ -34,6 +34,10 @@ struct BatchArgs {
     // partial pricing per instance: candidate rows and rounds between full
     // sweeps up to kPPSmallV vertices ([0], [1]) and above ([2], [3])
     int32_t pp[4];
+    // one-launch form: byte offset in the dynamic shared block where the
+    // instance's cost matrix is staged (0: the kernels read it from global
+    // memory)
+    int32_t cost_smem;
 };
 
 // A served request's device region: byte offsets of its arrays (256-aligned).

@@ -47,8 +47,8 @@ __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const 
         __syncthreads();
     }
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
+    ps.mark(PH_DUAL);    // the start tree and its duals
     sf_init_cta(c, bs);
-    ps.mark(PH_DUAL);
     if (!c.sc->done) tree_build_cta<kJumpPlain>(c, bs);
     for (int i = threadIdx.x; i < c.I.m; i += blockDim.x) c.row_best[i] = kNoKey;
     __syncthreads();
@@ -97,6 +97,27 @@ __device__ __forceinline__ int4 ld_stream4(const int4* p) {
 // ntile): its column tile's int32 duals staged in vt, then (row, segment)
 // units.  rows: price only the listed rows (c.sc->pp_n of them: partial
 // pricing), null for all.  The caller orders vt's previous readers.
+// Block-wide copy of ceil4(jn) int32 values from global into shared memory:
+// 16-byte loads, four per thread issued before any store (one L2 round trip
+// for a 512-thread block and an 8192-column tile of duals).  src and vt are
+// 16-byte aligned; for a dual tile (tiles start at multiples of 4 columns)
+// the rounded-up tail stays inside the dual array's allocation and is never
+// read.
+__device__ __forceinline__ void stage_i32(int32_t* vt, const int32_t* src, int jn) {
+    const int nq = (jn + 3) >> 2, bd = (int)blockDim.x;
+    const int4* s4 = reinterpret_cast<const int4*>(src);
+    int4* d4 = reinterpret_cast<int4*>(vt);
+    for (int q = threadIdx.x; q < nq; q += 4 * bd) {
+        int4 x[4];
+        #pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (q + k * bd < nq) x[k] = __ldcg(s4 + q + k * bd);
+        #pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (q + k * bd < nq) d4[q + k * bd] = x[k];
+    }
+}
+
 __device__ __forceinline__ void sweep_part(const Ctx& c, int tile, int ntile, const int32_t* rows, int32_t* vt,
                                            int bid, int nb) {
     const InstDev& I = c.I;
@@ -119,7 +140,7 @@ __device__ __forceinline__ void sweep_part(const Ctx& c, int tile, int ntile, co
         }
         return;
     }
-    for (int jj = threadIdx.x; jj < jn; jj += blockDim.x) vt[jj] = c.v32[j0 + jj];
+    stage_i32(vt, c.v32 + j0, jn);
     __syncthreads();
     const int4* v4 = reinterpret_cast<const int4*>(vt);
     for (long long u = (long long)rg * wpb + warp; u < units; u += stride) {
@@ -217,6 +238,7 @@ __device__ __forceinline__ BulkUnit bulk_unit(long long k, int rg, int nrg, int 
 
 __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int ntile) {
     __shared__ __align__(8) uint64_t full[kBulkWarps * kBulkDepth];
+    __shared__ __align__(8) uint64_t vbar;
     __shared__ PhaseLocal phl;
     extern __shared__ __align__(128) unsigned char bulk_smem[];
     PhaseScope ps(c.ph, &phl, PH_SWEEP);
@@ -244,7 +266,14 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
     uint64_t* bar = full + warp * kBulkDepth;
     if (lane == 0) {
         for (int d = 0; d < kBulkDepth; d++) mbar_init(&bar[d], 1);
+        if (warp == 0) mbar_init(&vbar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {   // the tile's int32 duals: one bulk copy (j0 is a multiple of 4 columns; the
+                              // rounded-up tail stays inside the dual array's allocation and is never read)
+        const uint32_t vbytes = (uint32_t)(((jn + 3) & ~3) * 4);
+        mbar_expect_tx(&vbar, vbytes);
+        bulk_g2s(vt, c.v32 + j0, vbytes, &vbar);
     }
     __syncwarp();
     auto issue = [&](long long j) {          // lane 0: unit j of this warp into buffer j % kBulkDepth
@@ -254,21 +283,22 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
         mbar_expect_tx(&bar[d], bytes);
         bulk_g2s(ring + (size_t)d * kBulkSeg, I.cost + (size_t)w.i * I.ldc + j0 + w.a, bytes, &bar[d]);
     };
-    if (lane == 0)            // the first units stream while the duals are staged
+    if (lane == 0)            // the first units stream while the duals land
         for (long long j = 0; j < cnt && j < kBulkDepth; j++) issue(j);
-    for (int jj = threadIdx.x; jj < jn; jj += blockDim.x) vt[jj] = c.v32[j0 + jj];
-    __syncthreads();
+    __syncthreads();          // vbar's initialisation is visible to every warp
+    // every lane waits (the copy's bytes become visible to the lanes that
+    // observe the phase); the outcome is made the same for the whole warp
+    const bool vt_ok = __all_sync(0xffffffffu, mbar_wait(&vbar, 0));
     for (long long j = 0; j < cnt; j++) {
         const int d = (int)(j % kBulkDepth);
-        // every lane waits (the copy's bytes become visible to the lanes that
-        // observe the phase); the outcome is made the same for the whole warp
-        if (!__all_sync(0xffffffffu, mbar_wait(&bar[d], (uint32_t)((j / kBulkDepth) & 1)))) {
+        if (!vt_ok || !__all_sync(0xffffffffu, mbar_wait(&bar[d], (uint32_t)((j / kBulkDepth) & 1)))) {
             if (lane == 0) {
                 fail_check(c.sc, 32);
                 // the copies still in flight land before the warp exits
                 const long long last = min(cnt, j + kBulkDepth);
-                for (long long q = j + 1; q < last; q++)
+                for (long long q = vt_ok ? j + 1 : j; q < last; q++)
                     mbar_wait(&bar[q % kBulkDepth], (uint32_t)((q / kBulkDepth) & 1));
+                if (!vt_ok) mbar_wait(&vbar, 0);
             }
             return;
         }
@@ -1043,6 +1073,28 @@ __global__ void k_fill_bench(int32_t* cost, size_t cells, int64_t* pot, int V) {
         pot[k] = (int64_t)((k * 40503u) % 700u);
 }
 
+// L2 read bandwidth: `passes` grid-stride passes over an L2-resident buffer,
+// L1 bypassed (ld.global.cg), four independent 16-byte loads in flight per
+// thread.  The xor of what was read is written only if it matches a value no
+// fill produces, so the loads cannot be dropped.
+__global__ void __launch_bounds__(512) k_l2_read(const int4* buf, size_t n4, int passes, int* sink) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    int acc = 0;
+    for (int p = 0; p < passes; p++) {
+        size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+        for (; k + 3 * stride < n4; k += 4 * stride) {
+            const int4 a = __ldcg(buf + k), b = __ldcg(buf + k + stride);
+            const int4 c = __ldcg(buf + k + 2 * stride), d = __ldcg(buf + k + 3 * stride);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w ^ b.x ^ b.y ^ b.z ^ b.w ^ c.x ^ c.y ^ c.z ^ c.w ^ d.x ^ d.y ^ d.z ^ d.w;
+        }
+        for (; k < n4; k += stride) {
+            const int4 a = __ldcg(buf + k);
+            acc ^= a.x ^ a.y ^ a.z ^ a.w;
+        }
+    }
+    if (acc == 0x7fffabcd) *sink = acc;
+}
+
 
 // ------------------------------------------------------- batched kernels ---
 // The batched form runs many instances side by side, one CTA per instance at
@@ -1124,7 +1176,7 @@ inline size_t setup_stage_bytes(int V) {
 // the working set.
 template <bool kStage>
 __device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& d, BlockScratch& bs,
-                                           unsigned char* smem) {
+                                           unsigned char* smem, PhaseScope* ps = nullptr) {
     Ctx c;
     batch_ctx(a, d, c);
     const Ctx g = c;
@@ -1154,6 +1206,7 @@ __device__ __forceinline__ void bsetup_one(const BatchArgs& a, const BatchDesc& 
         __syncthreads();
     }
     if (threadIdx.x == 0 && c.sc->events < 0) c.sc->status |= ST_VOGEL_UNDEF;
+    if (ps) ps->mark(PH_DUAL);    // the start tree and its duals
     for (int q = threadIdx.x; q < V - 1; q += blockDim.x) {
         d.bfs[3 * q + 0] = c.bfs_src[q];
         d.bfs[3 * q + 1] = c.bfs_dst[q];
@@ -1348,9 +1401,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_solve_one(BatchArgs a) {
     __shared__ PhaseLocal phl;
     extern __shared__ __align__(16) unsigned char smem[];
     PhaseScope ps(a.ph, &phl, PH_BFS);
-    const BatchDesc d = a.desc[0];
+    BatchDesc d = a.desc[0];
     if (!batch_desc_ok(a, d)) { bdesc_reject(a, d); return; }
-    bsetup_one<true>(a, d, bs, smem);
+    if (a.cost_smem > 0) {      // the whole matrix (m rows of ldc) fits beside the staging: read it from there
+        int32_t* cs = reinterpret_cast<int32_t*>(smem + a.cost_smem);
+        stage_i32(cs, d.cost, d.m * d.ldc);
+        __syncthreads();
+        d.cost = cs;
+    }
+    bsetup_one<true>(a, d, bs, smem, &ps);
     if (!d.sc->done) {
         if (a.light) brounds_one<true>(a, d, bs, smem, 1 << 30, &ps);
         else brounds_one<false>(a, d, bs, smem, 1 << 30, &ps);
@@ -1359,11 +1418,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_solve_one(BatchArgs a) {
     bfinal_one(a, d, bs);
 }
 
-// Block size of the one-launch form by instance size (FLOCK_PLAIN_THREADS=256
-// or 1024 overrides it, for tuning).
+// Block size of the one-launch form by instance size (FLOCK_PLAIN_THREADS=128,
+// 256 or 1024 overrides it, for tuning; 128 runs the 256-thread kernel).
 static int solve_one_threads(int V) {
     const char* e = getenv("FLOCK_PLAIN_THREADS");
-    if (e && (!strcmp(e, "256") || !strcmp(e, "1024"))) return atoi(e);
+    if (e && (!strcmp(e, "128") || !strcmp(e, "256") || !strcmp(e, "1024"))) return atoi(e);
     return V <= 512 ? 256 : 1024;
 }
 static const void* solve_one_fn(int threads) {
@@ -1588,7 +1647,7 @@ struct PlainSolver {
     DevBuf ws, cost, sd;
     DevBuf books;                   // "vam_device" Vogel: row and column books
     DevBuf one;                     // one-launch form: working set, basis, duals, scalars, descriptor
-    HostBuf h_desc;                 // one-launch form: the descriptor's pinned staging
+    HostBuf h_one;                  // one-launch form: pinned staging of its upload and download regions
     GridPivot* gp = nullptr;        // grid pivot round state (large instances)
     PhaseClock* ph = nullptr;       // device time per simplex phase
     ClusterPivot* cp = nullptr;     // cluster rounds' per-CTA slots
@@ -1712,37 +1771,52 @@ static void fill_flows_from_basis(int V, const int32_t* src, const int32_t* dst,
 static size_t instance_ws_bytes(int V, int m);
 
 // The plain solve of an instance below the grid-round size in ONE launch
-// (k_solve_one): costs and quantities already uploaded by prepare() (c.I);
-// the instance's working set, basis, initial list, duals, scalars and its
-// descriptor go into P.one.  Same results and statistics as the round form;
-// the phase clock splits the launch's device time.
-static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock_options& opt, const Ctx& c, int bfs,
+// (k_solve_one).  P.one holds, in this order, the upload region -- the
+// descriptor, the padded cost matrix, supplies and demands, the zeroed phase
+// clock -- and the download region -- the phase clock again, the basis, the
+// initial list, the duals and the scalars -- then the working set: one
+// host-to-device copy from pinned memory before the launch and one
+// device-to-host copy after it.  Same results and statistics as the round
+// form; the phase clock splits the launch's device time.
+static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock_options& opt, int bfs,
                             int max_rounds, flock_flow* flows, int64_t* du, int64_t* dv, flock_stats* st,
                             std::chrono::steady_clock::time_point t0) {
-    const int m = I->m, n = I->n, V = m + n, V1 = V - 1;
+    const int m = I->m, n = I->n, V = m + n, V1 = V - 1, ldc = (n + 3) & ~3;
     size_t o = 0;
-    const size_t o_ws = o;   o = al256(o + instance_ws_bytes(V, m));
+    const size_t o_desc = o; o = al256(o + sizeof(BatchDesc));
+    const size_t o_cost = o; o = al256(o + (size_t)m * ldc * 4);
+    const size_t o_sd = o;   o = al256(o + (size_t)V * 4);
+    const size_t o_ph = o;   o = al256(o + sizeof(PhaseClock));
+    const size_t up_end = o_ph + sizeof(PhaseClock);
     const size_t o_out = o;  o = al256(o + (size_t)3 * V1 * 4);
     const size_t o_bfs = o;  o = al256(o + (size_t)3 * V1 * 4);
     const size_t o_pot = o;  o = al256(o + (size_t)V * 8);
     const size_t o_sc = o;   o = al256(o + sizeof(Scalars));
-    const size_t o_desc = o; o = al256(o + sizeof(BatchDesc));
-    const size_t o_ph = o;   o = al256(o + sizeof(PhaseClock));
+    const size_t down_end = o_sc + sizeof(Scalars);
+    const size_t o_ws = o;   o = al256(o + instance_ws_bytes(V, m));
     FLOCK_CK(P.one.ensure(o));
-    FLOCK_CK(P.h_desc.ensure(sizeof(BatchDesc)));
-    BatchDesc* hd = P.h_desc.as<BatchDesc>();
-    hd->m = m; hd->n = n; hd->ldc = c.I.ldc; hd->index = 0;
-    hd->cost = c.I.cost;
-    hd->sd = c.I.supply;
+    FLOCK_CK(P.h_one.ensure(down_end));
+    uint8_t* h = P.h_one.as<uint8_t>();
+    BatchDesc* hd = P.h_one.as<BatchDesc>(o_desc);
+    hd->m = m; hd->n = n; hd->ldc = ldc; hd->index = 0;
+    hd->cost = P.one.as<int32_t>(o_cost);
+    hd->sd = P.one.as<int32_t>(o_sd);
     hd->ws = P.one.as<uint8_t>(o_ws);
     hd->out = P.one.as<int32_t>(o_out);
     hd->bfs = P.one.as<int32_t>(o_bfs);
     hd->pot = P.one.as<int64_t>(o_pot);
     hd->sc = P.one.as<Scalars>(o_sc);
     hd->done = nullptr;
+    int32_t* hc = P.h_one.as<int32_t>(o_cost);
+    for (int i = 0; i < m; i++) {
+        memcpy(hc + (size_t)i * ldc, I->cost + (size_t)i * n, (size_t)n * 4);
+        for (int j = n; j < ldc; j++) hc[(size_t)i * ldc + j] = 0;
+    }
+    memcpy(P.h_one.as<int32_t>(o_sd), I->supply, (size_t)m * 4);
+    memcpy(P.h_one.as<int32_t>(o_sd) + m, I->demand, (size_t)n * 4);
+    memset(h + o_ph, 0, sizeof(PhaseClock));
+    FLOCK_CK(cudaMemcpyAsync(P.one.p, h, up_end, cudaMemcpyHostToDevice, P.stream));
     PhaseClock* d_ph = P.one.as<PhaseClock>(o_ph);
-    FLOCK_CK(cudaMemcpyAsync(P.one.as<BatchDesc>(o_desc), hd, sizeof(BatchDesc), cudaMemcpyHostToDevice, P.stream));
-    FLOCK_CK(cudaMemsetAsync(d_ph, 0, sizeof(PhaseClock), P.stream));
     BatchArgs a;
     a.desc = P.one.as<BatchDesc>(o_desc);
     a.count = 1;
@@ -1756,27 +1830,32 @@ static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock
     a.light = stage_light(V, m) ? 1 : 0;
     a.ph = d_ph;
     block_pricing(a.pp);
-    const size_t smem = launch_smem_bytes(V, m, a.light != 0);
+    size_t smem = launch_smem_bytes(V, m, a.light != 0);
+    // the cost matrix into the same dynamic block when it fits (Vogel's
+    // rescans, the sweeps and the certificate then read shared memory)
+    a.cost_smem = 0;
+    const size_t cost_off = (smem + 15) & ~size_t(15), cost_bytes = (size_t)m * ldc * 4;
+    const char* cs_env = getenv("FLOCK_COST_SMEM");
+    if (cost_off + cost_bytes <= kStageSmemMax && !(cs_env && !strcmp(cs_env, "0"))) {
+        a.cost_smem = (int32_t)cost_off;
+        smem = cost_off + cost_bytes;
+    }
     const int threads = solve_one_threads(V);
     const void* fn = solve_one_fn(threads);
     void* kargs[] = {&a};
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     FLOCK_CK(cudaLaunchKernel(fn, dim3(1), dim3(threads), kargs, smem, P.stream));
     FLOCK_CK(cudaEventRecord(P.ev[2], P.stream));
-    std::vector<int32_t> h3((size_t)3 * V1);
-    std::vector<int64_t> pot((size_t)V);
-    FLOCK_CK(cudaMemcpyAsync(h3.data(), hd->out, (size_t)3 * V1 * 4, cudaMemcpyDeviceToHost, P.stream));
-    FLOCK_CK(cudaMemcpyAsync(pot.data(), hd->pot, (size_t)V * 8, cudaMemcpyDeviceToHost, P.stream));
-    Scalars* hs = P.h_sc.as<Scalars>();
-    FLOCK_CK(cudaMemcpyAsync(hs, hd->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, P.stream));
-    PhaseClock hph;
-    FLOCK_CK(cudaMemcpyAsync(&hph, d_ph, sizeof(PhaseClock), cudaMemcpyDeviceToHost, P.stream));
+    FLOCK_CK(cudaMemcpyAsync(h + o_ph, P.one.as<uint8_t>(o_ph), down_end - o_ph, cudaMemcpyDeviceToHost, P.stream));
     FLOCK_CK(cudaStreamSynchronize(P.stream));
     float ms_all = 0;
     cudaEventElapsedTime(&ms_all, P.ev[0], P.ev[2]);
-    const Scalars S = *hs;
+    const int32_t* h3 = P.h_one.as<int32_t>(o_out);
+    const int64_t* pot = P.h_one.as<int64_t>(o_pot);
+    const Scalars S = *P.h_one.as<Scalars>(o_sc);
+    const PhaseClock hph = *P.h_one.as<PhaseClock>(o_ph);
     const bool broken = S.status & (ST_TREE_CORRUPT | ST_SF_FAIL | ST_RANGE);
-    if (flows && !broken) fill_flows_from_basis(V, h3.data(), h3.data() + V1, h3.data() + 2 * V1, flows);
+    if (flows && !broken) fill_flows_from_basis(V, h3, h3 + V1, h3 + 2 * V1, flows);
     if (du && !broken) for (int i = 0; i < m; i++) du[i] = pot[i];
     if (dv && !broken) for (int j = 0; j < n; j++) dv[j] = pot[m + j];
     int status = S.status & kFailMask;
@@ -1818,6 +1897,12 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     std::lock_guard<std::mutex> lk(P.mu);
     if ((rc = P.setup())) return rc;
     const int m = I->m, n = I->n, V = m + n;
+    const int bfs = opt.bfs_method == FLOCK_BFS_NWC || opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE ? opt.bfs_method
+                                                                                                  : FLOCK_BFS_VOGEL;
+    // the one-launch form below the grid size (the stepping-stone mode runs
+    // its rounds on the round kernel at every size)
+    if (V < kGridPivotV && bfs != FLOCK_BFS_VOGEL_DEVICE && pivot_mode(opt) != 3)
+        return solve_one_launch(P, I, opt, bfs, max_rounds, flows, du, dv, st, t0);
     Ctx c;
     int32_t* out3 = nullptr;
     if ((rc = P.prepare(I, c, &out3))) return rc;
@@ -1827,12 +1912,6 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     FLOCK_CK(cudaMemsetAsync(P.ph, 0, sizeof(PhaseClock), P.stream));
     c.ph = P.ph;
     const int nt = threads_for(V);
-    const int bfs = opt.bfs_method == FLOCK_BFS_NWC || opt.bfs_method == FLOCK_BFS_VOGEL_DEVICE ? opt.bfs_method
-                                                                                                  : FLOCK_BFS_VOGEL;
-    // the one-launch form below the grid size (the stepping-stone mode runs
-    // its rounds on the round kernel at every size)
-    if (V < kGridPivotV && bfs != FLOCK_BFS_VOGEL_DEVICE && pivot_mode(opt) != 3)
-        return solve_one_launch(P, I, opt, c, bfs, max_rounds, flows, du, dv, st, t0);
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     int2 *rbook = nullptr, *cbook = nullptr;
     if (bfs == FLOCK_BFS_VOGEL_DEVICE && (rc = P.build_books(c, &rbook, &cbook))) return rc;
@@ -1975,8 +2054,9 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
         st->status = status;
         st->certified = (opt.verify && !broken && S.cert == 0) ? 1 : 0;
         st->vogel_events = S.events;
-        st->ms_bfs = ms_bfs;
-        st->ms_simplex = ms_loop;
+        // the setup launch's start tree counts toward the loop (phase clock)
+        st->ms_bfs = std::min((double)ms_bfs, hph.ns[PH_BFS] * 1e-6);
+        st->ms_simplex = ms_loop + (ms_bfs - st->ms_bfs);
         st->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         st->ms_dual = hph.ns[PH_DUAL] * 1e-6;
         st->ms_sweep = hph.ns[PH_SWEEP] * 1e-6;
@@ -2173,6 +2253,35 @@ static int bench_sweep(int m, int n, int iters, float* avg_ms, int* tile_out) {
     cudaEventElapsedTime(&ms, P.ev[0], P.ev[1]);
     *avg_ms = ms / iters;
     if (tile_out) *tile_out = tile;
+    return FLOCK_OK;
+}
+
+// Average device time of one k_l2_read launch over a buffer of `bytes`
+// (filled once, read `passes` times per launch), after one warm-up launch
+// that brings the buffer into L2.
+static int bench_l2(long long bytes, int passes, int iters, float* avg_ms) {
+    if (bytes < 16 || passes < 1 || iters < 1 || !avg_ms) return FLOCK_ERR_ARG;
+    PlainSolver& P = plain();
+    std::lock_guard<std::mutex> lk(P.mu);
+    int rc = P.setup();
+    if (rc) return rc;
+    const size_t n4 = (size_t)bytes / 16;
+    FLOCK_CK(P.cost.ensure(n4 * 16 + 16));
+    k_fill_bench<<<std::min(4096, (int)((n4 * 4 + 255) / 256)), 256, 0, P.stream>>>(P.cost.as<int32_t>(), n4 * 4,
+                                                                                    nullptr, 0);
+    FLOCK_CK(cudaGetLastError());
+    const int grid = 4 * num_sms();
+    int* sink = P.ws.ensure(256) == cudaSuccess ? P.ws.as<int>() : nullptr;
+    if (!sink) return FLOCK_ERR_CUDA;
+    const int4* buf = reinterpret_cast<const int4*>(P.cost.as<int32_t>());
+    k_l2_read<<<grid, 512, 0, P.stream>>>(buf, n4, passes, sink);
+    FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
+    for (int k = 0; k < iters; k++) k_l2_read<<<grid, 512, 0, P.stream>>>(buf, n4, passes, sink);
+    FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
+    FLOCK_CK(cudaEventSynchronize(P.ev[1]));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, P.ev[0], P.ev[1]);
+    *avg_ms = ms / iters;
     return FLOCK_OK;
 }
 
@@ -2461,6 +2570,7 @@ struct BatchRunner {
     BatchArgs args_for(int b) {
         BatchArgs a;
         a.ph = nullptr;
+        a.cost_smem = 0;
         block_pricing(a.pp);
         a.desc = d_desc.as<BatchDesc>() + bstart[b];
         a.count = bstart[b + 1] - bstart[b];
@@ -2816,6 +2926,7 @@ int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const f
     if (count < 1 || maxV > kMaxStagedV) return FLOCK_ERR_ARG;
     BatchArgs a;
     a.ph = nullptr;
+    a.cost_smem = 0;
     block_pricing(a.pp);
     a.desc = d_desc;
     a.count = count;
@@ -2965,8 +3076,6 @@ int flock_bench_batch_rerun(float* ms, int32_t* launches) { return flock::batch_
  * batch (after a re-solve, the re-solve's count). */
 int flock_bench_batch_cells(int64_t* cells) { return flock::batch_cells(cells); }
 
-/* Benchmark hook: average device time of the fused reduced-cost sweep on an
- * m x n matrix (random costs and duals, inputs resident). */
 // Benchmark hook: CTAs of the grid path's cluster rounds on this device (0:
 // the six-kernel rounds only).
 int flock_bench_cluster_ctas(int32_t* ctas) {
@@ -2979,8 +3088,16 @@ int flock_bench_cluster_ctas(int32_t* ctas) {
     return FLOCK_OK;
 }
 
+/* Benchmark hook: average device time of the fused reduced-cost sweep on an
+ * m x n matrix (random costs and duals, inputs resident). */
 int flock_bench_sweep(int32_t m, int32_t n, int32_t iters, float* avg_ms, int32_t* tile) {
     return flock::bench_sweep(m, n, iters, avg_ms, tile);
+}
+
+/* Benchmark hook: average device time of an L2 read-bandwidth kernel making
+ * `passes` passes over a buffer of `bytes` per launch. */
+int flock_bench_l2(int64_t bytes, int32_t passes, int32_t iters, float* avg_ms) {
+    return flock::bench_l2(bytes, passes, iters, avg_ms);
 }
 
 /* Test hook: partial pricing's candidate-row selection over host row keys

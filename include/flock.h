@@ -129,23 +129,24 @@ typedef struct {
     int32_t certified;       /* 1: certificate checked and passed */
     int32_t vogel_events;    /* Vogel steps whose line had no uncovered cell; -1 undefined */
     double ms_total;         /* wall time of the call (ms) */
-    double ms_bfs;           /* device time of the initial solution + start tree */
-    double ms_simplex;       /* device time of the pivot loop */
+    double ms_bfs;           /* device time of the initial solution (Vogel or NW corner) */
+    double ms_simplex;       /* device time of the start tree and the pivot loop */
     /* Device time per simplex phase (ms), the reference's model statistics
      * (uv_time, reduced_cost_time, pivot_time, cycle_discovery_time,
      * resolve_time, adjustment_time; uv_model_parallel.cu:301-341).  Set by
      * the plain solver (flock_solve, and the instances of more than 4096
      * vertices that the batched and served forms hand to it); 0 otherwise.
-     *   ms_dual:    rebuilds of the tree's duals, depths and intervals (at the
-     *               start and after a round that applied several pivots; a
-     *               single pivot updates the duals in place, inside ms_adjust)
+     *   ms_dual:    the strongly feasible start tree, rebuilds of the tree's
+     *               duals, depths and intervals (at the start and after a
+     *               round that applied several pivots; a single pivot
+     *               updates the duals in place, inside ms_adjust)
      *   ms_sweep:   reduced-cost sweeps and the choice of the entering cells
      *   ms_cycle:   cycle discovery (tree paths of the entering cells)
      *   ms_resolve: deconfliction of the candidates of a parallel round
      *   ms_adjust:  leaving edge, flow change and the in-place tree update
      *   ms_pivot = ms_cycle + ms_resolve + ms_adjust.
      * Launch gaps count toward the phase before them, so ms_dual + ms_sweep
-     * + ms_pivot is close to ms_simplex plus the start tree's dual rebuild. */
+     * + ms_pivot is close to ms_simplex. */
     double ms_dual, ms_sweep, ms_pivot, ms_cycle, ms_resolve, ms_adjust;
 } flock_stats;
 
