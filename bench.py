@@ -407,7 +407,8 @@ def served(fg) -> dict:
     """Served form on an open-loop Poisson stream: m, n log-uniform in
     [10, 2000], costs 1..1000, quantities 100..1000 (seeded).  Capacity is
     the batched throughput on the same pool; each offered rate is a fraction
-    of it.  Latency = submit to result (server clock)."""
+    of it.  Latency = submit to result (server clock), on a server warmed up
+    by 16 requests."""
     ms, ns = fg.generate_sizes(SEED + 4099, SERVE_POOL, 10, 2000)
     pool = [fg.generate(0, SEED * 31 + k, int(ms[k]), int(ns[k]), 1, 1000, 100, 1000) for k in range(SERVE_POOL)]
     fg.batch_solve(pool)                       # autotunes the buckets of this stream
@@ -429,6 +430,13 @@ def served(fg) -> dict:
     for frac in SERVE_RATES:
         lam = frac * cap
         srv = fg.Server(memory_budget_bytes=40 << 30, max_inflight_batches=16, max_batch=512)
+        # a long-lived server: its arena, streams and first launches are set
+        # up by a warm-up of 16 requests before the stream starts
+        warm = [srv.submit(pool[k]) for k in range(16)]
+        srv.drain()
+        got = 0
+        while got < len(warm):
+            got += len(srv.poll())
         lat, bad, size_of, by_size = [], 0, {}, {c: [] for c in classes}
 
         def take(results):

@@ -2915,10 +2915,15 @@ int serve_init() {
     return FLOCK_OK;
 }
 
-// Block size of a served launch by its largest instance (latency first:
-// larger instances get more threads).
+// Block size of a served launch by its largest instance, latency first: the
+// one-launch plain solver's sizes (FLOCK_SERVE_THREADS=64..1024, a multiple
+// of 32, overrides it, for tuning).
 static int serve_threads(int maxV) {
-    return maxV <= 128 ? 64 : maxV <= 512 ? 128 : maxV <= 1024 ? 256 : maxV <= 2944 ? 512 : 1024;
+    if (const char* e = getenv("FLOCK_SERVE_THREADS")) {
+        const int t = atoi(e);
+        if (t >= 64 && t <= 1024 && t % 32 == 0) return t;
+    }
+    return maxV <= 128 ? 128 : maxV <= 512 ? 256 : 1024;
 }
 
 int serve_launch(const BatchDesc* d_desc, int count, int maxV, int maxM, const flock_options& opt, int32_t* d_next,

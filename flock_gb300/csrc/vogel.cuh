@@ -46,150 +46,153 @@ __device__ __forceinline__ int4 top2_from_keys(uint64_t a1, uint64_t a2) {
 // crossing line of line L at crossing index x
 __device__ __forceinline__ int crossing_vertex(int L, int x, int m) { return L < m ? m + x : x; }
 
-// The writes of a Vogel step that other threads may still be reading when it
-// ends: the line it covered and its two residuals.  Thread 0 stores them
-// after the next step's barrier; until the barrier after that makes them
-// visible, every reader takes them from this copy, which every thread holds
-// in registers (all threads decide each step's allocation themselves).
-struct VogelPending {
-    int jc1 = -1, jc2 = -1;   // lines covered by the previous step and the step before it
-    int r0 = -1, r1 = -1;     // vertices whose residuals the previous step changed ...
-    int32_t q0 = 0, q1 = 0;   // ... and their new values
-    __device__ __forceinline__ bool covered(const Ctx& c, int v) const {
-        return v == jc1 || v == jc2 || c.covered[v];
-    }
-    __device__ __forceinline__ int32_t res(const Ctx& c, int v) const {
-        return v == r0 ? q0 : v == r1 ? q1 : c.res[v];
-    }
-    // thread 0, after the step's barrier: the previous step's writes
-    __device__ __forceinline__ void apply(const Ctx& c) const {
-        if (jc1 >= 0) c.covered[jc1] = 1;
-        if (r0 >= 0) c.res[r0] = q0;
-        if (r1 >= 0) c.res[r1] = q1;
-    }
-};
-
-__device__ __forceinline__ bool top2_valid(const Ctx& c, int L, int4 t, const VogelPending& pd) {
+__device__ __forceinline__ bool top2_valid(const Ctx& c, int L, int4 t) {
     const int m = c.I.m;
     if (t.z == -2) return false;                  // never built
     if (t.z < 0) return true;                     // nothing uncovered: stays so
-    if (pd.covered(c, crossing_vertex(L, t.z, m))) return false;
-    if (t.w >= 0 && pd.covered(c, crossing_vertex(L, t.w, m))) return false;
+    if (c.covered[crossing_vertex(L, t.z, m)]) return false;
+    if (t.w >= 0 && c.covered[crossing_vertex(L, t.w, m)]) return false;
     return true;
 }
 
-// This thread's share of line L's two cheapest uncovered crossing cells:
-// crossing indices first, first + step, ...
-__device__ __forceinline__ void vogel_scan_part(const Ctx& c, int L, int first, int step, const VogelPending& pd,
-                                                uint64_t& a1, uint64_t& a2) {
+// one warp rebuilds the cache of line L
+__device__ void vogel_rescan_warp(const Ctx& c, int L) {
     const InstDev& I = c.I;
-    a1 = kNoKey; a2 = kNoKey;
+    const int lane = threadIdx.x & 31;
+    uint64_t a1 = kNoKey, a2 = kNoKey;
     if (L < I.m) {
         const int32_t* row = I.cost + (size_t)L * I.ldc;
-        for (int j = first; j < I.n; j += step)
-            if (!pd.covered(c, I.m + j)) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+        for (int j = lane; j < I.n; j += 32)
+            if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
     } else {
         const int j = L - I.m;
-        for (int i = first; i < I.m; i += step)
-            if (!pd.covered(c, i)) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+        for (int i = lane; i < I.m; i += 32)
+            if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
     }
+    warp_top2(a1, a2);
+    if (lane == 0) c.top2[L] = top2_from_keys(a1, a2);
+}
+
+// the whole block rebuilds the cache of line L (block-uniform call)
+__device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs) {
+    const InstDev& I = c.I;
+    uint64_t a1 = kNoKey, a2 = kNoKey;
+    if (L < I.m) {
+        const int32_t* row = I.cost + (size_t)L * I.ldc;
+        for (int j = threadIdx.x; j < I.n; j += blockDim.x)
+            if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+    } else {
+        const int j = L - I.m;
+        for (int i = threadIdx.x; i < I.m; i += blockDim.x)
+            if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+    }
+    warp_top2(a1, a2);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) { bs.red[w] = a1; bs.red2[w] = a2; }
+    __syncthreads();
+    if (w == 0) {
+        uint64_t b1 = l < nw ? bs.red[l] : kNoKey, b2 = l < nw ? bs.red2[l] : kNoKey;
+        warp_top2(b1, b2);
+        if (l == 0) c.top2[L] = top2_from_keys(b1, b2);
+    }
+    __syncthreads();
 }
 
 // Refresh the stored penalties of lines [lo, hi) (all rows or all columns)
-// and return the largest (penalty, line) key among them, in every thread.
-// Thread t takes lines lo + t + k * blockDim, kVogelUnroll of them with their
-// loads issued together; a line whose cache lost a crossing goes to the
-// rescan list (list[], count *cnt, which is 0 on entry and again on return).
-// After the first barrier the listed lines are rebuilt: one warp per line
-// when there are at least as many lines as warps or the lines are short,
-// else the warps split them (warp w scans every g-th 32-wide slice of line
-// w mod k, g = warps / k) and every warp merges the partial top-2 pairs
-// after the second barrier (warp 0 stores them, then a third barrier makes
-// them visible).  Two barriers otherwise; the warp maxima go to slot[].
-// Thread 0 applies the previous step's pending writes after the first
-// barrier when `apply` is set.  Callers alternate two counters, so that the
-// reset of one refresh's counter (after its second barrier) cannot meet the
-// next refresh's additions.
-constexpr int kVogelUnroll = 4;
-constexpr int kVogelSplitLen = 512;   // lines of more crossings are split over warps
-__device__ uint64_t vogel_refresh(const Ctx& c, int lo, int hi, int32_t* list, int* cnt, uint64_t* slot,
-                                  BlockScratch& bs, const VogelPending& pd, bool apply) {
+// and return the largest (penalty, line) key among them.  A line whose cache
+// lost a crossing is rescanned first: one warp per line when there are at
+// least as many such lines as warps, else the warps split them (warp w scans
+// every g-th 32-wide slice of line w mod k, g = warps / k) and warp 0 merges
+// the partial top-2 pairs inside the final reduction.  That reduction also
+// settles the step's choice: `best` = the larger of the half's key and
+// `other` (the other half's largest key), and `stale` = whether the chosen
+// line's cache must be rebuilt, decided by one thread before the last
+// barrier (afterwards thread 0's allocation may change covered[]).  The
+// rescan count bs.i[ctr] must be 0 on entry and is 0 again on return (rows
+// and columns use different counters).  Three barriers.
+__device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uint64_t other, uint64_t& best,
+                                      int& stale, BlockScratch& bs) {
     const InstDev& I = c.I;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int bd = blockDim.x;
     uint64_t mx = 0;
-    for (int base = lo + threadIdx.x; base < hi; base += kVogelUnroll * bd) {
-        uint8_t cv[kVogelUnroll];
-        int4 t[kVogelUnroll];
-        int32_t d[kVogelUnroll];
-        #pragma unroll
-        for (int u = 0; u < kVogelUnroll; u++) {
-            const int v = base + u * bd;
-            if (v < hi) { cv[u] = c.covered[v]; t[u] = c.top2[v]; d[u] = c.diff[v]; }
+    for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
+        if (c.covered[v]) {
+            c.diff[v] = -1;
+            const uint64_t k = pack_i32(-1, (uint32_t)v);
+            mx = k > mx ? k : mx;
+            continue;
         }
-        #pragma unroll
-        for (int u = 0; u < kVogelUnroll; u++) {
-            const int v = base + u * bd;
-            if (v >= hi) continue;
-            if (cv[u] || v == pd.jc1 || v == pd.jc2) {
-                c.diff[v] = -1;
-                const uint64_t k = pack_i32(-1, (uint32_t)v);
-                mx = k > mx ? k : mx;
-            } else if (!top2_valid(c, v, t[u], pd)) {
-                list[atomicAdd(cnt, 1)] = v;
-            } else {
-                // a valid cache's penalty is the stored one: every cache
-                // rebuild stores its penalty with it
-                const uint64_t k = pack_i32(d[u], (uint32_t)v);
-                mx = k > mx ? k : mx;
-            }
-        }
+        const int4 t = c.top2[v];
+        if (!top2_valid(c, v, t)) { c.rescan[atomicAdd(&bs.i[ctr], 1)] = v; continue; }
+        // a valid cache's penalty is the stored one: every cache rebuild
+        // stores its penalty with it
+        const uint64_t k = pack_i32(c.diff[v], (uint32_t)v);
+        mx = k > mx ? k : mx;
     }
     __syncthreads();
-    if (apply && threadIdx.x == 0) pd.apply(c);
-    const int k = *cnt;
-    const bool split = k > 0 && k < nw && (lo == 0 ? I.n : I.m) > kVogelSplitLen;   // block-uniform
-    const int mine = split && lane < k ? list[lane] : -1;   // the split lines, kept past the second barrier
-    if (!split) {
+    const int k = bs.i[ctr];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (k >= nw) {
         for (int q = w; q < k; q += nw) {
-            const int L = list[q];
-            uint64_t a1, a2;
-            vogel_scan_part(c, L, lane, 32, pd, a1, a2);
-            warp_top2(a1, a2);
-            const int4 tt = top2_from_keys(a1, a2);
-            const int32_t pen = vogel_penalty(tt);
-            if (lane == 0) { c.top2[L] = tt; c.diff[L] = pen; }
-            const uint64_t key = pack_i32(pen, (uint32_t)L);
-            mx = key > mx ? key : mx;
+            const int L = c.rescan[q];
+            vogel_rescan_warp(c, L);
+            if (l == 0) {
+                const int32_t p = vogel_penalty(c.top2[L]);
+                c.diff[L] = p;
+                const uint64_t key = pack_i32(p, (uint32_t)L);
+                mx = key > mx ? key : mx;
+            }
         }
-    } else {
+    } else if (k > 0) {
         const int g = nw / k;
         if (w < g * k) {
-            uint64_t a1, a2;
-            vogel_scan_part(c, list[w % k], 32 * (w / k) + lane, 32 * g, pd, a1, a2);
+            const int L = c.rescan[w % k], s = w / k;
+            uint64_t a1 = kNoKey, a2 = kNoKey;
+            if (L < I.m) {
+                const int32_t* row = I.cost + (size_t)L * I.ldc;
+                for (int j = 32 * s + l; j < I.n; j += 32 * g)
+                    if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+            } else {
+                const int j = L - I.m;
+                for (int i = 32 * s + l; i < I.m; i += 32 * g)
+                    if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+            }
             warp_top2(a1, a2);
-            if (lane == 0) { bs.part1[w] = a1; bs.part2[w] = a2; }
+            if (l == 0) { bs.part1[w] = a1; bs.part2[w] = a2; }
         }
     }
     mx = warp_max_u64(mx);
-    if (lane == 0) slot[w] = mx;
+    if (l == 0) bs.red[w] = mx;        // every read of bs.red before this refresh preceded its first barrier
     __syncthreads();
-    if (threadIdx.x == 0) *cnt = 0;                    // every thread read it before the barrier above
-    uint64_t x = lane < nw ? slot[lane] : 0ull;
-    if (split) {
-        if (lane < k) {
+    if (w == 0) {
+        uint64_t x = l < nw ? bs.red[l] : 0ull;
+        if (k > 0 && k < nw && l < k) {
             const int g = nw / k;
             uint64_t a1 = kNoKey, a2 = kNoKey;
-            for (int q = 0; q < g; q++) top2_merge(a1, a2, bs.part1[lane + q * k], bs.part2[lane + q * k]);
-            const int4 tt = top2_from_keys(a1, a2);
-            const int32_t pen = vogel_penalty(tt);
-            if (w == 0) { c.top2[mine] = tt; c.diff[mine] = pen; }
-            const uint64_t key = pack_i32(pen, (uint32_t)mine);
+            for (int s = 0; s < g; s++) top2_merge(a1, a2, bs.part1[l + s * k], bs.part2[l + s * k]);
+            const int L = c.rescan[l];
+            const int4 t = top2_from_keys(a1, a2);
+            c.top2[L] = t;
+            const int32_t p = vogel_penalty(t);
+            c.diff[L] = p;
+            const uint64_t key = pack_i32(p, (uint32_t)L);
             x = key > x ? key : x;
         }
-        __syncthreads();      // the rebuilt caches are visible to every reader after the refresh
+        __syncwarp();                  // the merged caches are visible to lane 0 below
+        x = warp_max_u64(x);
+        if (l == 0) {
+            const uint64_t all = x > other ? x : other;
+            const int L = (int)key_idx(all);
+            bs.red[0] = x;
+            bs.red2[0] = all;
+            bs.i[9] = top2_valid(c, L, c.top2[L]) ? 0 : 1;
+            bs.i[ctr] = 0;                   // every thread read it before the barrier above
+        }
     }
-    return warp_max_u64(x);
+    __syncthreads();
+    best = bs.red2[0];
+    stale = bs.i[9];
+    return bs.red[0];
 }
 
 // Vogel's approximation.  Writes the V-1 allocations to c.bfs_* in allocation
@@ -199,12 +202,7 @@ __device__ uint64_t vogel_refresh(const Ctx& c, int lo, int hi, int32_t* list, i
 // A step covers exactly one line, so only that line's half (rows or
 // columns) has its penalties refreshed in the next step; the other half's
 // penalties stay as stored (the reference's staleness rule), and so does
-// its largest key.  Every thread runs the step's decisions on the same values
-// (the halves' largest keys, the chosen line's cache, the residuals), so a
-// step needs only the refresh's barriers (two, three when long lines are
-// rebuilt split over warps), plus one when the chosen line's cache must be
-// rebuilt (a line of the stale half can have lost a crossing since its last
-// refresh).
+// its largest key, kept in bs.red4[0] (rows) / bs.red4[1] (columns).
 __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n, V = m + n;
@@ -214,15 +212,15 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
     }
     // initial caches: rows one warp per row (coalesced), columns one thread
     // per column walking down the rows (coalesced across the warp)
-    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
     // (each cache is stored with its penalty: a refresh reuses the penalty
     // of every line whose cache stayed valid)
-    for (int i = w; i < m; i += nw) {
+    for (int i = threadIdx.x >> 5; i < m; i += nw) {
         const int32_t* row = I.cost + (size_t)i * I.ldc;
         uint64_t a1 = kNoKey, a2 = kNoKey;
-        for (int j = lane; j < n; j += 32) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+        for (int j = threadIdx.x & 31; j < n; j += 32) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
         warp_top2(a1, a2);
-        if (lane == 0) {
+        if ((threadIdx.x & 31) == 0) {
             const int4 t = top2_from_keys(a1, a2);
             c.top2[i] = t;
             c.diff[i] = vogel_penalty(t);
@@ -235,74 +233,64 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
         c.top2[m + j] = t;
         c.diff[m + j] = vogel_penalty(t);
     }
-    __syncthreads();
-    VogelPending pd;
-    bool pr = true, pc = true, stop = false;   // refresh rows / columns in this step
-    int cr = 0, cc = 0;                        // covered rows / columns
-    int prev = 0;                              // the reference's stale min-cost index
-    int events = 0;
-    uint64_t mrow = 0, mcol = 0;
-    unsigned nref = 0;
-    if (threadIdx.x == 0) { bs.i[0] = 0; bs.i[1] = 0; }
-    __syncthreads();
-    while (cr + cc < V - 1 && !stop) {
-        // rows list their rescans in rescan[0, m), columns in rescan[m, V)
-        if (pr) { mrow = vogel_refresh(c, 0, m, c.rescan, &bs.i[nref & 1], bs.red, bs, pd, true); nref++; }
-        if (pc) { mcol = vogel_refresh(c, m, V, c.rescan + m, &bs.i[nref & 1], bs.red, bs, pd, !pr); nref++; }
-        const uint64_t best = mrow > mcol ? mrow : mcol;
-        const int L = (int)key_idx(best);
-        int4 t = c.top2[L];
-        const bool stale = !top2_valid(c, L, t, pd);
-        if (stale) {      // block-uniform: the whole block rebuilds L's cache
-            uint64_t a1, a2;
-            vogel_scan_part(c, L, threadIdx.x, blockDim.x, pd, a1, a2);
-            warp_top2(a1, a2);
-            if (lane == 0) { bs.red3[w] = a1; bs.red4[w] = a2; }
-            __syncthreads();
-            uint64_t b1 = lane < nw ? bs.red3[lane] : kNoKey, b2 = lane < nw ? bs.red4[lane] : kNoKey;
-            warp_top2(b1, b2);
-            t = top2_from_keys(b1, b2);
-        }
-        const bool found = t.z >= 0;
-        const int cross = found ? t.z : prev;
-        if (!found) events++;
-        int row, col;
-        bool undefined;
-        if (L >= m) { col = L - m; row = cross; undefined = row < 0 || row >= m; }
-        else        { row = L; col = cross; undefined = col < 0 || col >= n; }
-        const int counter = cr + cc;
-        if (undefined) {
-            events = -1;
-            stop = true;
-            if (threadIdx.x == 0)
-                for (int k = counter; k < V - 1; k++) { c.bfs_src[k] = -1; c.bfs_dst[k] = -1; c.bfs_qty[k] = 0; }
-            break;
-        }
-        const int32_t rs = pd.res(c, row), rd = pd.res(c, m + col);
-        int32_t q, nrs, nrd;
-        int cov;
-        if (rd > rs) { q = rs; nrs = 0; nrd = rd - rs; cov = row; }
-        else         { q = rd; nrs = rs - rd; nrd = 0; cov = m + col; }
-        if (threadIdx.x == 0) {
-            c.bfs_src[counter] = row; c.bfs_dst[counter] = col; c.bfs_qty[counter] = q;
-            // a rebuilt cache keeps its penalty with it; the stored penalty
-            // only matters at the next refresh of L's half (stale until
-            // then; no thread reads L's cache before the next barrier: the
-            // next step refreshes the other half)
-            if (stale && cov != L) { c.top2[L] = t; c.diff[L] = vogel_penalty(t); }
-        }
-        pr = cov < m;
-        pc = !pr;
-        if (pr) cr++; else cc++;
-        if (found) prev = cross;
-        pd.jc2 = pd.jc1; pd.jc1 = cov;
-        pd.r0 = row; pd.q0 = nrs; pd.r1 = m + col; pd.q1 = nrd;
-    }
-    __syncthreads();      // every read of this step's state is done
     if (threadIdx.x == 0) {
-        pd.apply(c);
-        c.sc->events = events;
+        bs.i[0] = 1; bs.i[1] = 1;   // refresh rows / columns in the next step
+        bs.i[2] = 0; bs.i[3] = 0;   // covered rows / columns (counters)
+        bs.i[4] = 0;                // stale min-cost index
+        bs.i[5] = 0;                // events
+        bs.i[6] = 0; bs.i[8] = 0;   // rescan list lengths (rows, columns)
+        bs.red4[0] = 0; bs.red4[1] = 0;
+        bs.i[7] = 0;                // stop
     }
+    __syncthreads();
+    for (int step = 0; step < V - 1; step++) {
+        const int cr = bs.i[2], cc = bs.i[3];
+        if (cr + cc >= V - 1 || bs.i[7]) break;
+        const int pr = bs.i[0], pc = bs.i[1];
+        uint64_t mrow = bs.red4[0], mcol = bs.red4[1], best = 0;
+        int stale = 0;
+        if (pr) mrow = vogel_refresh_max(c, 0, m, 6, pc ? 0ull : mcol, best, stale, bs);
+        if (pc) mcol = vogel_refresh_max(c, m, V, 8, mrow, best, stale, bs);
+        const int L = (int)key_idx(best);
+        if (stale) vogel_rescan_block(c, L, bs);
+        if (threadIdx.x == 0) {
+            bs.red4[0] = mrow;
+            bs.red4[1] = mcol;
+            bs.i[0] = 0;
+            bs.i[1] = 0;
+            const int4 t = c.top2[L];
+            // a rebuilt cache keeps its penalty with it; the stored penalty
+            // only matters at the next refresh of L's half (stale until then)
+            if (stale) c.diff[L] = vogel_penalty(t);
+            const bool found = t.z >= 0;
+            const int cross = found ? t.z : bs.i[4];
+            if (!found) bs.i[5]++;
+            int row, col;
+            bool undefined;
+            if (L >= m) { col = L - m; row = cross; undefined = row < 0 || row >= m; }
+            else        { row = L; col = cross; undefined = col < 0 || col >= n; }
+            const int counter = cr + cc;
+            if (undefined) {
+                bs.i[5] = -1;
+                bs.i[7] = 1;
+                for (int k = counter; k < V - 1; k++) { c.bfs_src[k] = -1; c.bfs_dst[k] = -1; c.bfs_qty[k] = 0; }
+            } else {
+                const int32_t rs = c.res[row], rd = c.res[m + col];
+                int32_t q;
+                if (rd > rs) {
+                    q = rs; c.res[m + col] = rd - rs; c.res[row] = 0; c.covered[row] = 1;
+                    bs.i[0] = 1; bs.i[2] = cr + 1;
+                } else {
+                    q = rd; c.res[row] = rs - rd; c.res[m + col] = 0; c.covered[m + col] = 1;
+                    bs.i[1] = 1; bs.i[3] = cc + 1;
+                }
+                c.bfs_src[counter] = row; c.bfs_dst[counter] = col; c.bfs_qty[counter] = q;
+                if (found) bs.i[4] = cross;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c.sc->events = bs.i[5];
     __syncthreads();
 }
 

@@ -86,18 +86,17 @@ def _emu_vogel_files(tmp_path, seed, count, shapes):
 
 @pytest.mark.parametrize("threads,seed", [(32, 1), (96, 3), (256, 4)])
 def test_emulated_vogel_host(emu, tmp_path, threads, seed):
-    """The "vam_host" Vogel (vogel_cta: every thread takes each step's
-    decisions, one barrier per step, the covered line and residuals of a
-    step stored one step late) on the emulated CTA, where warp 0 runs ahead
-    of the others between barriers: allocations and the event count
-    identical to the oracle's restatement of the reference's sequential
-    Vogel, on tie-heavy, zero-quantity and wide instances; no barrier
-    divergence, no sanitizer report."""
+    """The "vam_host" Vogel (vogel_cta: cached top-2 crossings per line,
+    rescans spread over the warps, long lines split) on the emulated CTA,
+    where each warp runs ahead of the others up to its next barrier:
+    allocations and the event count identical to the oracle's restatement of
+    the reference's sequential Vogel, on tie-heavy, zero-quantity and wide
+    instances; no barrier divergence, no sanitizer report."""
     import numpy as np
     import oracle
 
     def shapes(rng, k):
-        # lines longer than 512 crossings are rebuilt split over warps
+        # few long lines: rescans split over warps
         if k % 8 == 7:
             return int(rng.integers(520, 640)), int(rng.integers(2, 8))
         if k % 8 == 6:
