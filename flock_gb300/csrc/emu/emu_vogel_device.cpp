@@ -1,6 +1,7 @@
 // emu_vogel_device.cpp -- runs the device functions of the "vam_device" Vogel
 // variant (book_line_cta for every line, then vogel_books_cta) or, with
-// EMU_VOGEL=host, the "vam_host" Vogel (vogel_cta) on an emulated CTA
+// EMU_VOGEL=host / wide, the "vam_host" Vogel (vogel_cta, its staged form /
+// its wide-instance form with a column-major copy) on an emulated CTA
 // (cuda_emu.h) under AddressSanitizer / UBSan, for the binary instance files
 // given as arguments, and prints each allocation list:
 //   <file> events=<e> barrier_mismatch=<k> flows=<src>,<dst>,<qty>;...
@@ -44,12 +45,21 @@ static int run_one(const char* path) {
     c.res = arr<int32_t>(keep, V);
     c.top2 = arr<int4>(keep, V);
     const char* variant = getenv("EMU_VOGEL");
-    if (variant && !strcmp(variant, "host")) {
+    if (variant && (!strcmp(variant, "host") || !strcmp(variant, "wide"))) {
         c.covered = arr<uint8_t>(keep, V);
         c.diff = arr<int32_t>(keep, V);
         c.rescan = arr<int32_t>(keep, V);
         BlockScratch bs;
-        const int r = emu::run_cta([&] { vogel_cta(c, bs); });
+        const bool wide = !strcmp(variant, "wide");
+        // the wide form's column-major copy (n rows of ceil4(m))
+        const int ldcT = (m + 3) & ~3;
+        int32_t* T = arr<int32_t>(keep, (size_t)n * ldcT);
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < ldcT; i++) T[(size_t)j * ldcT + i] = i < m ? C[(size_t)i * ldc + j] : 0;
+        const int r = emu::run_cta([&] {
+            if (wide) vogel_cta<true>(c, bs, T);
+            else vogel_cta(c, bs);
+        });
         const int mism = r ? (r < 0 ? 1000 : r) : 0;
         printf("%s events=%d barrier_mismatch=%d flows=", path, sc->events, mism);
         for (int k = 0; k < V - 1; k++) printf("%d,%d,%d;", c.bfs_src[k], c.bfs_dst[k], c.bfs_qty[k]);

@@ -34,12 +34,51 @@
 namespace flock {
 
 // ------------------------------------------------------------ kernels ------
-__global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const int2* rbook, const int2* cbook) {
+// Vogel's per-line state (diff, res, rescan list, covered: V * 13 bytes) in
+// the launch's dynamic shared memory when the host gives it room: every
+// refresh reads it several times per line.  The top-2 caches stay in the
+// working set.
+constexpr size_t kVogelStageMax = 200 * 1024;
+__host__ __device__ inline size_t vogel_stage_bytes(int V) {
+    return 3 * (((size_t)V * 4 + 15) & ~size_t(15)) + (((size_t)V + 15) & ~size_t(15));
+}
+__device__ __forceinline__ void vogel_stage(Ctx& c, unsigned char* smem, int V) {
+    const size_t w = ((size_t)V * 4 + 15) & ~size_t(15);
+    c.diff = reinterpret_cast<int32_t*>(smem);
+    c.res = reinterpret_cast<int32_t*>(smem + w);
+    c.rescan = reinterpret_cast<int32_t*>(smem + 2 * w);
+    c.covered = reinterpret_cast<uint8_t*>(smem + 3 * w);
+}
+
+// Column-major copy of the cost matrix for Vogel's column scans:
+// costT[j * ldcT + i] = cost[i * ldc + j], through a 32 x 33 shared tile.
+__global__ void __launch_bounds__(256) k_transpose(const int32_t* cost, int m, int n, int ldc, int32_t* costT,
+                                                   int ldcT) {
+    __shared__ int32_t tile[32][33];
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int i = i0 + k, j = j0 + threadIdx.x;
+        if (i < m && j < n) tile[k][threadIdx.x] = cost[(size_t)i * ldc + j];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int j = j0 + k, i = i0 + threadIdx.x;
+        if (j < n && i < m) costT[(size_t)j * ldcT + i] = tile[threadIdx.x][k];
+    }
+}
+
+// costT: the column-major copy (null: columns are read from the rows);
+// stage: the dynamic block holds vogel_stage_bytes(V).
+__global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const int2* rbook, const int2* cbook,
+                                                   const int32_t* costT, int stage) {
     __shared__ BlockScratch bs;
     __shared__ PhaseLocal phl;
+    extern __shared__ __align__(16) unsigned char su_smem[];
     PhaseScope ps(c.ph, &phl, PH_BFS);
     if (bfs_method == FLOCK_BFS_VOGEL) {
-        vogel_cta(c, bs);
+        Ctx cv = c;
+        if (stage) vogel_stage(cv, su_smem, c.I.m + c.I.n);
+        vogel_cta<true>(cv, bs, costT);
     } else if (bfs_method == FLOCK_BFS_VOGEL_DEVICE) {
         vogel_books_cta(c, rbook, cbook, bs);
     } else {
@@ -55,9 +94,12 @@ __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const 
     ps.mark(PH_SWEEP);   // the first round's sweep
 }
 
-__global__ void __launch_bounds__(1024, 1) k_vogel_only(Ctx c) {
+__global__ void __launch_bounds__(1024, 1) k_vogel_only(Ctx c, const int32_t* costT, int stage) {
     __shared__ BlockScratch bs;
-    vogel_cta(c, bs);
+    extern __shared__ __align__(16) unsigned char vo_smem[];
+    Ctx cv = c;
+    if (stage) vogel_stage(cv, vo_smem, c.I.m + c.I.n);
+    vogel_cta<true>(cv, bs, costT);
 }
 
 // "vam_device" Vogel: the books (one block per line: rows, then columns),
@@ -811,13 +853,26 @@ __device__ void cluster_cand_sweep(const Ctx& c, int pn, bool narrow, int rank, 
             const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
             int32_t bv = INT32_MAX, bj = INT32_MAX, bdual = 0;
             const int qa = a >> 2, qb = b >> 2;
-            for (int q = qa + lane; q < qb; q += 32) {
-                const int4 cv = row[q], vv = v4[q];
+            auto take = [&](const int4 cv, const int4 vv, int q) {
                 int32_t t;
                 t = cv.x - vv.x; if (t < bv) { bv = t; bj = 4 * q; bdual = vv.x; }
                 t = cv.y - vv.y; if (t < bv) { bv = t; bj = 4 * q + 1; bdual = vv.y; }
                 t = cv.z - vv.z; if (t < bv) { bv = t; bj = 4 * q + 2; bdual = vv.z; }
                 t = cv.w - vv.w; if (t < bv) { bv = t; bj = 4 * q + 3; bdual = vv.w; }
+            };
+            if (qb - qa == kSegCols / 4) {
+                // a full segment: the lane's 8 cost vectors in flight at once
+                // (one L2 round trip); the duals are read as they are used
+                int4 cv[kSegCols / 128];
+                #pragma unroll
+                for (int k = 0; k < kSegCols / 128; k++) cv[k] = ld_stream4(row + qa + lane + 32 * k);
+                #pragma unroll
+                for (int k = 0; k < kSegCols / 128; k++) {
+                    const int q = qa + lane + 32 * k;
+                    take(cv[k], v4[q], q);
+                }
+            } else {
+                for (int q = qa + lane; q < qb; q += 32) take(row[q], v4[q], q);
             }
             if (lane < b - 4 * qb) {
                 const int j = 4 * qb + lane;
@@ -1646,6 +1701,7 @@ struct PlainSolver {
     std::mutex mu;
     DevBuf ws, cost, sd;
     DevBuf books;                   // "vam_device" Vogel: row and column books
+    DevBuf costT;                   // Vogel's column-major copy of the costs
     DevBuf one;                     // one-launch form: working set, basis, duals, scalars, descriptor
     HostBuf h_one;                  // one-launch form: pinned staging of its upload and download regions
     GridPivot* gp = nullptr;        // grid pivot round state (large instances)
@@ -1668,6 +1724,9 @@ struct PlainSolver {
             FLOCK_CK(cudaFuncSetAttribute(solve_one_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)kStageSmemMax));
         FLOCK_CK(cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBulkSmem));
+        FLOCK_CK(cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVogelStageMax));
+        FLOCK_CK(cudaFuncSetAttribute(k_vogel_only, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kVogelStageMax));
         // the largest cluster the cluster rounds can be launched with (one cluster)
         cluster_ctas = 0;
         if (cudaFuncSetAttribute(k_cround, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
@@ -1738,6 +1797,19 @@ struct PlainSolver {
         FLOCK_CK(cudaMemcpyAsync(sd.as<int32_t>() + m, I->demand, (size_t)n * 4, cudaMemcpyHostToDevice, stream));
         return FLOCK_OK;
     }
+
+    // The column-major copy of the uploaded costs for Vogel's column scans
+    // (null when it cannot be allocated: the scans then read the rows).
+    const int32_t* transposed(const Ctx& c) {
+        const int m = c.I.m, n = c.I.n, ldcT = (m + 3) & ~3;
+        if (costT.ensure((size_t)n * ldcT * 4 + 16) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        k_transpose<<<dim3((n + 31) / 32, (m + 31) / 32), dim3(32, 8), 0, stream>>>(c.I.cost, m, n, c.I.ldc,
+                                                                                   costT.as<int32_t>(), ldcT);
+        return cudaGetLastError() == cudaSuccess ? costT.as<int32_t>() : nullptr;
+    }
+    // Dynamic shared memory of the Vogel launches (0: the line state stays
+    // in the working set).
+    static size_t vogel_smem(int V) { return vogel_stage_bytes(V) <= kVogelStageMax ? vogel_stage_bytes(V) : 0; }
 
     int reset_scalars(Scalars* dsc, int mode, int max_rounds, bool partial = false) {
         Scalars z;
@@ -1915,7 +1987,9 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     FLOCK_CK(cudaEventRecord(P.ev[0], P.stream));
     int2 *rbook = nullptr, *cbook = nullptr;
     if (bfs == FLOCK_BFS_VOGEL_DEVICE && (rc = P.build_books(c, &rbook, &cbook))) return rc;
-    k_setup<<<1, nt, 0, P.stream>>>(c, bfs, rbook, cbook);
+    const int32_t* costT = bfs == FLOCK_BFS_VOGEL ? P.transposed(c) : nullptr;
+    const size_t vsm = bfs == FLOCK_BFS_VOGEL ? PlainSolver::vogel_smem(V) : 0;
+    k_setup<<<1, nt, vsm, P.stream>>>(c, bfs, rbook, cbook, costT, vsm ? 1 : 0);
     FLOCK_CK(cudaGetLastError());
     FLOCK_CK(cudaEventRecord(P.ev[1], P.stream));
     int grid = 0, tile = 0, ntile = 0, bgrid = 0, btile = 0, bntile = 0;
@@ -2095,7 +2169,8 @@ static int vogel_plain(const flock_instance* I, flock_flow* flows, int32_t* even
         if ((rc = P.build_books(c, &rbook, &cbook))) return rc;
         k_vogel_books_only<<<1, threads_for(V), 0, P.stream>>>(c, rbook, cbook);
     } else {
-        k_vogel_only<<<1, threads_for(V), 0, P.stream>>>(c);
+        const size_t vsm = PlainSolver::vogel_smem(V);
+        k_vogel_only<<<1, threads_for(V), vsm, P.stream>>>(c, P.transposed(c), vsm ? 1 : 0);
     }
     FLOCK_CK(cudaGetLastError());
     std::vector<int32_t> a((size_t)V), b((size_t)V), q((size_t)V);

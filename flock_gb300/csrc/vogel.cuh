@@ -55,37 +55,76 @@ __device__ __forceinline__ bool top2_valid(const Ctx& c, int L, int4 t) {
     return true;
 }
 
-// one warp rebuilds the cache of line L
-__device__ void vogel_rescan_warp(const Ctx& c, int L) {
+// This thread's share (crossing indices first, first + step, ...) of line
+// L's two cheapest uncovered crossing cells.  kWide (instances whose line
+// state is in global memory): four crossings' loads issued together, and a
+// column read from the column-major copy costT (n rows of ceil4(m)) when
+// there is one, instead of one row per element.
+template <bool kWide>
+__device__ __forceinline__ void vogel_scan(const Ctx& c, int L, int first, int step, const int32_t* costT,
+                                           uint64_t& a1, uint64_t& a2) {
     const InstDev& I = c.I;
-    const int lane = threadIdx.x & 31;
-    uint64_t a1 = kNoKey, a2 = kNoKey;
-    if (L < I.m) {
-        const int32_t* row = I.cost + (size_t)L * I.ldc;
-        for (int j = lane; j < I.n; j += 32)
-            if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
+    a1 = kNoKey; a2 = kNoKey;
+    const int32_t* line = nullptr;
+    const uint8_t* cov = nullptr;
+    int len = 0;
+    if (L < I.m) { line = I.cost + (size_t)L * I.ldc; cov = c.covered + I.m; len = I.n; }
+    else if (kWide && costT) { line = costT + (size_t)(L - I.m) * ((I.m + 3) & ~3); cov = c.covered; len = I.m; }
+    if (line) {
+        if (kWide) {
+            int x = first;
+            for (; x + 3 * step < len; x += 4 * step) {
+                int32_t cv[4];
+                uint8_t cc[4];
+                #pragma unroll
+                for (int u = 0; u < 4; u++) { cv[u] = line[x + u * step]; cc[u] = cov[x + u * step]; }
+                #pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (!cc[u]) top2_insert(a1, a2, pack_i32(cv[u], (uint32_t)(x + u * step)));
+            }
+            for (; x < len; x += step)
+                if (!cov[x]) top2_insert(a1, a2, pack_i32(line[x], (uint32_t)x));
+        } else {
+            for (int x = first; x < len; x += step)
+                if (!cov[x]) top2_insert(a1, a2, pack_i32(line[x], (uint32_t)x));
+        }
     } else {
         const int j = L - I.m;
-        for (int i = lane; i < I.m; i += 32)
-            if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+        if (kWide) {
+            int i = first;
+            for (; i + 3 * step < I.m; i += 4 * step) {
+                int32_t cv[4];
+                uint8_t cc[4];
+                #pragma unroll
+                for (int u = 0; u < 4; u++) { cv[u] = cost_of(I, i + u * step, j); cc[u] = c.covered[i + u * step]; }
+                #pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (!cc[u]) top2_insert(a1, a2, pack_i32(cv[u], (uint32_t)(i + u * step)));
+            }
+            for (; i < I.m; i += step)
+                if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+        } else {
+            for (int i = first; i < I.m; i += step)
+                if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
+        }
     }
+}
+
+// one warp rebuilds the cache of line L
+template <bool kWide>
+__device__ void vogel_rescan_warp(const Ctx& c, int L, const int32_t* costT) {
+    const int lane = threadIdx.x & 31;
+    uint64_t a1, a2;
+    vogel_scan<kWide>(c, L, lane, 32, costT, a1, a2);
     warp_top2(a1, a2);
     if (lane == 0) c.top2[L] = top2_from_keys(a1, a2);
 }
 
 // the whole block rebuilds the cache of line L (block-uniform call)
-__device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs) {
-    const InstDev& I = c.I;
-    uint64_t a1 = kNoKey, a2 = kNoKey;
-    if (L < I.m) {
-        const int32_t* row = I.cost + (size_t)L * I.ldc;
-        for (int j = threadIdx.x; j < I.n; j += blockDim.x)
-            if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
-    } else {
-        const int j = L - I.m;
-        for (int i = threadIdx.x; i < I.m; i += blockDim.x)
-            if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
-    }
+template <bool kWide>
+__device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs, const int32_t* costT) {
+    uint64_t a1, a2;
+    vogel_scan<kWide>(c, L, threadIdx.x, blockDim.x, costT, a1, a2);
     warp_top2(a1, a2);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
     __syncthreads();
@@ -111,23 +150,52 @@ __device__ void vogel_rescan_block(const Ctx& c, int L, BlockScratch& bs) {
 // barrier (afterwards thread 0's allocation may change covered[]).  The
 // rescan count bs.i[ctr] must be 0 on entry and is 0 again on return (rows
 // and columns use different counters).  Three barriers.
+template <bool kWide>
 __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uint64_t other, uint64_t& best,
-                                      int& stale, BlockScratch& bs) {
-    const InstDev& I = c.I;
+                                      int& stale, BlockScratch& bs, const int32_t* costT) {
     uint64_t mx = 0;
-    for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
-        if (c.covered[v]) {
-            c.diff[v] = -1;
-            const uint64_t k = pack_i32(-1, (uint32_t)v);
-            mx = k > mx ? k : mx;
-            continue;
+    if (kWide) {    // four lines' loads issued together (their latency is a global-memory round trip)
+        const int bd = blockDim.x;
+        for (int base = lo + threadIdx.x; base < hi; base += 4 * bd) {
+            uint8_t cv[4];
+            int4 t[4];
+            int32_t d[4];
+            #pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int v = base + u * bd;
+                if (v < hi) { cv[u] = c.covered[v]; t[u] = c.top2[v]; d[u] = c.diff[v]; }
+            }
+            #pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int v = base + u * bd;
+                if (v >= hi) continue;
+                if (cv[u]) {
+                    c.diff[v] = -1;
+                    const uint64_t k = pack_i32(-1, (uint32_t)v);
+                    mx = k > mx ? k : mx;
+                } else if (!top2_valid(c, v, t[u])) {
+                    c.rescan[atomicAdd(&bs.i[ctr], 1)] = v;
+                } else {
+                    const uint64_t k = pack_i32(d[u], (uint32_t)v);
+                    mx = k > mx ? k : mx;
+                }
+            }
         }
-        const int4 t = c.top2[v];
-        if (!top2_valid(c, v, t)) { c.rescan[atomicAdd(&bs.i[ctr], 1)] = v; continue; }
-        // a valid cache's penalty is the stored one: every cache rebuild
-        // stores its penalty with it
-        const uint64_t k = pack_i32(c.diff[v], (uint32_t)v);
-        mx = k > mx ? k : mx;
+    } else {
+        for (int v = lo + threadIdx.x; v < hi; v += blockDim.x) {
+            if (c.covered[v]) {
+                c.diff[v] = -1;
+                const uint64_t k = pack_i32(-1, (uint32_t)v);
+                mx = k > mx ? k : mx;
+                continue;
+            }
+            const int4 t = c.top2[v];
+            if (!top2_valid(c, v, t)) { c.rescan[atomicAdd(&bs.i[ctr], 1)] = v; continue; }
+            // a valid cache's penalty is the stored one: every cache rebuild
+            // stores its penalty with it
+            const uint64_t k = pack_i32(c.diff[v], (uint32_t)v);
+            mx = k > mx ? k : mx;
+        }
     }
     __syncthreads();
     const int k = bs.i[ctr];
@@ -135,7 +203,7 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
     if (k >= nw) {
         for (int q = w; q < k; q += nw) {
             const int L = c.rescan[q];
-            vogel_rescan_warp(c, L);
+            vogel_rescan_warp<kWide>(c, L, costT);
             if (l == 0) {
                 const int32_t p = vogel_penalty(c.top2[L]);
                 c.diff[L] = p;
@@ -147,16 +215,8 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
         const int g = nw / k;
         if (w < g * k) {
             const int L = c.rescan[w % k], s = w / k;
-            uint64_t a1 = kNoKey, a2 = kNoKey;
-            if (L < I.m) {
-                const int32_t* row = I.cost + (size_t)L * I.ldc;
-                for (int j = 32 * s + l; j < I.n; j += 32 * g)
-                    if (!c.covered[I.m + j]) top2_insert(a1, a2, pack_i32(row[j], (uint32_t)j));
-            } else {
-                const int j = L - I.m;
-                for (int i = 32 * s + l; i < I.m; i += 32 * g)
-                    if (!c.covered[i]) top2_insert(a1, a2, pack_i32(cost_of(I, i, j), (uint32_t)i));
-            }
+            uint64_t a1, a2;
+            vogel_scan<kWide>(c, L, 32 * s + l, 32 * g, costT, a1, a2);
             warp_top2(a1, a2);
             if (l == 0) { bs.part1[w] = a1; bs.part2[w] = a2; }
         }
@@ -203,7 +263,12 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
 // columns) has its penalties refreshed in the next step; the other half's
 // penalties stay as stored (the reference's staleness rule), and so does
 // its largest key, kept in bs.red4[0] (rows) / bs.red4[1] (columns).
-__device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
+// kWide: the form for instances whose line state is in global memory (the
+// plain solver's setup, flock_vogel): loads batched, columns read from costT
+// when given.  The staged forms (line state in shared memory) keep the
+// leaner loops and their registers.
+template <bool kWide = false>
+__device__ void vogel_cta(const Ctx& c, BlockScratch& bs, const int32_t* costT = nullptr) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n, V = m + n;
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
@@ -249,10 +314,10 @@ __device__ void vogel_cta(const Ctx& c, BlockScratch& bs) {
         const int pr = bs.i[0], pc = bs.i[1];
         uint64_t mrow = bs.red4[0], mcol = bs.red4[1], best = 0;
         int stale = 0;
-        if (pr) mrow = vogel_refresh_max(c, 0, m, 6, pc ? 0ull : mcol, best, stale, bs);
-        if (pc) mcol = vogel_refresh_max(c, m, V, 8, mrow, best, stale, bs);
+        if (pr) mrow = vogel_refresh_max<kWide>(c, 0, m, 6, pc ? 0ull : mcol, best, stale, bs, costT);
+        if (pc) mcol = vogel_refresh_max<kWide>(c, m, V, 8, mrow, best, stale, bs, costT);
         const int L = (int)key_idx(best);
-        if (stale) vogel_rescan_block(c, L, bs);
+        if (stale) vogel_rescan_block<kWide>(c, L, bs, costT);
         if (threadIdx.x == 0) {
             bs.red4[0] = mrow;
             bs.red4[1] = mcol;

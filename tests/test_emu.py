@@ -84,10 +84,13 @@ def _emu_vogel_files(tmp_path, seed, count, shapes):
     return files, insts
 
 
-@pytest.mark.parametrize("threads,seed", [(32, 1), (96, 3), (256, 4)])
-def test_emulated_vogel_host(emu, tmp_path, threads, seed):
+@pytest.mark.parametrize("threads,seed,variant", [(32, 1, "host"), (96, 3, "host"), (256, 4, "host"),
+                                                  (96, 5, "wide"), (256, 6, "wide")])
+def test_emulated_vogel_host(emu, tmp_path, threads, seed, variant):
     """The "vam_host" Vogel (vogel_cta: cached top-2 crossings per line,
-    rescans spread over the warps, long lines split) on the emulated CTA,
+    rescans spread over the warps, long lines split; the staged form and the
+    wide-instance form with batched loads and a column-major copy) on the
+    emulated CTA,
     where each warp runs ahead of the others up to its next barrier:
     allocations and the event count identical to the oracle's restatement of
     the reference's sequential Vogel, on tie-heavy, zero-quantity and wide
@@ -110,7 +113,7 @@ def test_emulated_vogel_host(emu, tmp_path, threads, seed):
     files, insts = _emu_vogel_files(tmp_path, seed, 25, shapes)
     exe = os.path.join(EMU_DIR, "emu_vogel_device")
     r = subprocess.run([exe] + files, capture_output=True, text=True,
-                       env=dict(os.environ, EMU_THREADS=str(threads), EMU_VOGEL="host"), timeout=600)
+                       env=dict(os.environ, EMU_THREADS=str(threads), EMU_VOGEL=variant), timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert not re.search(r"ERROR: AddressSanitizer|runtime error:", r.stderr), r.stderr[-2000:]
     lines = r.stdout.splitlines()
