@@ -191,6 +191,11 @@ struct InstDev {
     const int32_t* cost;      // m x ldc, row-major
     const int32_t* supply;    // m
     const int32_t* demand;    // n
+    // the grid path's 16-bit copy of the costs when every cost fits (m x
+    // ldc16, ldc16 a multiple of 8), read by its full and candidate sweeps;
+    // null otherwise
+    const int16_t* cost16 = nullptr;
+    int32_t ldc16 = 0;
 };
 
 // Per-instance working set.  Pointers may refer to shared or global memory.

@@ -67,6 +67,17 @@ __global__ void __launch_bounds__(256) k_transpose(const int32_t* cost, int m, i
     }
 }
 
+// 16-bit copy of the costs (every cost fits): cost16[i * ldc16 + j], the
+// padding columns zero.
+__global__ void __launch_bounds__(256) k_cost16(const int32_t* cost, int m, int n, int ldc, int16_t* cost16,
+                                                int ldc16) {
+    const size_t cells = (size_t)m * ldc16;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < cells; k += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = k / ldc16, j = k % ldc16;
+        cost16[k] = j < (size_t)n ? (int16_t)cost[i * ldc + j] : (int16_t)0;
+    }
+}
+
 // costT: the column-major copy (null: columns are read from the rows);
 // stage: the dynamic block holds vogel_stage_bytes(V).
 __global__ void __launch_bounds__(1024, 1) k_setup(Ctx c, int bfs_method, const int2* rbook, const int2* cbook,
@@ -269,12 +280,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 struct BulkUnit {
     int i, a, b;
 };
-__device__ __forceinline__ BulkUnit bulk_unit(long long k, int rg, int nrg, int nseg, int jn) {
+__device__ __forceinline__ BulkUnit bulk_unit(long long k, int rg, int nrg, int nseg, int jn, int segc) {
     const long long u = rg + k * nrg;
     BulkUnit w;
     w.i = (int)(u / nseg);
-    w.a = (int)(u % nseg) * kBulkSeg;
-    w.b = min(jn, w.a + kBulkSeg);
+    w.a = (int)(u % nseg) * segc;
+    w.b = min(jn, w.a + segc);
     return w;
 }
 
@@ -289,7 +300,11 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
     const int m = I.m, n = I.n;
     const int t = (int)blockIdx.x % ntile, rg = (int)blockIdx.x / ntile, nrg = (int)gridDim.x / ntile;
     const int j0 = t * tile, jn = min(tile, n - j0);
-    const int nseg = (jn + kBulkSeg - 1) / kBulkSeg;
+    // 16-bit costs (the copy exists only with narrow duals in mind): units
+    // of 2 kBulkSeg columns, the same 4 KB per copy
+    const bool h16 = I.cost16 != nullptr && c.sc->narrow;
+    const int segc = h16 ? 2 * kBulkSeg : kBulkSeg;
+    const int nseg = (jn + segc - 1) / segc;
     const long long units = (long long)m * nseg;
     const long long mine = units > rg ? (units - rg + nrg - 1) / nrg : 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -297,7 +312,7 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
     const long long cnt = mine > warp ? (mine - warp + kBulkWarps - 1) / kBulkWarps : 0;
     if (!c.sc->narrow) {      // wide duals: exact int64 keys per element
         for (long long j = 0; j < cnt; j++) {
-            const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn);
+            const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn, segc);
             const uint64_t key = row_best_exact(I.cost + (size_t)w.i * I.ldc, c.pot[w.i], c.pot + m, j0 + w.a, j0 + w.b);
             if (lane == 0) atomicMin((unsigned long long*)&c.row_best[w.i], (unsigned long long)key);
         }
@@ -320,10 +335,13 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
     __syncwarp();
     auto issue = [&](long long j) {          // lane 0: unit j of this warp into buffer j % kBulkDepth
         const int d = (int)(j % kBulkDepth);
-        const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn);
-        const uint32_t bytes = (uint32_t)(((w.b - w.a + 3) & ~3) * 4);   // within the row pitch (ldc = ceil4(n))
+        const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn, segc);
+        // within the row pitch (ldc = ceil4(n), ldc16 = ceil8(n))
+        const uint32_t bytes = h16 ? (uint32_t)(((w.b - w.a + 7) & ~7) * 2) : (uint32_t)(((w.b - w.a + 3) & ~3) * 4);
+        const void* src = h16 ? (const void*)(I.cost16 + (size_t)w.i * I.ldc16 + j0 + w.a)
+                              : (const void*)(I.cost + (size_t)w.i * I.ldc + j0 + w.a);
         mbar_expect_tx(&bar[d], bytes);
-        bulk_g2s(ring + (size_t)d * kBulkSeg, I.cost + (size_t)w.i * I.ldc + j0 + w.a, bytes, &bar[d]);
+        bulk_g2s(ring + (size_t)d * kBulkSeg, src, bytes, &bar[d]);
     };
     if (lane == 0)            // the first units stream while the duals land
         for (long long j = 0; j < cnt && j < kBulkDepth; j++) issue(j);
@@ -344,20 +362,31 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
             }
             return;
         }
-        const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn);
+        const BulkUnit w = bulk_unit(warp + j * kBulkWarps, rg, nrg, nseg, jn, segc);
         const int64_t ui = c.pot[w.i];                 // used after the reduction: its latency overlaps it
         const int32_t* src = ring + (size_t)d * kBulkSeg;
         const int4* s4 = reinterpret_cast<const int4*>(src);
         const int4* v4 = reinterpret_cast<const int4*>(vt + w.a);
-        const int nq = (w.b - w.a) >> 2;
         int32_t bv = INT32_MAX, bj = INT32_MAX;
         const int jb = j0 + w.a;
-        #pragma unroll 4
-        for (int q = lane; q < nq; q += 32) min4(bv, bj, s4[q], v4[q], jb + 4 * q);
-        if (lane < ((w.b - w.a) & 3)) {
-            const int jl = 4 * nq + lane;
-            const int32_t tv = src[jl] - vt[w.a + jl];
-            if (tv < bv) { bv = tv; bj = jb + jl; }
+        if (h16) {
+            const int nq = (w.b - w.a) >> 3;
+            #pragma unroll 4
+            for (int q = lane; q < nq; q += 32) min8(bv, bj, s4[q], v4[2 * q], v4[2 * q + 1], jb + 8 * q);
+            if (lane < ((w.b - w.a) & 7)) {
+                const int jl = 8 * nq + lane;
+                const int32_t tv = (int32_t)reinterpret_cast<const int16_t*>(src)[jl] - vt[w.a + jl];
+                if (tv < bv) { bv = tv; bj = jb + jl; }
+            }
+        } else {
+            const int nq = (w.b - w.a) >> 2;
+            #pragma unroll 4
+            for (int q = lane; q < nq; q += 32) min4(bv, bj, s4[q], v4[q], jb + 4 * q);
+            if (lane < ((w.b - w.a) & 3)) {
+                const int jl = 4 * nq + lane;
+                const int32_t tv = src[jl] - vt[w.a + jl];
+                if (tv < bv) { bv = tv; bj = jb + jl; }
+            }
         }
         __syncwarp();                                  // every lane has read the buffer
         if (lane == 0 && j + kBulkDepth < cnt) {
@@ -838,17 +867,59 @@ __device__ void cluster_cand_sweep(const Ctx& c, int pn, bool narrow, int rank, 
     const int lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
     const int gw = rank * wpb + (threadIdx.x >> 5), nw = nctas * wpb;
-    const int nseg = (n + kSegCols - 1) / kSegCols;
+    // 16-bit costs: units of 2 kSegCols columns, the same 8 vectors per lane
+    const bool h16 = I.cost16 != nullptr && narrow;
+    const int segc = h16 ? 2 * kSegCols : kSegCols;
+    const int nseg = (n + segc - 1) / segc;
     const int units = pn * nseg;
     const int4* v4 = reinterpret_cast<const int4*>(c.v32);
     for (int u = gw; u < units; u += nw) {
         const int i = c.prow[u / nseg], sg = u % nseg;
         if (!FLOCK_IN(i, m)) { *bad = 1; continue; }
-        const int a = sg * kSegCols, b = min(n, a + kSegCols);
+        const int a = sg * segc, b = min(n, a + segc);
         const int64_t ui = c.pot[i];                   // used after the reduction: its latency overlaps it
         uint64_t key;
         if (!narrow) {
             key = row_best_exact(I.cost + (size_t)i * I.ldc, ui, c.pot + m, a, b);
+        } else if (h16) {
+            const int4* row = reinterpret_cast<const int4*>(I.cost16 + (size_t)i * I.ldc16);
+            int32_t bv = INT32_MAX, bj = INT32_MAX, bdual = 0;
+            const int qa = a >> 3, qb = b >> 3;
+            auto take8 = [&](const int4 cv, int q) {      // 8 costs against their duals (the winner's kept)
+                const int4 va = v4[2 * q], vb = v4[2 * q + 1];
+                const uint32_t w[4] = {(uint32_t)cv.x, (uint32_t)cv.y, (uint32_t)cv.z, (uint32_t)cv.w};
+                const int32_t v[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+                #pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const int32_t t = (int32_t)(int16_t)(uint16_t)(w[k >> 1] >> (16 * (k & 1))) - v[k];
+                    if (t < bv) { bv = t; bj = 8 * q + k; bdual = v[k]; }
+                }
+            };
+            if (qb - qa == kSegCols / 4) {
+                // a full segment: the lane's 8 cost vectors in flight at once
+                int4 cv[kSegCols / 128];
+                #pragma unroll
+                for (int k = 0; k < kSegCols / 128; k++) cv[k] = ld_stream4(row + qa + lane + 32 * k);
+                #pragma unroll
+                for (int k = 0; k < kSegCols / 128; k++) take8(cv[k], qa + lane + 32 * k);
+            } else {
+                for (int q = qa + lane; q < qb; q += 32) take8(row[q], q);
+            }
+            if (lane < b - 8 * qb) {
+                const int j = 8 * qb + lane;
+                const int32_t vj = c.v32[j];
+                const int32_t tv = (int32_t)I.cost16[(size_t)i * I.ldc16 + j] - vj;
+                if (tv < bv) { bv = tv; bj = j; bdual = vj; }
+            }
+            // the row key as narrow_row_key forms it; the winning column's
+            // dual comes from the lane that found it
+            const uint64_t mine = pack_i32(bv, (uint32_t)bj);
+            const uint64_t kk = warp_min_u64(mine);
+            const unsigned who = __ballot_sync(0xffffffffu, mine == kk);
+            const int32_t vw = __shfl_sync(0xffffffffu, bdual, __ffs(who) - 1);
+            const int64_t r = (int64_t)key_val(kk) - ui;
+            key = vw == kDead32 || r < INT32_MIN ? row_best_exact(I.cost + (size_t)i * I.ldc, ui, c.pot + m, a, b)
+                                                 : pack_i32(clamp32(r), (uint32_t)key_idx(kk));
         } else {
             const int4* row = reinterpret_cast<const int4*>(I.cost + (size_t)i * I.ldc);
             int32_t bv = INT32_MAX, bj = INT32_MAX, bdual = 0;
@@ -1557,10 +1628,12 @@ static int validate_shape(const flock_instance* I, std::string* msg) {
     return FLOCK_OK;
 }
 
-static bool costs_in_range(const int32_t* c, size_t cnt) {
-    int bad = 0;
-    for (size_t k = 0; k < cnt; k++) bad |= (c[k] > (1 << 30)) | (c[k] < -(1 << 30));
-    return !bad;
+static bool costs_in_range(const int32_t* c, size_t cnt, int32_t* lo_out = nullptr, int32_t* hi_out = nullptr) {
+    int32_t lo = INT32_MAX, hi = INT32_MIN;
+    for (size_t k = 0; k < cnt; k++) { lo = std::min(lo, c[k]); hi = std::max(hi, c[k]); }
+    if (lo_out) *lo_out = lo;
+    if (hi_out) *hi_out = hi;
+    return cnt == 0 || (lo >= -(1 << 30) && hi <= (1 << 30));
 }
 
 // Copy one cost row and check the accepted range |c| <= 2^30 in the same pass.
@@ -1654,13 +1727,17 @@ static void parallel_for(int count, const F& f) {
     if (!pool.try_run(nt, body)) body();
 }
 
-int validate_instance(const flock_instance* I) {
+// Shape and cost checks; with fits16, whether every cost fits in 16 bits.
+static int validate_instance_range(const flock_instance* I, bool* fits16) {
     std::string msg;
     const int rc = validate_shape(I, &msg);
     if (rc) { set_error(msg); return rc; }
-    if (!costs_in_range(I->cost, (size_t)I->m * I->n)) { set_error("cost out of range"); return FLOCK_ERR_RANGE; }
+    int32_t lo = 0, hi = 0;
+    if (!costs_in_range(I->cost, (size_t)I->m * I->n, &lo, &hi)) { set_error("cost out of range"); return FLOCK_ERR_RANGE; }
+    if (fits16) *fits16 = lo >= INT16_MIN && hi <= INT16_MAX;
     return FLOCK_OK;
 }
+int validate_instance(const flock_instance* I) { return validate_instance_range(I, nullptr); }
 
 // Scalars::mode of a pivot method: 0 sequential, 1 parallel, 2 switch, 3
 // parallel stepping stone.
@@ -1702,6 +1779,7 @@ struct PlainSolver {
     DevBuf ws, cost, sd;
     DevBuf books;                   // "vam_device" Vogel: row and column books
     DevBuf costT;                   // Vogel's column-major copy of the costs
+    DevBuf cost16;                  // grid path: 16-bit copy of the costs for the sweeps
     DevBuf one;                     // one-launch form: working set, basis, duals, scalars, descriptor
     HostBuf h_one;                  // one-launch form: pinned staging of its upload and download regions
     GridPivot* gp = nullptr;        // grid pivot round state (large instances)
@@ -1806,6 +1884,18 @@ struct PlainSolver {
         k_transpose<<<dim3((n + 31) / 32, (m + 31) / 32), dim3(32, 8), 0, stream>>>(c.I.cost, m, n, c.I.ldc,
                                                                                    costT.as<int32_t>(), ldcT);
         return cudaGetLastError() == cudaSuccess ? costT.as<int32_t>() : nullptr;
+    }
+    // The 16-bit copy of the uploaded costs into c.I (grid path, every cost
+    // fits); without room for it the sweeps read the int32 costs.
+    void narrow_copy(Ctx& c) {
+        const int m = c.I.m, n = c.I.n, ldc16 = (n + 7) & ~7;
+        if (cost16.ensure((size_t)m * ldc16 * 2 + 16) != cudaSuccess) { cudaGetLastError(); return; }
+        const size_t cells = (size_t)m * ldc16;
+        const int grid = (int)std::min<size_t>(4 * (size_t)num_sms(), (cells + 255) / 256);
+        k_cost16<<<std::max(1, grid), 256, 0, stream>>>(c.I.cost, m, n, c.I.ldc, cost16.as<int16_t>(), ldc16);
+        if (cudaGetLastError() != cudaSuccess) return;
+        c.I.cost16 = cost16.as<int16_t>();
+        c.I.ldc16 = ldc16;
     }
     // Dynamic shared memory of the Vogel launches (0: the line state stays
     // in the working set).
@@ -1959,7 +2049,8 @@ static int solve_one_launch(PlainSolver& P, const flock_instance* I, const flock
 static int solve_plain(const flock_instance* I, const flock_options* opt_in, flock_flow* flows,
                        int64_t* du, int64_t* dv, flock_stats* st) {
     const auto t0 = std::chrono::steady_clock::now();
-    int rc = validate_instance(I);
+    bool fits16 = false;
+    int rc = validate_instance_range(I, &fits16);
     if (rc) return rc;
     flock_options opt;
     flock_default_options(&opt);
@@ -1978,6 +2069,10 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     Ctx c;
     int32_t* out3 = nullptr;
     if ((rc = P.prepare(I, c, &out3))) return rc;
+    // the grid path's sweeps read 16-bit costs when every cost fits
+    // (FLOCK_COST16=0 keeps them on the int32 costs)
+    const char* c16_env = getenv("FLOCK_COST16");
+    if (fits16 && V >= kGridPivotV && !(c16_env && !strcmp(c16_env, "0"))) P.narrow_copy(c);
     // partial pricing runs on the plain path from kGridPivotV vertices (grid rounds)
     const bool partial = pricing_of(opt) && V >= kGridPivotV;
     if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds, partial))) return rc;
@@ -2219,7 +2314,10 @@ static void sweep_shape(int m, int n, int* grid, int* tile, int* ntile) {
 static int test_sweep(int m, int n, const int32_t* cost, const int64_t* pot, uint64_t* keys, int cta_form,
                       int threads) {
     if (m < 1 || n < 1 || !cost || !pot || !keys) return FLOCK_ERR_ARG;
-    if (cta_form && (threads < 32 || threads > 1024 || threads % 32)) return FLOCK_ERR_ARG;
+    if (cta_form > 0 && (threads < 32 || threads > 1024 || threads % 32)) return FLOCK_ERR_ARG;
+    if (cta_form < 0)        // the bulk sweep on the 16-bit copy: every cost must fit
+        for (size_t k = 0; k < (size_t)m * n; k++)
+            if (cost[k] < INT16_MIN || cost[k] > INT16_MAX) return FLOCK_ERR_RANGE;
     PlainSolver& P = plain();
     std::lock_guard<std::mutex> lk(P.mu);
     int rc = P.setup();
@@ -2241,7 +2339,11 @@ static int test_sweep(int m, int n, const int32_t* cost, const int64_t* pot, uin
     FLOCK_CK(cudaMemcpyAsync(c.pot, pot, (size_t)V * 8, cudaMemcpyHostToDevice, P.stream));
     k_publish_duals<<<1, 1024, 0, P.stream>>>(c);
     FLOCK_CK(cudaMemsetAsync(c.row_best, 0xff, (size_t)m * 8, P.stream));
-    if (cta_form) {
+    if (cta_form < 0) {
+        P.narrow_copy(c);
+        if (!c.I.cost16) { set_error("no room for the 16-bit copy"); return FLOCK_ERR_CUDA; }
+    }
+    if (cta_form > 0) {
         k_sweep_cta_only<<<1, threads, 0, P.stream>>>(c);
     } else {
         int grid = 0, tile = 0, ntile = 0;
@@ -3195,7 +3297,9 @@ int flock_test_parallel_for(int32_t count, int32_t* hits) {
     return FLOCK_OK;
 }
 
-/* Test hook: one reduced-cost sweep over host costs and duals, row keys back. */
+/* Test hook: one reduced-cost sweep over host costs and duals, row keys back
+ * (cta_form 0: the bulk sweep; > 0: the one-block sweep with `threads`;
+ * < 0: the bulk sweep on the 16-bit copy of the costs). */
 int flock_test_sweep(int32_t m, int32_t n, const int32_t* cost, const int64_t* pot, uint64_t* keys,
                      int32_t cta_form, int32_t threads) {
     return flock::test_sweep(m, n, cost, pot, keys, cta_form, threads);

@@ -457,6 +457,18 @@ __device__ __forceinline__ void min4(int32_t& bv, int32_t& bj, const int4 cv, co
     t = cv.w - vv.w; if (t < bv) { bv = t; bj = j + 3; }
 }
 
+// Eight 16-bit costs (one 16-byte vector) against their eight int32 duals.
+__device__ __forceinline__ void min8(int32_t& bv, int32_t& bj, const int4 cv, const int4 va, const int4 vb, int j) {
+    const uint32_t w[4] = {(uint32_t)cv.x, (uint32_t)cv.y, (uint32_t)cv.z, (uint32_t)cv.w};
+    const int32_t v[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+    #pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int32_t c = (int32_t)(int16_t)(uint16_t)(w[k >> 1] >> (16 * (k & 1)));
+        const int32_t t = c - v[k];
+        if (t < bv) { bv = t; bj = j + k; }
+    }
+}
+
 // Turn the warp's narrow minimum over columns [j0, j1) of row i into the
 // row key.  The key equals row_best_exact's unless the winning column is a
 // zero-demand one or the reduced cost is below INT32_MIN; those rows are

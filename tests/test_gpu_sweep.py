@@ -64,6 +64,18 @@ def test_sweep_narrow(m, n):
             np.testing.assert_array_equal(gpu_keys(cost, pot, 1, thr), exp)
 
 
+@pytest.mark.parametrize("m,n", [(1, 1), (3, 2), (7, 9), (37, 53), (9, 2047), (9, 2048), (9, 2049), (4, 4100),
+                                 (300, 301), (3, 8193), (2, 20003)])
+def test_sweep_16bit_copy(m, n):
+    """The bulk sweep on the 16-bit copy of the costs (the grid path's sweeps
+    when every cost fits): keys identical to the int32 form's, costs at the
+    16-bit limits included."""
+    cost, pot = case(m * 131 + n, m, n, lo=-32768, hi=32767, plo=-40000, phi=40000)
+    exp = expected_keys(cost, pot)
+    np.testing.assert_array_equal(gpu_keys(cost, pot, -1), exp)
+    np.testing.assert_array_equal(gpu_keys(cost, pot, 0), exp)
+
+
 @pytest.mark.parametrize("m,n", [(5, 7), (40, 1500), (3, 9000)])
 def test_sweep_ties_and_dead_columns(m, n):
     cost = np.full((m, n), 5, np.int32)
@@ -72,6 +84,7 @@ def test_sweep_ties_and_dead_columns(m, n):
     pot[:m] = 7                       # every live reduced cost is -2: first live column wins
     exp = expected_keys(cost, pot)
     np.testing.assert_array_equal(gpu_keys(cost, pot), exp)
+    np.testing.assert_array_equal(gpu_keys(cost, pot, -1), exp)
     if n <= 3000:
         np.testing.assert_array_equal(gpu_keys(cost, pot, 1, 256), exp)
     # a dead column holds the int32 minimum (cheaper cost, live duals at the
