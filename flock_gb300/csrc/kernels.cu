@@ -859,9 +859,125 @@ __device__ __forceinline__ int cluster_ctas() {
     return (int)r;
 }
 
-// Sweep of the candidate rows prow[0..pn) over the cluster: (row, segment of
-// kSegCols columns) units, one warp each, keys into row_best by atomicMin.
-__device__ void cluster_cand_sweep(const Ctx& c, int pn, bool narrow, int rank, int nctas, int* bad) {
+// The cluster rounds' register form (every thread owns at most one vertex:
+// V <= CTAs x threads).  During the rounds the owner is the only writer of
+// its vertex's parent, depth, flow, interval and dual, so it keeps them in
+// registers and writes them through for the other readers (the candidate
+// sweep's duals, the entering cell's endpoints, the path cache, the next
+// launch).
+struct OwnVertex {
+    int32_t v, parent, depth, side;
+    int64_t flow, pot;
+    int2 iv;
+};
+
+__device__ __forceinline__ void own_load(const Ctx& c, OwnVertex& o, int v, const int2* ivA) {
+    const int V = c.I.m + c.I.n;
+    o.v = v;
+    o.side = 0;
+    if (v < V) { o.parent = c.parent[v]; o.depth = c.depth[v]; o.flow = c.flow[v]; o.pot = c.pot[v]; o.iv = ivA[v]; }
+    else { o.parent = -2; o.depth = 0; o.flow = 0; o.pot = 0; o.iv = make_int2(0, 0); }
+}
+
+// member_slice for the owned vertex (its side kept in the register state).
+__device__ __forceinline__ void member_one(const Ctx& c, OwnVertex& o, int pk, int pl, int dk, int dl,
+                                           uint64_t& mk, uint64_t& ml) {
+    const int m = c.I.m, V = m + c.I.n;
+    o.side = 0;
+    if (o.v >= V || o.parent < 0) return;
+    const bool on_k = iv_in(o.iv, pk), on_l = iv_in(o.iv, pl);
+    if (on_k == on_l) return;
+    o.side = on_k ? 1 : 2;
+    const int i = (o.side == 1 ? dk : dl) - o.depth;
+    if (!FLOCK_IN(i, V)) { fail_check(c.sc, 17); return; }
+    const int slot = o.side == 1 ? i : V - 1 - i;
+    c.path[slot] = o.v;
+    c.pflow[slot] = o.flow;
+    if (o.side == 1 && o.v < m) { const uint64_t f = oflow(o.flow); mk = f < mk ? f : mk; }
+    if (o.side == 2 && o.v >= m) { const uint64_t f = oflow(o.flow); ml = f < ml ? f : ml; }
+}
+
+// pick_slice for the owned vertex.
+__device__ __forceinline__ uint64_t pick_one(const Ctx& c, const OwnVertex& o, bool lside, uint64_t fmin) {
+    const int m = c.I.m;
+    if ((lside ? (o.side == 2 && o.v >= m) : (o.side == 1 && o.v < m)) && oflow(o.flow) == fmin)
+        return ((uint64_t)(uint32_t)o.depth << 32) | (uint32_t)o.v;
+    return lside ? kNoKey : 0ull;
+}
+
+// update_slice for the owned vertex, its register state updated with it.
+__device__ __forceinline__ void update_one(const Ctx& c, const PivotParams& pp, OwnVertex& o, const int2* ivA,
+                                           int2* ivB, int& dwide, int& bad, const int32_t* spv, const int2* siv) {
+    const int m = c.I.m, V = m + c.I.n;
+    const int v = o.v;
+    if (v >= V || o.parent == -2) return;
+    const int t = pp.t;
+    const bool lside = pp.eside == 2;
+    const int base = lside ? V - 1 : 0, dir = lside ? -1 : 1;   // e's chain entry i at path[base + dir * i]
+    const int2 Q = pp.Q, O = pp.O;
+    const int P = Q.x, s = Q.y;
+    const int ins = O.x - (O.x >= P + s ? s : 0) + 1;
+    const int2 w = o.iv;
+    int2 nw;
+    if (iv_in(Q, w.x)) {
+        int lo = 0, hi = t;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            const int pv = spv ? spv[mid] : c.path[base + dir * mid];
+            if (!FLOCK_IN(pv, V)) { bad = 1; break; }
+            if (iv_in(siv ? siv[mid] : ivA[pv], w.x)) hi = mid; else lo = mid + 1;
+        }
+        const int i = lo;
+        const int pi = spv ? spv[i] : c.path[base + dir * i];
+        if (!FLOCK_IN(pi, V)) { bad = 1; return; }
+        const int2 Pi = siv ? siv[i] : ivA[pi];
+        int off = 0, rank = w.x - Pi.x;
+        int pc = -1;
+        if (i > 0) {
+            pc = spv ? spv[i - 1] : c.path[base + dir * (i - 1)];
+            if (!FLOCK_IN(pc, V)) { bad = 1; return; }
+            const int2 Pc = siv ? siv[i - 1] : ivA[pc];
+            off = Pc.y;
+            if (w.x >= Pc.x) rank -= Pc.y;
+        }
+        nw.x = ins + off + rank;
+        nw.y = v == pi ? s - off : w.y;
+        o.depth = pp.dother + 1 - pp.de + 2 * i + o.depth;
+        c.depth[v] = o.depth;
+        const int64_t p0 = o.pot;
+        const int64_t p1 = p0 + ((v < m) == (pp.e < m) ? pp.r : -pp.r);
+        o.pot = p1;
+        c.pot[v] = p1;
+        if (v >= m) {
+            int w0 = 0, w1 = 0;
+            narrow_dual(p0, w0);
+            c.v32[v - m] = narrow_dual(p1, w1);
+            dwide += w1 - w0;
+        }
+        if (v == pi) {                             // the reversed path (every cycle edge in S is on it)
+            o.parent = i == 0 ? pp.other : pc;
+            o.flow = i == 0 ? pp.th : c.pflow[base + dir * (i - 1)] + ((pp.eside == 1) == (pc < m) ? -pp.th : pp.th);
+            c.parent[v] = o.parent;
+            c.flow[v] = o.flow;
+        }
+    } else {
+        if (o.side) {
+            o.flow += (o.side == 1) == (v < m) ? -pp.th : pp.th;
+            c.flow[v] = o.flow;
+        }
+        const int y = w.x - (w.x >= P + s ? s : 0);
+        nw.x = y + (y >= ins ? s : 0);
+        nw.y = w.y - (iv_in(w, P) ? s : 0) + (iv_in(w, O.x) ? s : 0);
+    }
+    o.iv = nw;
+    ivB[v] = nw;
+}
+
+// Sweep of the candidate rows prow[0..pn) (the launch's shared copy of
+// c.prow) over the cluster: (row, segment of kSegCols columns) units, one
+// warp each, keys into row_best by atomicMin.
+__device__ void cluster_cand_sweep(const Ctx& c, const int32_t* prow, int pn, bool narrow, int rank, int nctas,
+                                   int* bad) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
     const int lane = threadIdx.x & 31;
@@ -874,7 +990,7 @@ __device__ void cluster_cand_sweep(const Ctx& c, int pn, bool narrow, int rank, 
     const int units = pn * nseg;
     const int4* v4 = reinterpret_cast<const int4*>(c.v32);
     for (int u = gw; u < units; u += nw) {
-        const int i = c.prow[u / nseg], sg = u % nseg;
+        const int i = prow[u / nseg], sg = u % nseg;
         if (!FLOCK_IN(i, m)) { *bad = 1; continue; }
         const int a = sg * segc, b = min(n, a + segc);
         const int64_t ui = c.pot[i];                   // used after the reduction: its latency overlaps it
@@ -974,11 +1090,13 @@ constexpr size_t kCRoundSmem = (size_t)kPathCache * (sizeof(int2) + sizeof(int32
 // full_first: round 0 is the pivot of the full round that k_gchoose_all has
 // just priced and counted (its entering cell in gp->best, every row key
 // current); its update clears every row key for the coming candidate sweeps.
+template <bool kOne>
 __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivot* cp, const GridPivot* gp,
                                                               int full_first) {
     __shared__ BlockScratch bs;
     __shared__ PhaseLocal phl;
     __shared__ uint64_t s_red[2];
+    __shared__ int32_t s_prow[kPPRows];    // the candidate rows: fixed for the launch
     extern __shared__ __align__(16) unsigned char cr_smem[];
     int2* siv = reinterpret_cast<int2*>(cr_smem);
     int32_t* spv = reinterpret_cast<int32_t*>(siv + kPathCache);
@@ -995,9 +1113,12 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     const int pivots0 = pivots;
     const bool partial = c.sc->pricing != 0;
     const uint64_t full_best = full_first ? gp->best : kNoKey;
+    for (int t = threadIdx.x; t < pn; t += blockDim.x) s_prow[t] = c.prow[t];   // visible after barrier 0
     if (rank == 0 && threadIdx.x == 0) { cp->abort[0] = 0; cp->abort[1] = 0; }
     if (threadIdx.x == 0) cp->dwide[rank] = 0;
     const int v0 = rank * blockDim.x + threadIdx.x, stride = nctas * blockDim.x;
+    OwnVertex own;
+    if (kOne) own_load(c, own, v0, c.iv + (ivp ? V : 0));
     enum { kRun, kExhausted, kAged, kCapped, kFailed };
     int why = kRun;
     for (int r = 0;; r++) {
@@ -1012,7 +1133,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         if (!full_round && age >= refresh) { why = kAged; break; }
         ps.mark(PH_SWEEP);
         int bad = 0;
-        if (!full_round) cluster_cand_sweep(c, pn, nwide == 0, rank, nctas, &bad);
+        if (!full_round) cluster_cand_sweep(c, s_prow, pn, nwide == 0, rank, nctas, &bad);
         if (bad) { fail_check(c.sc, 19); cp->abort[r & 1] = 1; }
         cluster_sync_all();                                      // barrier 1
         if (rank == 0 && threadIdx.x == 0 && r > 0) cp->abort[(r - 1) & 1] = 0;   // read by all before barrier 1
@@ -1023,7 +1144,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
             best = full_best;
         } else {
             for (int t = threadIdx.x; t < pn; t += blockDim.x) {
-                const int i = c.prow[t];
+                const int i = s_prow[t];
                 if (!FLOCK_IN(i, m)) continue;
                 const uint64_t key = c.row_best[i];
                 if (key != kNoKey && key_val(key) < 0 && key_idx(key) < ncols) {
@@ -1047,7 +1168,8 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         const int dk = c.depth[k], dl = c.depth[l];
         const int64_t r_enter = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
         uint64_t mk = kNoKey, ml = kNoKey;
-        member_slice(c, ivA, k, l, dk, dl, v0, stride, mk, ml);
+        if (kOne) member_one(c, own, ivA[k].x, ivA[l].x, dk, dl, mk, ml);
+        else member_slice(c, ivA, k, l, dk, dl, v0, stride, mk, ml);
         mk = block_min_u64(mk, bs);
         ml = block_min_u64(ml, bs);
         if (threadIdx.x == 0) { cp->mk[rank] = mk; cp->ml[rank] = ml; }
@@ -1062,7 +1184,8 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         const uint64_t gmk = s_red[0], gml = s_red[1];
         const bool lside = gml <= gmk;
         const uint64_t fmin = lside ? gml : gmk;
-        uint64_t pick = fmin == kNoKey ? (lside ? kNoKey : 0ull) : pick_slice(c, lside, fmin, v0, stride);
+        uint64_t pick = fmin == kNoKey ? (lside ? kNoKey : 0ull)
+                                       : kOne ? pick_one(c, own, lside, fmin) : pick_slice(c, lside, fmin, v0, stride);
         pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
         if (threadIdx.x == 0) cp->pick[rank] = pick;
         cluster_sync_all();                                      // barrier 3
@@ -1107,7 +1230,8 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         if (threadIdx.x == 0) bs.i[7] = 0;
         __syncthreads();
         int dwide = 0, ubad = 0;
-        update_slice(c, pp, ivA, ivB, v0, stride, dwide, ubad, cached ? spv : nullptr, cached ? siv : nullptr);
+        if (kOne) update_one(c, pp, own, ivA, ivB, dwide, ubad, cached ? spv : nullptr, cached ? siv : nullptr);
+        else update_slice(c, pp, ivA, ivB, v0, stride, dwide, ubad, cached ? spv : nullptr, cached ? siv : nullptr);
         if (ubad) { fail_check(c.sc, 24); cp->abort[r & 1] = 1; }
         if (dwide) atomicAdd(&bs.i[7], dwide);
         __syncthreads();
@@ -1118,7 +1242,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
             for (int i = v0; i < m; i += stride) c.row_best[i] = kNoKey;
         } else if (rank == 0) {
             for (int t2 = threadIdx.x; t2 < pn; t2 += blockDim.x) {
-                const int i = c.prow[t2];
+                const int i = s_prow[t2];
                 if (FLOCK_IN(i, m)) c.row_best[i] = kNoKey;
             }
         }
@@ -1130,7 +1254,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         cluster_sync_all();          // every CTA has read the candidate keys
         if (rank == 0)
             for (int t2 = threadIdx.x; t2 < pn; t2 += blockDim.x) {
-                const int i = c.prow[t2];
+                const int i = s_prow[t2];
                 if (FLOCK_IN(i, m)) c.row_best[i] = kNoKey;
             }
     }
@@ -1807,16 +1931,20 @@ struct PlainSolver {
                                       (int)kVogelStageMax));
         // the largest cluster the cluster rounds can be launched with (one cluster)
         cluster_ctas = 0;
-        if (cudaFuncSetAttribute(k_cround, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-            cudaFuncSetAttribute(k_cround, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCRoundSmem) ==
+        if (cudaFuncSetAttribute(k_cround<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            cudaFuncSetAttribute(k_cround<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCRoundSmem) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k_cround<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+            cudaFuncSetAttribute(k_cround<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCRoundSmem) ==
                 cudaSuccess) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(kClusterMax);
             cfg.blockDim = dim3(kCRoundThreads);
             cfg.dynamicSmemBytes = kCRoundSmem;
-            int cs = 0;
-            if (cudaOccupancyMaxPotentialClusterSize(&cs, (const void*)k_cround, &cfg) == cudaSuccess)
-                cluster_ctas = std::min(cs, kClusterMax);
+            int cs = 0, cs1 = 0;
+            if (cudaOccupancyMaxPotentialClusterSize(&cs, (const void*)k_cround<false>, &cfg) == cudaSuccess &&
+                cudaOccupancyMaxPotentialClusterSize(&cs1, (const void*)k_cround<true>, &cfg) == cudaSuccess)
+                cluster_ctas = std::min(std::min(cs, cs1), kClusterMax);
         }
         if (cluster_ctas < 2) cluster_ctas = 0;
         cudaGetLastError();
@@ -2140,7 +2268,11 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                     }
                     if (clustered) {
                         // the full round's pivot and the candidate rounds in one cluster launch
-                        FLOCK_CK(cudaLaunchKernelEx(&ccfg, k_cround, c, P.cp, (const GridPivot*)P.gp, 1));
+                        // the register form when every thread owns at most one vertex
+                        if (V <= P.cluster_ctas * kCRoundThreads)
+                            FLOCK_CK(cudaLaunchKernelEx(&ccfg, k_cround<true>, c, P.cp, (const GridPivot*)P.gp, 1));
+                        else
+                            FLOCK_CK(cudaLaunchKernelEx(&ccfg, k_cround<false>, c, P.cp, (const GridPivot*)P.gp, 1));
                     } else {
                         k_gmember<<<gg, 256, 0, P.stream>>>(c, P.gp);
                         k_gpick<<<gg, 256, 0, P.stream>>>(c, P.gp);
