@@ -839,8 +839,6 @@ constexpr int kCRoundThreads = 1024;
 constexpr int kClusterMax = 16;
 
 struct ClusterPivot {
-    uint64_t mk[kClusterMax], ml[kClusterMax];     // member step: each CTA's side minima
-    uint64_t pick[kClusterMax];                    // pick step: each CTA's leaving-edge candidate
     int32_t dwide[kClusterMax];                    // update step: change of the int32-window miss count
     int32_t abort[2];                              // a failed check in the round of that parity
 };
@@ -848,6 +846,19 @@ struct ClusterPivot {
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+// Another CTA's copy of a shared variable (distributed shared memory): the
+// writer stores it before a cluster barrier, the readers load it after.
+__device__ __forceinline__ uint32_t dsmem_of(const void* local, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(local)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ uint64_t dsmem_ld_u64(uint32_t a) {
+    uint64_t v;
+    asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ int cluster_rank() {
     uint32_t r;
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -1095,7 +1106,9 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
                                                               int full_first) {
     __shared__ BlockScratch bs;
     __shared__ PhaseLocal phl;
-    __shared__ uint64_t s_red[2];
+    // this CTA's share of the round's cluster-wide minima, read by warp 0 of
+    // every CTA through distributed shared memory (s_red: the results)
+    __shared__ uint64_t x_mk, x_ml, x_pick, s_red[2];
     __shared__ int32_t s_prow[kPPRows];    // the candidate rows: fixed for the launch
     extern __shared__ __align__(16) unsigned char cr_smem[];
     int2* siv = reinterpret_cast<int2*>(cr_smem);
@@ -1116,6 +1129,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     for (int t = threadIdx.x; t < pn; t += blockDim.x) s_prow[t] = c.prow[t];   // visible after barrier 0
     if (rank == 0 && threadIdx.x == 0) { cp->abort[0] = 0; cp->abort[1] = 0; }
     if (threadIdx.x == 0) cp->dwide[rank] = 0;
+    const int lane = threadIdx.x & 31;
     const int v0 = rank * blockDim.x + threadIdx.x, stride = nctas * blockDim.x;
     OwnVertex own;
     if (kOne) own_load(c, own, v0, c.iv + (ivp ? V : 0));
@@ -1172,13 +1186,13 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         else member_slice(c, ivA, k, l, dk, dl, v0, stride, mk, ml);
         mk = block_min_u64(mk, bs);
         ml = block_min_u64(ml, bs);
-        if (threadIdx.x == 0) { cp->mk[rank] = mk; cp->ml[rank] = ml; }
+        if (threadIdx.x == 0) { x_mk = mk; x_ml = ml; }
         cluster_sync_all();                                      // barrier 2
         ps.mark(PH_ADJUST);
-        if (threadIdx.x == 0) {
-            uint64_t a = kNoKey, b = kNoKey;
-            for (int q = 0; q < nctas; q++) { a = min(a, cp->mk[q]); b = min(b, cp->ml[q]); }
-            s_red[0] = a; s_red[1] = b;
+        if (threadIdx.x < 32) {
+            const uint64_t a = warp_min_u64(lane < nctas ? dsmem_ld_u64(dsmem_of(&x_mk, lane)) : kNoKey);
+            const uint64_t b = warp_min_u64(lane < nctas ? dsmem_ld_u64(dsmem_of(&x_ml, lane)) : kNoKey);
+            if (lane == 0) { s_red[0] = a; s_red[1] = b; }
         }
         __syncthreads();
         const uint64_t gmk = s_red[0], gml = s_red[1];
@@ -1187,15 +1201,12 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         uint64_t pick = fmin == kNoKey ? (lside ? kNoKey : 0ull)
                                        : kOne ? pick_one(c, own, lside, fmin) : pick_slice(c, lside, fmin, v0, stride);
         pick = lside ? block_min_u64(pick, bs) : block_max_u64(pick, bs);
-        if (threadIdx.x == 0) cp->pick[rank] = pick;
+        if (threadIdx.x == 0) x_pick = pick;
         cluster_sync_all();                                      // barrier 3
-        if (threadIdx.x == 0) {
-            uint64_t q64 = lside ? kNoKey : 0ull;
-            for (int q = 0; q < nctas; q++) {
-                const uint64_t x = cp->pick[q];
-                q64 = lside ? min(q64, x) : max(q64, x);
-            }
-            s_red[0] = q64;
+        if (threadIdx.x < 32) {
+            const uint64_t x = lane < nctas ? dsmem_ld_u64(dsmem_of(&x_pick, lane)) : (lside ? kNoKey : 0ull);
+            const uint64_t y = lside ? warp_min_u64(x) : warp_max_u64(x);
+            if (lane == 0) s_red[0] = y;
         }
         __syncthreads();
         const uint64_t q64 = s_red[0];
@@ -1249,9 +1260,11 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         ivp ^= 1;
         pivots++;
     }
-    // every CTA leaves the loop at the same point; CTA 0 writes the scalars back
+    // every CTA leaves the loop at the same point; none exits while another
+    // may still read its shared variables or the candidate keys
+    cluster_sync_all();
+    // CTA 0 writes the scalars back
     if (why == kExhausted) {
-        cluster_sync_all();          // every CTA has read the candidate keys
         if (rank == 0)
             for (int t2 = threadIdx.x; t2 < pn; t2 += blockDim.x) {
                 const int i = s_prow[t2];
