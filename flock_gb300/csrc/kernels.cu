@@ -498,7 +498,7 @@ __device__ void grid_choose(const Ctx& c, GridPivot* gp, BlockScratch& bs, bool 
 // side, as single_pivot_iv records them), over the vertices v0, v0 + stride,
 // ...  (iv: the current interval buffer; dk, dl: the endpoints' depths).
 __device__ __forceinline__ void member_slice(const Ctx& c, const int2* iv, int k, int l, int dk, int dl, int v0,
-                                             int stride, uint64_t& mk, uint64_t& ml) {
+                                             int stride, uint64_t& mk, uint64_t& ml, int2* piv = nullptr) {
     const int m = c.I.m, V = m + c.I.n;
     const int pk = iv[k].x, pl = iv[l].x;
     for (int v = v0; v < V; v += stride) {
@@ -516,6 +516,7 @@ __device__ __forceinline__ void member_slice(const Ctx& c, const int2* iv, int k
         const int slot = side == 1 ? i : V - 1 - i;
         c.path[slot] = v;
         c.pflow[slot] = f;
+        if (piv) piv[slot] = iv[v];
         if (side == 1 && v < m) { const uint64_t o = oflow(f); mk = o < mk ? o : mk; }
         if (side == 2 && v >= m) { const uint64_t o = oflow(f); ml = o < ml ? o : ml; }
     }
@@ -892,7 +893,7 @@ __device__ __forceinline__ void own_load(const Ctx& c, OwnVertex& o, int v, cons
 
 // member_slice for the owned vertex (its side kept in the register state).
 __device__ __forceinline__ void member_one(const Ctx& c, OwnVertex& o, int pk, int pl, int dk, int dl,
-                                           uint64_t& mk, uint64_t& ml) {
+                                           uint64_t& mk, uint64_t& ml, int2* piv) {
     const int m = c.I.m, V = m + c.I.n;
     o.side = 0;
     if (o.v >= V || o.parent < 0) return;
@@ -904,6 +905,7 @@ __device__ __forceinline__ void member_one(const Ctx& c, OwnVertex& o, int pk, i
     const int slot = o.side == 1 ? i : V - 1 - i;
     c.path[slot] = o.v;
     c.pflow[slot] = o.flow;
+    piv[slot] = o.iv;
     if (o.side == 1 && o.v < m) { const uint64_t f = oflow(o.flow); mk = f < mk ? f : mk; }
     if (o.side == 2 && o.v >= m) { const uint64_t f = oflow(o.flow); ml = f < ml ? f : ml; }
 }
@@ -987,8 +989,8 @@ __device__ __forceinline__ void update_one(const Ctx& c, const PivotParams& pp, 
 // Sweep of the candidate rows prow[0..pn) (the launch's shared copy of
 // c.prow) over the cluster: (row, segment of kSegCols columns) units, one
 // warp each, keys into row_best by atomicMin.
-__device__ void cluster_cand_sweep(const Ctx& c, const int32_t* prow, int pn, bool narrow, int rank, int nctas,
-                                   int* bad) {
+__device__ uint64_t cluster_cand_sweep(const Ctx& c, const int32_t* prow, int pn, bool narrow, int rank, int nctas,
+                                       int* bad) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n;
     const int lane = threadIdx.x & 31;
@@ -1000,6 +1002,7 @@ __device__ void cluster_cand_sweep(const Ctx& c, const int32_t* prow, int pn, bo
     const int nseg = (n + segc - 1) / segc;
     const int units = pn * nseg;
     const int4* v4 = reinterpret_cast<const int4*>(c.v32);
+    uint64_t best = kNoKey;
     for (int u = gw; u < units; u += nw) {
         const int i = prow[u / nseg], sg = u % nseg;
         if (!FLOCK_IN(i, m)) { *bad = 1; continue; }
@@ -1090,7 +1093,15 @@ __device__ void cluster_cand_sweep(const Ctx& c, const int32_t* prow, int pn, bo
                                                  : pack_i32(clamp32(r), (uint32_t)jw);
         }
         if (lane == 0) atomicMin((unsigned long long*)&c.row_best[i], (unsigned long long)key);
+        // the sequential rule's entering row over this warp's units: the
+        // smallest (reduced cost, row) among the negative unit keys, which
+        // over all units equals the smallest (row key, row) of the rows
+        if (key != kNoKey && key_val(key) < 0) {
+            const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
+            best = P < best ? P : best;
+        }
     }
+    return best;
 }
 
 // Entries of the re-hung path the cluster rounds cache in shared memory for
@@ -1108,7 +1119,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     __shared__ PhaseLocal phl;
     // this CTA's share of the round's cluster-wide minima, read by warp 0 of
     // every CTA through distributed shared memory (s_red: the results)
-    __shared__ uint64_t x_mk, x_ml, x_pick, s_red[2];
+    __shared__ uint64_t x_best, x_mk, x_ml, x_pick, s_red[2];
     __shared__ int32_t s_prow[kPPRows];    // the candidate rows: fixed for the launch
     extern __shared__ __align__(16) unsigned char cr_smem[];
     int2* siv = reinterpret_cast<int2*>(cr_smem);
@@ -1116,7 +1127,6 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     PhaseScope ps(c.ph, &phl, PH_SWEEP);
     const int rank = cluster_rank(), nctas = cluster_ctas();
     const int m = c.I.m, V = m + c.I.n;
-    const uint32_t ncols = (uint32_t)c.I.n;
     // the solve's scalars, read by every CTA before any CTA can change them
     const int done0 = c.sc->done;
     const int pn = min(max(c.sc->pp_n, 0), kPPRows);
@@ -1133,6 +1143,10 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     const int v0 = rank * blockDim.x + threadIdx.x, stride = nctas * blockDim.x;
     OwnVertex own;
     if (kOne) own_load(c, own, v0, c.iv + (ivp ? V : 0));
+    // the path entries' old intervals, written with the entries by the
+    // membership step: the pointer-jumping scratch acc0 (8 bytes per
+    // vertex), which only the rebuilds use and the cluster rounds never run
+    int2* piv = reinterpret_cast<int2*>(c.acc0);
     enum { kRun, kExhausted, kAged, kCapped, kFailed };
     int why = kRun;
     for (int r = 0;; r++) {
@@ -1147,26 +1161,26 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         if (!full_round && age >= refresh) { why = kAged; break; }
         ps.mark(PH_SWEEP);
         int bad = 0;
-        if (!full_round) cluster_cand_sweep(c, s_prow, pn, nwide == 0, rank, nctas, &bad);
+        if (!full_round) {
+            // this CTA's smallest (reduced cost, row), for the cluster's entering cell
+            const uint64_t mine = block_min_u64(cluster_cand_sweep(c, s_prow, pn, nwide == 0, rank, nctas, &bad), bs);
+            if (threadIdx.x == 0) x_best = mine;
+        }
         if (bad) { fail_check(c.sc, 19); cp->abort[r & 1] = 1; }
         cluster_sync_all();                                      // barrier 1
         if (rank == 0 && threadIdx.x == 0 && r > 0) cp->abort[(r - 1) & 1] = 0;   // read by all before barrier 1
         // the entering cell: the full round's, else the smallest (reduced
-        // cost, row) among the candidates
+        // cost, row) over the CTAs' units (distributed shared memory)
         uint64_t best = kNoKey;
         if (full_round) {
             best = full_best;
         } else {
-            for (int t = threadIdx.x; t < pn; t += blockDim.x) {
-                const int i = s_prow[t];
-                if (!FLOCK_IN(i, m)) continue;
-                const uint64_t key = c.row_best[i];
-                if (key != kNoKey && key_val(key) < 0 && key_idx(key) < ncols) {
-                    const uint64_t P = pack_i32(key_val(key), (uint32_t)i);
-                    best = P < best ? P : best;
-                }
+            if (threadIdx.x < 32) {
+                const uint64_t b = warp_min_u64(lane < nctas ? dsmem_ld_u64(dsmem_of(&x_best, lane)) : kNoKey);
+                if (lane == 0) s_red[0] = b;
             }
-            best = block_min_u64(best, bs);
+            __syncthreads();
+            best = s_red[0];
         }
         if (best == kNoKey || !FLOCK_IN((int)key_idx(best), m)) { why = kExhausted; break; }
         if (!full_round) {           // the full round was counted when it was priced
@@ -1182,8 +1196,8 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         const int dk = c.depth[k], dl = c.depth[l];
         const int64_t r_enter = (int64_t)cost_of(c.I, k, l - m) - c.pot[k] - c.pot[l];
         uint64_t mk = kNoKey, ml = kNoKey;
-        if (kOne) member_one(c, own, ivA[k].x, ivA[l].x, dk, dl, mk, ml);
-        else member_slice(c, ivA, k, l, dk, dl, v0, stride, mk, ml);
+        if (kOne) member_one(c, own, ivA[k].x, ivA[l].x, dk, dl, mk, ml, piv);
+        else member_slice(c, ivA, k, l, dk, dl, v0, stride, mk, ml, piv);
         mk = block_min_u64(mk, bs);
         ml = block_min_u64(ml, bs);
         if (threadIdx.x == 0) { x_mk = mk; x_ml = ml; }
@@ -1233,9 +1247,8 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
         if (cached) {
             const int base = lside ? V - 1 : 0, dir = lside ? -1 : 1;
             for (int i = threadIdx.x; i <= t; i += blockDim.x) {
-                const int pv = c.path[base + dir * i];
-                spv[i] = pv;
-                siv[i] = FLOCK_IN(pv, V) ? ivA[pv] : make_int2(0, 0);
+                spv[i] = c.path[base + dir * i];
+                siv[i] = piv[base + dir * i];      // written with the path entry (ivA of it)
             }
         }
         if (threadIdx.x == 0) bs.i[7] = 0;
