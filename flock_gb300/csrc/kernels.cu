@@ -2668,6 +2668,10 @@ struct BatchRunner {
     DevBuf d_cost, d_sd, d_desc, d_out, d_bfs, d_pot, d_sc, d_ws, d_ctr;
     HostBuf h_cost, h_sd, h_desc, h_out, h_sc, h_ctr;
     cudaStream_t st[kNumBuckets] = {};
+    // the first bucket's later staging chunks (its uploads and launches
+    // overlap the packing of the next chunk)
+    static constexpr int kStageChunks = 4;
+    cudaStream_t cst[kStageChunks - 1] = {};
     cudaEvent_t ev_start = nullptr, ev_done = nullptr, ev_join = nullptr;
     bool init = false;
     // per call
@@ -2691,6 +2695,7 @@ struct BatchRunner {
     int setup() {
         if (init) return FLOCK_OK;
         for (auto& s : st) FLOCK_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        for (auto& s : cst) FLOCK_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         FLOCK_CK(cudaEventCreate(&ev_start));
         FLOCK_CK(cudaEventCreate(&ev_done));
         FLOCK_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
@@ -2796,10 +2801,12 @@ struct BatchRunner {
     // pinned staging buffers (threads over instances), checking the cost
     // range in the same pass.  Returns false if an instance of the bucket
     // has a cost outside |c| <= 2^30 (flagged in cost_bad).
-    bool pack_bucket(int b) {
+    bool pack_bucket(int b) { return pack_range(b, 0, bstart[b + 1] - bstart[b]); }
+    // Pack instances [lo, hi) of bucket b (positions in its order).
+    bool pack_range(int b, int lo, int hi) {
         std::atomic<int> bad{0};
-        parallel_for(bstart[b + 1] - bstart[b], [&](int q) {
-            const int k = order_[bstart[b] + q];
+        parallel_for(hi - lo, [&](int q) {
+            const int k = order_[bstart[b] + lo + q];
             const int m = m_of[k], n = n_of[k], ldc = (n + 3) & ~3;
             int32_t* dst = h_cost.as<int32_t>() + cost_off[k];
             bool ok = true;
@@ -2835,12 +2842,12 @@ struct BatchRunner {
         return FLOCK_ERR_RANGE;
     }
 
-    // Pack and upload bucket b on stream s (its cost and quantity ranges are
-    // contiguous in both arenas).
-    int stage_bucket(int b, cudaStream_t s) {
-        if (bstart[b + 1] == bstart[b]) return FLOCK_OK;
-        if (!pack_bucket(b)) return cost_failure();
-        const int k0 = order_[bstart[b]], k1 = order_[bstart[b + 1] - 1];
+    // Pack and upload instances [lo, hi) of bucket b on stream s (their
+    // cost and quantity ranges are contiguous in both arenas).
+    int stage_range(int b, int lo, int hi, cudaStream_t s) {
+        if (hi <= lo) return FLOCK_OK;
+        if (!pack_range(b, lo, hi)) return cost_failure();
+        const int k0 = order_[bstart[b] + lo], k1 = order_[bstart[b] + hi - 1];
         const int64_t c0 = cost_off[k0], c1 = cost_off[k1] + (int64_t)m_of[k1] * ((n_of[k1] + 3) & ~3);
         const int64_t s0 = sd_off[k0], s1 = sd_off[k1] + V_of[k1];
         FLOCK_CK(cudaMemcpyAsync(d_cost.as<int32_t>() + c0, h_cost.as<int32_t>() + c0, (size_t)(c1 - c0) * 4,
@@ -2923,11 +2930,11 @@ struct BatchRunner {
 
     size_t bucket_smem(int b) { return launch_smem_bytes(bmaxV[b], bmaxM[b], stage_light(bmaxV[b], bmaxM[b])); }
 
-    int grid_for(int b, const TuneCfg& t, size_t smem, const void* fn) {
+    int grid_for(int b, const TuneCfg& t, size_t smem, const void* fn, int count = -1) {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, smem);
         if (per_sm < 1) per_sm = 1;
-        const int nb = bstart[b + 1] - bstart[b];
+        const int nb = count >= 0 ? count : bstart[b + 1] - bstart[b];
         return std::max(1, std::min(nb, per_sm * num_sms() * t.grid_mult));
     }
 
@@ -2965,23 +2972,43 @@ struct BatchRunner {
         cudaGraphExec_t exec[kNumBuckets] = {};
         bool live[kNumBuckets] = {};
         launches = 0;
+        bool chunked = false;     // the first bucket staged from the host goes in kStageChunks pieces
         // largest bucket first: its long solves start before the small ones
         for (int b = kNumBuckets - 1; b >= 0; b--) {
             const int nb = bstart[b + 1] - bstart[b];
             if (!nb || (only_bucket >= 0 && b != only_bucket)) continue;
             BatchArgs a = args_for(b);
             a.next = ctr(b);
-            if (stage && (rc = stage_bucket(b, st[b]))) return rc;
             if (cfg[b].persistent) {
                 const size_t smem = bucket_smem(b);
-                FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
                 const void* fn = bsolve_fn(cfg[b].threads);
-                void* kargs[] = {&a};
-                FLOCK_CK(cudaLaunchKernel(fn, dim3(grid_for(b, cfg[b], smem, fn)), dim3(cfg[b].threads), kargs, smem,
-                                          st[b]));
-                launches++;
+                // staged from the host: the first bucket in chunks on their own
+                // streams (each chunk's kernel starts once that chunk is
+                // packed and uploaded); the largest instances lead
+                const int K = stage && !chunked && nb >= 4 * kStageChunks ? kStageChunks : 1;
+                chunked |= stage;
+                for (int q = 0; q < K; q++) {
+                    const int lo = (int)((int64_t)nb * q / K), hi = (int)((int64_t)nb * (q + 1) / K);
+                    cudaStream_t sq = q == 0 ? st[b] : cst[q - 1];
+                    if (q > 0) FLOCK_CK(cudaStreamWaitEvent(sq, ev_start, 0));
+                    if (stage && (rc = stage_range(b, lo, hi, sq))) return rc;
+                    BatchArgs aq = a;
+                    aq.desc = a.desc + lo;
+                    aq.count = hi - lo;
+                    aq.next = ctr(b) + q;       // one work-stealing counter per chunk
+                    FLOCK_CK(cudaMemsetAsync(aq.next, 0, sizeof(int32_t), sq));
+                    void* kargs[] = {&aq};
+                    FLOCK_CK(cudaLaunchKernel(fn, dim3(grid_for(b, cfg[b], smem, fn, hi - lo)), dim3(cfg[b].threads),
+                                              kargs, smem, sq));
+                    launches++;
+                    if (q > 0) {
+                        FLOCK_CK(cudaEventRecord(ev_join, sq));
+                        FLOCK_CK(cudaStreamWaitEvent(st[b], ev_join, 0));
+                    }
+                }
                 continue;
             }
+            if (stage && (rc = stage_range(b, 0, nb, st[b]))) return rc;
             live[b] = true;
             FLOCK_CK(cudaMemsetAsync(a.next, 0, sizeof(int32_t), st[b]));
             k_bsetup<<<grid_for(b, cfg[b], 0, (const void*)k_bsetup), cfg[b].threads, 0, st[b]>>>(a);
