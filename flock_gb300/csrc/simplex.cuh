@@ -69,13 +69,62 @@ __device__ __forceinline__ int uf_find(int32_t* uf, int x) {
 }
 
 // ------------------------------------------------------------ start tree ---
+// Warp 0 (all its lanes) extends the tree from the queued vertices
+// order[qh, qt): level by level, each lane takes one queued vertex and claims
+// its positive-cell neighbours that no vertex has claimed yet (parent -2 ->
+// the vertex, by compare-and-swap), appending them to the queue; every
+// parent precedes its children in the queue.  On a forest each vertex is
+// claimed once; a second path to a vertex (a cycle among the positive cells)
+// shows as fewer claims than positive cells, which the caller checks.
+// Returns the new tail; *claims (lane 0) grows by the claims made.
+__device__ __forceinline__ int warp_extend(const Ctx& c, int qh, int qt, int* s_tail, int* claims) {
+    const int V = c.I.m + c.I.n;
+    const int lane = threadIdx.x & 31;
+    int mine = 0;
+    while (qh < qt) {                                 // warp-uniform
+        const int end = qt;
+        if (lane == 0) *s_tail = end;
+        __syncwarp();
+        for (int b0 = qh; b0 < end; b0 += 32) {
+            const int idx = b0 + lane;
+            if (idx >= end) continue;
+            const int p = c.order[idx];
+            if (!FLOCK_IN(p, V)) { fail_check(c.sc, 31); continue; }
+            const int dp = c.depth[p];
+            const int e1 = c.csr_start[p + 1];
+            for (int e = c.csr_start[p]; e < e1; e++) {
+                const int ch = c.csr_adj[e];
+                if (!FLOCK_IN(ch, V)) { fail_check(c.sc, 31); break; }
+                if (atomicCAS(&c.parent[ch], -2, p) != -2) continue;
+                c.depth[ch] = dp + 1;
+                const int slot = atomicAdd(s_tail, 1);
+                if (slot >= V) { fail_check(c.sc, 34); break; }
+                c.order[slot] = ch;
+                mine++;
+            }
+        }
+        __syncwarp();
+        qh = end;
+        qt = min(*s_tail, V);
+        __syncwarp();                                 // every lane read the tail before lane 0 resets it
+    }
+    mine = (int)__reduce_add_sync(0xffffffffu, (unsigned)mine);
+    if (lane == 0) *claims += mine;
+    return qt;
+}
+
 // Builds the strongly feasible start tree from the allocation list c.bfs_*.
 // If the list is not a feasible solution whose positive cells form a forest
-// (the reference's undefined Vogel case), the NW-corner solution is used.
+// (the reference's undefined Vogel case), the NW-corner solution is used:
+// a list that does not balance the supplies and demands is replaced before
+// the tree is built; a cycle among the positive cells shows after the
+// traversal (fewer claims than positive cells) and the build restarts from
+// the NW-corner list.
 __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
     const InstDev& I = c.I;
     const int m = I.m, n = I.n, V = m + n;
-    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.bsum[v] = 0; c.uf[v] = v; }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) c.bsum[v] = 0;
     if (threadIdx.x == 0) bs.i[0] = 0;
     __syncthreads();
     for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
@@ -88,15 +137,6 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
     for (int v = threadIdx.x; v < V; v += blockDim.x) {
         const int64_t want = v < m ? I.supply[v] : I.demand[v - m];
         if (c.bsum[v] != want) bs.i[0] = 1;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && !bs.i[0]) {
-        for (int k = 0; k < V - 1; k++) {
-            if (c.bfs_qty[k] <= 0) continue;
-            int ra = uf_find(c.uf, c.bfs_src[k]), rb = uf_find(c.uf, m + c.bfs_dst[k]);
-            if (ra == rb) { bs.i[0] = 1; break; }
-            c.uf[ra] = rb;
-        }
     }
     __syncthreads();
     if (bs.i[0]) {
@@ -128,114 +168,111 @@ __device__ void sf_init_cta(const Ctx& c, BlockScratch& bs) {
         if (M > ((int64_t)1 << 62) / (S + 2)) c.sc->status |= ST_RANGE;
     }
 
-    // CSR of positive cells (order[] holds degrees, then cursors)
-    for (int v = threadIdx.x; v < V; v += blockDim.x) c.order[v] = 0;
-    __syncthreads();
-    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
-        if (c.bfs_qty[k] <= 0 || c.bfs_src[k] < 0) continue;
-        atomicAdd(&c.order[c.bfs_src[k]], 1);
-        atomicAdd(&c.order[m + c.bfs_dst[k]], 1);
-    }
-    __syncthreads();
-    for (int v = threadIdx.x; v < V; v += blockDim.x) c.csr_start[v] = c.order[v];
-    __syncthreads();
-    const int32_t tot = block_exclusive_scan_i32(c.csr_start, V, bs);
-    if (threadIdx.x == 0) c.csr_start[V] = tot;
-    for (int v = threadIdx.x; v < V; v += blockDim.x) c.order[v] = c.csr_start[v];
-    __syncthreads();
-    for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
-        if (c.bfs_qty[k] <= 0 || c.bfs_src[k] < 0) continue;
-        const int a = c.bfs_src[k], b = m + c.bfs_dst[k];
-        c.csr_adj[atomicAdd(&c.order[a], 1)] = b;
-        c.csr_adj[atomicAdd(&c.order[b], 1)] = a;
-    }
-    for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = -2; c.depth[v] = 0; }
-    __syncthreads();
-
-    // components of the positive cells, attached to the tree built so far
-    if (threadIdx.x == 0) {
-        c.parent[root] = -1;
-        c.depth[root] = 0;
-        c.order[0] = root;
-        int qh = 0, qt = 1;
-        while (qh < qt) {
-            const int p = c.order[qh++];
-            for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
-                const int ch = c.csr_adj[e];
-                if (!FLOCK_IN(ch, V)) { fail_check(c.sc, 31); break; }
-                if (c.parent[ch] == -2 && ch != root) {
-                    if (qt >= V) { fail_check(c.sc, 34); break; }
-                    c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch;
-                }
-            }
-        }
-        bs.i[1] = 0;   // scan pointer
-        bs.i[2] = qt;  // queue tail
-    }
-    __syncthreads();
-    for (int guard = 0; guard <= V; guard++) {
-        if (threadIdx.x == 0) {
-            int w = bs.i[1];
-            while (w < V && (c.parent[w] != -2 || w == root || (w >= m && I.demand[w - m] == 0))) w++;
-            bs.i[1] = w;
-            int rc = -1;
-            if (w < V) {
-                if (w < m) rc = w;
-                else {
-                    for (int e = c.csr_start[w]; e < c.csr_start[w + 1]; e++) {
-                        const int x = c.csr_adj[e];
-                        if (x < m && (rc < 0 || x < rc)) rc = x;
-                    }
-                }
-            }
-            bs.i[3] = rc;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        // CSR of positive cells (order[] holds degrees, then cursors)
+        for (int v = threadIdx.x; v < V; v += blockDim.x) c.order[v] = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+            if (c.bfs_qty[k] <= 0 || c.bfs_src[k] < 0) continue;
+            atomicAdd(&c.order[c.bfs_src[k]], 1);
+            atomicAdd(&c.order[m + c.bfs_dst[k]], 1);
         }
         __syncthreads();
-        const int rc = bs.i[3];
-        if (rc < 0) break;
-        uint64_t best = kNoKey;
-        for (int j = threadIdx.x; j < n; j += blockDim.x)
-            if (c.parent[m + j] != -2) {
-                const uint64_t k = pack_i32(cost_of(I, rc, j), (uint32_t)j);
-                best = k < best ? k : best;
+        for (int v = threadIdx.x; v < V; v += blockDim.x) c.csr_start[v] = c.order[v];
+        __syncthreads();
+        const int32_t tot = block_exclusive_scan_i32(c.csr_start, V, bs);
+        if (threadIdx.x == 0) c.csr_start[V] = tot;
+        for (int v = threadIdx.x; v < V; v += blockDim.x) c.order[v] = c.csr_start[v];
+        __syncthreads();
+        for (int k = threadIdx.x; k < V - 1; k += blockDim.x) {
+            if (c.bfs_qty[k] <= 0 || c.bfs_src[k] < 0) continue;
+            const int a = c.bfs_src[k], b = m + c.bfs_dst[k];
+            c.csr_adj[atomicAdd(&c.order[a], 1)] = b;
+            c.csr_adj[atomicAdd(&c.order[b], 1)] = a;
+        }
+        for (int v = threadIdx.x; v < V; v += blockDim.x) { c.parent[v] = -2; c.depth[v] = 0; }
+        __syncthreads();
+
+        // components of the positive cells, attached to the tree built so far
+        if (warp == 0) {
+            if (lane == 0) {
+                c.parent[root] = -1;
+                c.depth[root] = 0;
+                c.order[0] = root;
+                bs.i[1] = 0;   // scan pointer
+                bs.i[6] = 0;   // claims
             }
-        best = block_min_u64(best, bs);
-        if (threadIdx.x == 0 && (best == kNoKey || !FLOCK_IN(rc, m) || bs.i[2] >= V)) fail_check(c.sc, 33);
-        if (threadIdx.x == 0 && !(best == kNoKey || !FLOCK_IN(rc, m) || bs.i[2] >= V)) {
-            const int js = m + (int)key_idx(best);
-            int qt = bs.i[2];
-            int qh = qt;
-            c.parent[rc] = js;
-            c.depth[rc] = c.depth[js] + 1;
-            c.order[qt++] = rc;
-            while (qh < qt) {
-                const int p = c.order[qh++];
-                for (int e = c.csr_start[p]; e < c.csr_start[p + 1]; e++) {
-                    const int ch = c.csr_adj[e];
-                    if (!FLOCK_IN(ch, V)) { fail_check(c.sc, 32); break; }
-                    if (c.parent[ch] == -2 && ch != root) {
-                        if (qt >= V) { fail_check(c.sc, 35); break; }
-                        c.parent[ch] = p; c.depth[ch] = c.depth[p] + 1; c.order[qt++] = ch;
+            __syncwarp();
+            const int qt = warp_extend(c, 0, 1, &bs.i[5], &bs.i[6]);
+            if (lane == 0) bs.i[2] = qt;   // queue tail
+        }
+        __syncthreads();
+        for (int guard = 0; guard <= V; guard++) {
+            if (threadIdx.x == 0) {
+                int w = bs.i[1];
+                while (w < V && (c.parent[w] != -2 || w == root || (w >= m && I.demand[w - m] == 0))) w++;
+                bs.i[1] = w;
+                int rc = -1;
+                if (w < V) {
+                    if (w < m) rc = w;
+                    else {
+                        for (int e = c.csr_start[w]; e < c.csr_start[w + 1]; e++) {
+                            const int x = c.csr_adj[e];
+                            if (x < m && (rc < 0 || x < rc)) rc = x;
+                        }
                     }
                 }
+                bs.i[3] = rc;
             }
-            bs.i[2] = qt;
+            __syncthreads();
+            const int rc = bs.i[3];
+            if (rc < 0) break;
+            uint64_t best = kNoKey;
+            for (int j = threadIdx.x; j < n; j += blockDim.x)
+                if (c.parent[m + j] != -2) {
+                    const uint64_t k = pack_i32(cost_of(I, rc, j), (uint32_t)j);
+                    best = k < best ? k : best;
+                }
+            best = block_min_u64(best, bs);
+            const bool ok = !(best == kNoKey || !FLOCK_IN(rc, m) || bs.i[2] >= V);   // block-uniform
+            if (threadIdx.x == 0 && !ok) fail_check(c.sc, 33);
+            if (ok && warp == 0) {
+                const int qt0 = bs.i[2];
+                if (lane == 0) {
+                    const int js = m + (int)key_idx(best);
+                    c.parent[rc] = js;
+                    c.depth[rc] = c.depth[js] + 1;
+                    c.order[qt0] = rc;
+                }
+                __syncwarp();
+                const int qt = warp_extend(c, qt0, qt0 + 1, &bs.i[5], &bs.i[6]);
+                if (lane == 0) bs.i[2] = qt;
+            }
+            __syncthreads();
+            if (!ok) break;
         }
+        // a forest has as many claims (vertices reached through positive
+        // cells) as positive cells; more cells means a cycle among them
+        const bool cycle = bs.i[6] != tot / 2;       // block-uniform: read after the barrier above
+        __syncthreads();
+        if (!cycle || attempt == 1) break;
+        if (threadIdx.x == 0) { nwc_thread0(c); c.sc->status |= ST_START_REPAIRED; }
         __syncthreads();
     }
 
     // perturbed flows, children before parents (reverse BFS order)
+    const int qt = bs.i[2];
+    for (int q = threadIdx.x; q < qt; q += blockDim.x) {
+        const int v = c.order[q];
+        int64_t b;
+        if (v < m) b = M * I.supply[v] + 1;
+        else if (v != root) b = -(M * I.demand[v - m] - 1);
+        else b = -(M * I.demand[v - m] + (v_alive - 1));
+        c.bsum[v] = b;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        const int qt = bs.i[2];
         if (qt != v_alive) c.sc->status |= ST_SF_FAIL;
-        for (int q = 0; q < qt; q++) {
-            const int v = c.order[q];
-            int64_t b;
-            if (v < m) b = M * I.supply[v] + 1;
-            else if (v != root) b = -(M * I.demand[v - m] - 1);
-            else b = -(M * I.demand[v - m] + (v_alive - 1));
-            c.bsum[v] = b;
-        }
         for (int q = qt - 1; q >= 1; q--) {
             const int v = c.order[q];
             const int p = c.parent[v];
