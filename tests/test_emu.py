@@ -84,9 +84,9 @@ def _emu_vogel_files(tmp_path, seed, count, shapes):
     return files, insts
 
 
-@pytest.mark.parametrize("threads,seed,variant", [(32, 1, "host"), (96, 3, "host"), (256, 4, "host"),
-                                                  (96, 5, "wide"), (256, 6, "wide")])
-def test_emulated_vogel_host(emu, tmp_path, threads, seed, variant):
+@pytest.mark.parametrize("threads,seed,variant,count", [(32, 1, "host", 25), (96, 3, "host", 25), (256, 4, "host", 10),
+                                                        (96, 5, "wide", 25), (256, 6, "wide", 10)])
+def test_emulated_vogel_host(emu, tmp_path, threads, seed, variant, count):
     """The "vam_host" Vogel (vogel_cta: cached top-2 crossings per line,
     rescans spread over the warps, long lines split; the staged form and the
     wide-instance form with batched loads and a column-major copy) on the
@@ -110,7 +110,7 @@ def test_emulated_vogel_host(emu, tmp_path, threads, seed, variant):
             return int(rng.integers(1, 6)), int(rng.integers(100, 200))
         return int(rng.integers(1, 50)), int(rng.integers(1, 50))
 
-    files, insts = _emu_vogel_files(tmp_path, seed, 25, shapes)
+    files, insts = _emu_vogel_files(tmp_path, seed, count, shapes)
     exe = os.path.join(EMU_DIR, "emu_vogel_device")
     r = subprocess.run([exe] + files, capture_output=True, text=True,
                        env=dict(os.environ, EMU_THREADS=str(threads), EMU_VOGEL=variant), timeout=600)
