@@ -46,7 +46,10 @@ namespace {
 constexpr int kServeMaxV = 4096;     // largest m + n solved by the group kernels
 constexpr int kSlots = 1 << 16;      // completion flags (requests in flight)
 constexpr int kDescCap = 1 << 17;    // descriptor pool entries
-constexpr int kStreams = 16;
+// launch streams: enough that a new group nearly always finds an idle one
+// (a group queued behind a long-running launch on a busy stream waits for it)
+constexpr int kStreams = 64;
+constexpr int kUrgentV = 512;        // size classes launched on the high-priority streams
 
 using Clock = std::chrono::steady_clock;
 
@@ -140,7 +143,7 @@ struct flock_server {
     cudaStream_t up = nullptr, down = nullptr;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> stream_last;
-    int rr = 0;
+    int rr = 0, rr_hi = 0;
 
     static int64_t request_bytes(int m, int n) {
         if (m + n > kServeMaxV) return plain_bytes(m, n);
@@ -170,8 +173,16 @@ struct flock_server {
         const int ns = std::max(kStreams, cfg.max_inflight_batches);
         streams.resize(ns);
         stream_last.assign(ns, nullptr);
-        for (auto& st : streams)
-            if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+        // the first half of the pool at the highest priority, for the size
+        // classes up to kUrgentV: their blocks are scheduled ahead of the
+        // larger classes' waiting blocks, so short requests do not queue
+        // behind long ones
+        int lo_pri = 0, hi_pri = 0;
+        if ((e = cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri)) != cudaSuccess) return fail(e, "stream priorities");
+        for (int k = 0; k < ns; k++)
+            if ((e = cudaStreamCreateWithPriority(&streams[k], cudaStreamNonBlocking, k < ns / 2 ? hi_pri : lo_pri)) !=
+                cudaSuccess)
+                return fail(e, "stream");
         const int rc = flock::serve_init();
         if (rc) return rc;
         dev_ready = true;
@@ -183,14 +194,18 @@ struct flock_server {
         return FLOCK_ERR_CUDA;
     }
 
-    // An idle stream of the pool (its last launch finished), else the next one.
-    int pick_stream() {
-        for (size_t k = 0; k < streams.size(); k++) {
-            const int s = (rr + (int)k) % (int)streams.size();
-            if (!stream_last[s] || cudaEventQuery(stream_last[s]) == cudaSuccess) { rr = s + 1; return s; }
+    // An idle stream of the pool half for the launch's priority (urgent: the
+    // first half) whose last launch finished, else the half's next one.
+    int pick_stream(bool urgent) {
+        const int half = (int)streams.size() / 2;
+        const int base = urgent ? 0 : half, cnt = urgent ? half : (int)streams.size() - half;
+        int& r = urgent ? rr_hi : rr;
+        for (int k = 0; k < cnt; k++) {
+            const int s = base + (r + k) % cnt;
+            if (!stream_last[s] || cudaEventQuery(stream_last[s]) == cudaSuccess) { r = s - base + 1; return s; }
         }
-        const int s = rr % (int)streams.size();
-        rr = s + 1;
+        const int s = base + r % cnt;
+        r = s - base + 1;
         return s;
     }
 
@@ -262,7 +277,7 @@ struct flock_server {
                                  up)) != cudaSuccess) return fail(e, "descriptor upload");
         if ((e = cudaMemsetAsync(d_next + doff, 0, sizeof(int32_t), up)) != cudaSuccess) return fail(e, "counter reset");
         if ((e = cudaEventRecord(G.ev, up)) != cudaSuccess) return fail(e, "event");
-        const int s = pick_stream();
+        const int s = pick_stream(maxV <= kUrgentV);
         if ((e = cudaStreamWaitEvent(streams[s], G.ev, 0)) != cudaSuccess) return fail(e, "stream wait");
         const int rc = flock::serve_launch(d_desc + doff, (int)g.size(), maxV, maxM, cfg.options, d_next + doff, streams[s]);
         if (rc) return rc;

@@ -244,7 +244,7 @@ int flock_batch_solve(int32_t count, const flock_instance* insts, const flock_op
 typedef struct flock_server flock_server;
 typedef struct {
     int64_t memory_budget_bytes;   /* resident device state allowed (default 40 GiB) */
-    int32_t max_inflight_batches;  /* launch streams (at least 16 are used), default 16 */
+    int32_t max_inflight_batches;  /* launch streams (at least 64 are used), default 16 */
     int32_t max_batch;             /* instances admitted per launch group, default 512 */
     flock_options options;
 } flock_server_config;
