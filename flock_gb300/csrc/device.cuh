@@ -53,7 +53,7 @@ constexpr int kPPRows = 128;     // partial pricing: capacity of the candidate-r
 constexpr int kPPSmallV = 1024;
 constexpr int kPPRowsSmall = 32, kPPRefreshSmall = 8;
 constexpr int kPPRowsLarge = 64, kPPRefreshLarge = 32;
-// The plain solver's grid path (4096 vertices and more), whose candidate
+// The plain solver's grid path (2400 vertices and more), whose candidate
 // rounds run inside one thread-block cluster: a longer candidate list picks
 // better entering cells (fewer pivots) and costs little there (8000 x 8000
 // Euclidean: 57,815 pivots in 1.50 s with 64 rows / 32 rounds, 53,784 in

@@ -453,7 +453,20 @@ struct GridPivot {
     int2 Q, O;
 };
 
-constexpr int kGridPivotV = 4096;     // plain instances with m + n >= this use the grid round
+// plain instances with m + n >= this use the grid round (its cluster rounds
+// beat one CTA from about 2400 vertices: 1500 x 1000 uniform 82 vs 98 ms,
+// 2000 x 2000 180 vs 299 ms; 1000 x 1000 Euclidean 77 vs 67 ms)
+constexpr int kGridPivotV = 2400;
+// The grid-round threshold in effect (FLOCK_GRID_V overrides kGridPivotV, for
+// tuning; at least 64).
+static int grid_pivot_v() {
+    static const int v = [] {
+        const char* e = getenv("FLOCK_GRID_V");
+        const int x = e ? atoi(e) : 0;
+        return x >= 64 ? x : kGridPivotV;
+    }();
+    return v;
+}
 
 __device__ __forceinline__ const int2* iv_now(const Ctx& c, int V) { return c.iv + (c.sc->ivp ? V : 0); }
 
@@ -2218,7 +2231,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                                                                                                   : FLOCK_BFS_VOGEL;
     // the one-launch form below the grid size (the stepping-stone mode runs
     // its rounds on the round kernel at every size)
-    if (V < kGridPivotV && bfs != FLOCK_BFS_VOGEL_DEVICE && pivot_mode(opt) != 3)
+    if (V < grid_pivot_v() && bfs != FLOCK_BFS_VOGEL_DEVICE && pivot_mode(opt) != 3)
         return solve_one_launch(P, I, opt, bfs, max_rounds, flows, du, dv, st, t0);
     Ctx c;
     int32_t* out3 = nullptr;
@@ -2226,9 +2239,9 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     // the grid path's sweeps read 16-bit costs when every cost fits
     // (FLOCK_COST16=0 keeps them on the int32 costs)
     const char* c16_env = getenv("FLOCK_COST16");
-    if (fits16 && V >= kGridPivotV && !(c16_env && !strcmp(c16_env, "0"))) P.narrow_copy(c);
+    if (fits16 && V >= grid_pivot_v() && !(c16_env && !strcmp(c16_env, "0"))) P.narrow_copy(c);
     // partial pricing runs on the plain path from kGridPivotV vertices (grid rounds)
-    const bool partial = pricing_of(opt) && V >= kGridPivotV;
+    const bool partial = pricing_of(opt) && V >= grid_pivot_v();
     if ((rc = P.reset_scalars(c.sc, pivot_mode(opt), max_rounds, partial))) return rc;
     FLOCK_CK(cudaMemsetAsync(P.ph, 0, sizeof(PhaseClock), P.stream));
     c.ph = P.ph;
@@ -2247,7 +2260,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
     Scalars* hs = P.h_sc.as<Scalars>();
     // the grid rounds apply single pivots: the parallel stepping stone's
     // multi-pivot rounds run on one block at every size
-    if (V >= kGridPivotV && pivot_mode(opt) != 3) {
+    if (V >= grid_pivot_v() && pivot_mode(opt) != 3) {
         // large instance: the pivot round over the whole GPU, chunks of
         // rounds captured once as a CUDA graph
         FLOCK_CK(cudaMemsetAsync(P.gp, 0, sizeof(GridPivot), P.stream));

@@ -91,9 +91,9 @@ enum { FLOCK_PIVOT_SEQUENTIAL = 0, FLOCK_PIVOT_PARALLEL = 1, FLOCK_PIVOT_SWITCH 
  * costs as candidates and the following rounds re-price only those rows,
  * until they hold no negative reduced cost or K rounds have passed;
  * optimality is only declared after a full sweep.  R / K: 32 / 8 for
- * instances of up to 1024 vertices, 64 / 32 up to 4095 (batched and served
- * forms, the plain one-launch solve), 128 / 64 for the plain solver from 4096
- * vertices.  The optimum is the same; the pivot sequence differs.  FLOCK_PIVOT_SS
+ * instances of up to 1024 vertices, 64 / 32 above (batched and served forms,
+ * the plain one-launch solve below 2400 vertices), 128 / 64 for the plain
+ * solver from 2400 vertices (its grid and cluster rounds).  The optimum is the same; the pivot sequence differs.  FLOCK_PIVOT_SS
  * always prices fully. */
 enum { FLOCK_PRICING_FULL = 0, FLOCK_PRICING_PARTIAL = 1 };
 
