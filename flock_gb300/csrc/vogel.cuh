@@ -57,7 +57,8 @@ __device__ __forceinline__ bool top2_valid(const Ctx& c, int L, int4 t) {
 
 // This thread's share (crossing indices first, first + step, ...) of line
 // L's two cheapest uncovered crossing cells.  kWide (instances whose line
-// state is in global memory): four crossings' loads issued together, and a
+// state is in global memory): eight (four along a column read row by row)
+// crossings' loads issued together, and a
 // column read from the column-major copy costT (n rows of ceil4(m)) when
 // there is one, instead of one row per element.
 template <bool kWide>
@@ -72,14 +73,16 @@ __device__ __forceinline__ void vogel_scan(const Ctx& c, int L, int first, int s
     else if (kWide && costT) { line = costT + (size_t)(L - I.m) * ((I.m + 3) & ~3); cov = c.covered; len = I.m; }
     if (line) {
         if (kWide) {
+            // eight crossings' loads in flight (a rescan's stride leaves a lane
+            // about len / (32 g) crossings: one or two batches at 8000)
             int x = first;
-            for (; x + 3 * step < len; x += 4 * step) {
-                int32_t cv[4];
-                uint8_t cc[4];
+            for (; x + 7 * step < len; x += 8 * step) {
+                int32_t cv[8];
+                uint8_t cc[8];
                 #pragma unroll
-                for (int u = 0; u < 4; u++) { cv[u] = line[x + u * step]; cc[u] = cov[x + u * step]; }
+                for (int u = 0; u < 8; u++) { cv[u] = line[x + u * step]; cc[u] = cov[x + u * step]; }
                 #pragma unroll
-                for (int u = 0; u < 4; u++)
+                for (int u = 0; u < 8; u++)
                     if (!cc[u]) top2_insert(a1, a2, pack_i32(cv[u], (uint32_t)(x + u * step)));
             }
             for (; x < len; x += step)
