@@ -248,7 +248,11 @@ __device__ uint64_t vogel_refresh_max(const Ctx& c, int lo, int hi, int ctr, uin
             const int L = (int)key_idx(all);
             bs.red[0] = x;
             bs.red2[0] = all;
-            bs.i[9] = top2_valid(c, L, c.top2[L]) ? 0 : 1;
+            // an uncovered line of the half just refreshed has an exact cache
+            // (checked or rebuilt above): the wide form reads the cache only
+            // for a line of the other half or a covered one (penalty -1)
+            const bool check = !kWide || other > x || key_val(all) == -1;
+            bs.i[9] = check && !top2_valid(c, L, c.top2[L]) ? 1 : 0;
             bs.i[ctr] = 0;                   // every thread read it before the barrier above
         }
     }
