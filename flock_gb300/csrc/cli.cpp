@@ -40,7 +40,7 @@ int main(int argc, char** argv) {
         return 255;
     }
     if (algo == "cpu_lp_solve") {
-        log_error("cpu_lp_solve needs Gurobi, which this build does not include");
+        log_error("cpu_lp_solve needs Gurobi, which this library does not include");
         return 254;
     }
     if (algo != "parallel_uv" && algo != "parallel_ss" && algo != "switch_hybrid") {

@@ -110,6 +110,6 @@ public:
     int totalIterations = 0;
     double totalSolveTime = 0;
     lpModel(ProblemInstance* problem, flowInformation* flows) : data(problem), optimal_flows(flows) {}
-    void execute() { throw flock_error(FLOCK_ERR_ARG, "cpu_lp_solve needs Gurobi, which this build does not include"); }
+    void execute() { throw flock_error(FLOCK_ERR_ARG, "cpu_lp_solve needs Gurobi, which this library does not include"); }
     void create_flows() {}
 };
