@@ -2948,7 +2948,18 @@ struct BatchRunner {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, smem);
         if (per_sm < 1) per_sm = 1;
         const int nb = count >= 0 ? count : bstart[b + 1] - bstart[b];
-        return std::max(1, std::min(nb, per_sm * num_sms() * t.grid_mult));
+        int g = std::max(1, std::min(nb, per_sm * num_sms() * t.grid_mult));
+        // FLOCK_GRID_CAP="b:g,...": at most g blocks for bucket b (diagnostics)
+        if (const char* e = getenv("FLOCK_GRID_CAP")) {
+            for (const char* p = e; *p;) {
+                int bb = -1, gg = 0, used = 0;
+                if (sscanf(p, "%d:%d%n", &bb, &gg, &used) != 2) break;
+                if (bb == b && gg >= 1) g = std::min(g, gg);
+                p += used;
+                if (*p == ',') p++;
+            }
+        }
+        return g;
     }
 
     // Pricing rounds of bucket b as a CUDA graph: `chunk` x (zero the
