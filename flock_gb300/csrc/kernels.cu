@@ -1122,18 +1122,24 @@ __device__ uint64_t cluster_cand_sweep(const Ctx& c, const int32_t* prow, int pn
 constexpr int kPathCache = 8192;
 constexpr size_t kCRoundSmem = (size_t)kPathCache * (sizeof(int2) + sizeof(int32_t));
 
-// full_first: round 0 is the pivot of the full round that k_gchoose_all has
-// just priced and counted (its entering cell in gp->best, every row key
-// current); its update clears every row key for the coming candidate sweeps.
+// full_first: round 0 is the full round that the bulk sweep has just priced
+// (every row key current): the cluster chooses its entering cell and the
+// next candidate rows (select_candidate_rows' rule), counts it, pivots, and
+// the update clears every row key for the coming candidate sweeps.  (gp: the
+// grid rounds' block, unused by this form.)
 template <bool kOne>
 __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivot* cp, const GridPivot* gp,
                                                               int full_first) {
+    (void)gp;
     __shared__ BlockScratch bs;
     __shared__ PhaseLocal phl;
     // this CTA's share of the round's cluster-wide minima, read by warp 0 of
     // every CTA through distributed shared memory (s_red: the results)
     __shared__ uint64_t x_best, x_mk, x_ml, x_pick, s_red[2];
     __shared__ int32_t s_prow[kPPRows];    // the candidate rows: fixed for the launch
+    // the full round's candidate selection: this CTA's smallest key value,
+    // histogram and count of kept rows, read through distributed shared memory
+    __shared__ int32_t x_rmin, x_hist[32], x_cnt, s_sel[3], s_wsum[32];
     extern __shared__ __align__(16) unsigned char cr_smem[];
     int2* siv = reinterpret_cast<int2*>(cr_smem);
     int32_t* spv = reinterpret_cast<int32_t*>(siv + kPathCache);
@@ -1142,17 +1148,146 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     const int m = c.I.m, V = m + c.I.n;
     // the solve's scalars, read by every CTA before any CTA can change them
     const int done0 = c.sc->done;
-    const int pn = min(max(c.sc->pp_n, 0), kPPRows);
+    int pn = min(max(c.sc->pp_n, 0), kPPRows);
     const int refresh = max(c.sc->pp_refresh, 1);
     const int max_rounds = c.sc->max_rounds;
     int rounds = c.sc->rounds, age = c.sc->pp_age, pivots = c.sc->pivots, ivp = c.sc->ivp, nwide = c.sc->nwide;
     const int pivots0 = pivots;
     const bool partial = c.sc->pricing != 0;
-    const uint64_t full_best = full_first ? gp->best : kNoKey;
+    const int lane = threadIdx.x & 31;
+    uint64_t full_best = kNoKey;
+    bool optimal = false;
+    if (full_first && !done0) {
+        // The full round's entering cell and candidate rows (the full sweep
+        // has just priced every row): select_candidate_rows' rule over the
+        // cluster.  CTA q takes a contiguous range of rows, a thread a
+        // contiguous chunk of it (row order = thread order); the smallest
+        // key value, the 32-bin histogram and the kept rows' counts are
+        // combined across the CTAs through distributed shared memory.
+        const int ncols = c.I.n;
+        const int per = (m + nctas - 1) / nctas, r0 = min(m, rank * per), r1 = min(m, r0 + per);
+        const int chunk = (r1 - r0 + (int)blockDim.x - 1) / (int)blockDim.x;
+        const int t0 = min(r1, r0 + (int)threadIdx.x * chunk), t1 = min(r1, t0 + chunk);
+        uint64_t pb = kNoKey;
+        int32_t rmn = 0;
+        int bad = 0;
+        for (int i = t0; i < t1; i++) {
+            const uint64_t k = c.row_best[i];
+            const int32_t v = key_val(k);
+            rmn = min(rmn, v);
+            if (k != kNoKey && v < 0) {
+                if ((int)key_idx(k) >= ncols) { bad = 1; continue; }
+                const uint64_t P = pack_i32(v, (uint32_t)i);
+                pb = P < pb ? P : pb;
+            }
+        }
+        if (bad) fail_check(c.sc, 18);
+        pb = block_min_u64(pb, bs);
+        rmn = key_val(block_min_u64(pack_i32(rmn, 0u), bs));
+        if (threadIdx.x == 0) { x_best = pb; x_rmin = rmn; }
+        if (threadIdx.x < 32) x_hist[threadIdx.x] = 0;
+        cluster_sync_all();                                      // selection barrier 1
+        if (threadIdx.x < 32) {
+            const uint64_t b = warp_min_u64(lane < nctas ? dsmem_ld_u64(dsmem_of(&x_best, lane)) : kNoKey);
+            int32_t rq = 0;
+            if (lane < nctas) {
+                uint32_t a = dsmem_of(&x_rmin, lane), r;
+                asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+                rq = (int32_t)r;
+            }
+            const int32_t rm = key_val(warp_min_u64(pack_i32(rq, 0u)));
+            if (lane == 0) { s_red[0] = b; s_sel[0] = rm; }
+        }
+        __syncthreads();
+        full_best = s_red[0];
+        const int32_t rmin = s_sel[0];
+        const int64_t span = rmin < 0 ? -(int64_t)rmin : 1;
+        if (rmin < 0)
+            for (int i = t0; i < t1; i++) {
+                const int32_t v = key_val(c.row_best[i]);
+                if (v < 0) atomicAdd(&x_hist[((int64_t)v - rmin) * 32 / span], 1);
+            }
+        __syncthreads();
+        cluster_sync_all();                                      // selection barrier 2: every histogram complete
+        const int cap = min(max(c.sc->pp_rows, 1), kPPRows);
+        if (threadIdx.x < 32) {
+            int h = 0;
+            for (int q = 0; q < nctas; q++) {
+                uint32_t a = dsmem_of(&x_hist[lane], q), r;
+                asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+                h += (int)r;
+            }
+            s_wsum[lane] = h;
+            __syncwarp();
+            if (lane == 0) {
+                int last = -1;
+                if (rmin < 0) {
+                    int cum = s_wsum[0];
+                    last = 0;
+                    for (int b = 1; b < 32 && cum + s_wsum[b] <= cap; b++) { cum += s_wsum[b]; last = b; }
+                }
+                s_sel[1] = last;
+            }
+        }
+        __syncthreads();
+        const int last = s_sel[1];
+        // this thread's kept rows, then their positions in row order
+        int mine = 0;
+        if (last >= 0)
+            for (int i = t0; i < t1; i++) {
+                const int32_t v = key_val(c.row_best[i]);
+                mine += v < 0 && ((int64_t)v - rmin) * 32 / span <= last;
+            }
+        int incl = mine;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        if (lane == 31) s_wsum[w] = incl;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int x = lane < nw ? s_wsum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane < nw) s_wsum[lane] = x;              // inclusive per-warp sums
+            if (lane == 31) x_cnt = x;                    // this CTA's kept rows
+        }
+        __syncthreads();
+        const int before_w = (w > 0 ? s_wsum[w - 1] : 0) + incl - mine;
+        cluster_sync_all();                                      // selection barrier 3: every count complete
+        if (threadIdx.x < 32) {
+            int cq = 0;
+            if (lane < nctas) {
+                uint32_t a = dsmem_of(&x_cnt, lane), r;
+                asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+                cq = (int)r;
+            }
+            const int lower = (int)__reduce_add_sync(0xffffffffu, lane < rank ? (unsigned)cq : 0u);
+            const int total = (int)__reduce_add_sync(0xffffffffu, (unsigned)cq);
+            if (lane == 0) { s_sel[0] = lower; s_sel[2] = total; }
+        }
+        __syncthreads();
+        int slot = s_sel[0] + before_w;
+        if (last >= 0)
+            for (int i = t0; i < t1; i++) {
+                const int32_t v = key_val(c.row_best[i]);
+                if (v < 0 && ((int64_t)v - rmin) * 32 / span <= last) {
+                    if (slot < cap) c.prow[slot] = i;
+                    slot++;
+                }
+            }
+        pn = min(s_sel[2], cap);
+        rounds++;                    // the full round
+        age = 1;                     // a full sweep resets the age; this round counts
+        optimal = full_best == kNoKey;
+        cluster_sync_all();                                      // selection barrier 4: every kept row written
+    }
     for (int t = threadIdx.x; t < pn; t += blockDim.x) s_prow[t] = c.prow[t];   // visible after barrier 0
     if (rank == 0 && threadIdx.x == 0) { cp->abort[0] = 0; cp->abort[1] = 0; }
     if (threadIdx.x == 0) cp->dwide[rank] = 0;
-    const int lane = threadIdx.x & 31;
     const int v0 = rank * blockDim.x + threadIdx.x, stride = nctas * blockDim.x;
     OwnVertex own;
     if (kOne) own_load(c, own, v0, c.iv + (ivp ? V : 0));
@@ -1169,7 +1304,7 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
             if (cp->abort[(r - 1) & 1]) { why = kFailed; break; }
         }
         const bool full_round = full_first && r == 0;   // the same in every CTA
-        if (done0 || (!full_round && (!partial || pn <= 0))) { why = kAged; break; }
+        if (done0 || optimal || (!full_round && (!partial || pn <= 0))) { why = kAged; break; }
         if (!full_round && rounds >= max_rounds) { why = kCapped; break; }
         if (!full_round && age >= refresh) { why = kAged; break; }
         ps.mark(PH_SWEEP);
@@ -1298,6 +1433,11 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
             }
     }
     if (rank == 0 && threadIdx.x == 0 && !done0) {
+        if (full_first) {            // the full round's selection (select_candidate_rows' scalars)
+            c.sc->pp_n = pn;
+            c.sc->ncand = optimal ? 0 : 1;
+            if (optimal) c.sc->done = 1;
+        }
         c.sc->rounds = rounds;
         c.sc->pp_age = why == kExhausted ? refresh : age;     // the next round sweeps every row
         c.sc->pivots = pivots;
@@ -2298,8 +2438,8 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
                 for (int r = 0; r < chunk; r++) {
                     if (clustered) {
                         // the cluster rounds leave only full sweeps to the grid: the bulk-copy sweep
+                        // (the full round's entering cell and candidate rows are chosen in the cluster)
                         k_sweep<<<bgrid, kBulkThreads, kBulkSmem, P.stream>>>(c, btile, bntile);
-                        k_gchoose_all<<<1, 1024, 0, P.stream>>>(c, P.gp);
                     } else {
                         k_gsweep<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
                         if (partial) k_gsweep_rest<<<grid, kSweepThreads, 0, P.stream>>>(c, P.gp, tile, ntile);
