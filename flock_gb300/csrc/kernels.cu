@@ -294,6 +294,9 @@ __global__ void __launch_bounds__(kBulkThreads, 1) k_sweep(Ctx c, int tile, int 
     __shared__ __align__(8) uint64_t vbar;
     __shared__ PhaseLocal phl;
     extern __shared__ __align__(128) unsigned char bulk_smem[];
+    // the cluster rounds that follow may be scheduled now; they wait for
+    // this grid's completion before they read anything
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     PhaseScope ps(c.ph, &phl, PH_SWEEP);
     if (c.sc->done) { ps.idle(); return; }
     const InstDev& I = c.I;
@@ -1143,6 +1146,10 @@ __global__ void __launch_bounds__(kCRoundThreads, 1) k_cround(Ctx c, ClusterPivo
     extern __shared__ __align__(16) unsigned char cr_smem[];
     int2* siv = reinterpret_cast<int2*>(cr_smem);
     int32_t* spv = reinterpret_cast<int32_t*>(siv + kPathCache);
+    // launched as the full sweep's programmatic dependent: the cluster is
+    // scheduled while the sweep drains, and waits here for its completion
+    // (and its writes) before reading anything
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     PhaseScope ps(c.ph, &phl, PH_SWEEP);
     const int rank = cluster_rank(), nctas = cluster_ctas();
     const int m = c.I.m, V = m + c.I.n;
@@ -2415,7 +2422,7 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
         const char* form = getenv("FLOCK_GRID_FORM");
         const bool clustered = partial && P.cluster_ctas >= 2 && !(form && !strcmp(form, "rounds"));
         cudaLaunchConfig_t ccfg = {};
-        cudaLaunchAttribute cattr[1];
+        cudaLaunchAttribute cattr[2];
         ccfg.gridDim = dim3(P.cluster_ctas);
         ccfg.blockDim = dim3(kCRoundThreads);
         ccfg.dynamicSmemBytes = kCRoundSmem;
@@ -2425,7 +2432,12 @@ static int solve_plain(const flock_instance* I, const flock_options* opt_in, flo
         cattr[0].val.clusterDim.y = 1;
         cattr[0].val.clusterDim.z = 1;
         ccfg.attrs = cattr;
-        ccfg.numAttrs = 1;
+        // the cluster launch is the full sweep's programmatic dependent
+        // (FLOCK_PDL=0: an ordinary stream dependency)
+        cattr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        cattr[1].val.programmaticStreamSerializationAllowed = 1;
+        const char* pdl_env = getenv("FLOCK_PDL");
+        ccfg.numAttrs = pdl_env && !strcmp(pdl_env, "0") ? 1 : 2;
         int chunk = clustered ? 2 : 8;
         cudaGraphExec_t exec = nullptr;
         int exec_chunk = 0;
